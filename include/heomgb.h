@@ -1,0 +1,166 @@
+/* heomgb.h -- C ABI of the GB300-native HEOM propagation engine.
+ *
+ * Drop-in for libheom's propagation path: the heom_hilb / heom_liou / heom_ado
+ * models built from H, the bath couplings V, the exponential noise
+ * decomposition and the hierarchy depth, stepped by rk4 / lsrk4 / rkdp through
+ * qme_solver.  Each entry point names the reference interface it replaces
+ * (file:line in the libheom tree).  Plain pointers and sizes only; complex
+ * numbers are two doubles (re, im); matrices are row-major (the reference's
+ * `row_major` order).  Every call returns a heomgb_status; nothing exits the
+ * process (the reference's CUDA_CALL/std::exit is replaced by status codes).
+ *
+ * Threading: one qme / solver object must not be used from two host threads
+ * at once (the reference's engines are not re-entrant either).
+ */
+#ifndef HEOMGB_H
+#define HEOMGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum heomgb_status {
+  HEOMGB_OK = 0,
+  HEOMGB_ERR_INVALID_ARGUMENT = 1, /* bad size, index, null pointer, missing kwarg   */
+  HEOMGB_ERR_STATE = 2,            /* call out of order (e.g. solve before set_param) */
+  HEOMGB_ERR_CUDA = 3,             /* CUDA runtime error (message via last_error)     */
+  HEOMGB_ERR_ALLOC = 4,            /* device or host allocation failed                */
+  HEOMGB_ERR_UNSUPPORTED = 5,      /* option outside what this build implements       */
+  HEOMGB_ERR_NUMERIC = 6,          /* non-finite step-size control / attempt cap hit  */
+  HEOMGB_ERR_CAPACITY = 7          /* request above a documented fixed maximum        */
+} heomgb_status;
+
+/* Model forms: heom_hilb (heom_hilb.h:18-216), heom_liou (heom_liou.h:18-259),
+ * heom_ado (heom_ado.h:18-204). */
+typedef enum heomgb_form { HEOMGB_HILB = 0, HEOMGB_LIOU = 1, HEOMGB_ADO = 2 } heomgb_form;
+
+/* Integrators: rk4 (solver/rk4.h:15-66), lsrk4 (solver/lsrk4.h:15-48),
+ * rkdp (solver/rkdp.h:15-180). */
+typedef enum heomgb_solver_kind { HEOMGB_RK4 = 0, HEOMGB_LSRK4 = 1, HEOMGB_RKDP = 2 } heomgb_solver_kind;
+
+/* Arithmetic of the right-hand side.  FP64: everything in double (the plain
+ * drop-in).  MIXED: the bulk complex products and the stage inputs in FP32,
+ * while the state vector, stage accumulation, error norm and step control
+ * stay FP64. */
+typedef enum heomgb_precision { HEOMGB_FP64 = 0, HEOMGB_MIXED = 1 } heomgb_precision;
+
+typedef struct heomgb_qme heomgb_qme;
+typedef struct heomgb_solver heomgb_solver;
+typedef struct heomgb_qme_solver heomgb_qme_solver;
+
+/* The reference's kwargs_t (type.h:49) with the keys its solvers read:
+ * "dt" (fixed_step_size_solver.h:37, adaptive_step_size_solver.h:40),
+ * "atol", "rtol" (adaptive_step_size_solver.h:42-43).  A key the solver needs
+ * but whose has_* flag is 0 gives HEOMGB_ERR_INVALID_ARGUMENT (the reference
+ * throws std::out_of_range). */
+typedef struct heomgb_kwargs {
+  double dt, atol, rtol;
+  int has_dt, has_atol, has_rtol;
+} heomgb_kwargs;
+
+/* Called at every output time, as solver_base::solve does (solver_base.h:72-78). */
+typedef void (*heomgb_callback)(double t, void* user);
+
+/* ---- diagnostics -------------------------------------------------------- */
+const char* heomgb_last_error(void);             /* thread-local message of the last failure */
+const char* heomgb_version(void);
+int heomgb_abi_version(void);
+/* Number of kernels this library has launched so far (graph nodes included). */
+long long heomgb_launch_count(void);
+
+/* ---- model (qme) --------------------------------------------------------- */
+/* heom_hilb/heom_liou/heom_ado(int max_depth, int n_inner_threads,
+ * int n_outer_threads) -- heom_hilb.h:41-43, heom.h:44-50.  The thread counts
+ * are accepted for interface parity; the device path does not use them. */
+heomgb_status heomgb_qme_create(heomgb_form form, int max_depth, int n_inner_threads, int n_outer_threads,
+                                heomgb_qme** out);
+heomgb_status heomgb_qme_destroy(heomgb_qme* q);
+
+/* Public members n_level / n_level_2 / H (qme_base.h:32-36).  H: n*n complex. */
+heomgb_status heomgb_qme_set_hamiltonian(heomgb_qme* q, int n_level, const double* H);
+/* alloc_noises(n_noise) -- qme_base.h:47-60. */
+heomgb_status heomgb_qme_alloc_noises(heomgb_qme* q, int n_noise);
+/* V[u], len_gamma[u], gamma[u], phi_0[u], sigma[u], S[u], A[u], s_delta[u]
+ * (qme_base.h:38-45).  V: n*n, gamma/S/A: len*len, phi_0/sigma: len, s_delta: 1
+ * complex.  Off-diagonal gamma entries are accepted and, as in the reference
+ * (heom.h:110 clears gamma[u] before reading them), never contribute. */
+heomgb_status heomgb_qme_set_noise(heomgb_qme* q, int u, const double* V, int len_gamma, const double* gamma,
+                                   const double* phi_0, const double* sigma, const double* S, const double* A,
+                                   const double* s_delta);
+heomgb_status heomgb_qme_set_precision(heomgb_qme* q, heomgb_precision p);
+/* Run the model's CUDA work on this stream (a cudaStream_t); NULL restores the
+ * library's own stream.  Must precede heomgb_qme_solver_create to affect it. */
+heomgb_status heomgb_qme_set_stream(heomgb_qme* q, void* cuda_stream);
+/* set_param(engine) -- heom_hilb.h:57-68 / heom.h:57-139 / heom_liou.h:66-119 /
+ * heom_ado.h:62-189.  Builds the hierarchy tables on the device, uploads H/V and
+ * the per-ADO damping, and builds the superoperators of the Liouville forms. */
+heomgb_status heomgb_qme_set_param(heomgb_qme* q);
+/* get_n_hrchy() -- heom.h:52-55. */
+heomgb_status heomgb_qme_get_n_hrchy(const heomgb_qme* q, int* n_hrchy);
+/* Number of linear noise modes (hs.n_dim, heom.h:62-63). */
+heomgb_status heomgb_qme_get_n_dim(const heomgb_qme* q, int* n_dim);
+/* main_size() = n_level^2 * n_hrchy -- heom_hilb.h:45-49. */
+heomgb_status heomgb_qme_main_size(const heomgb_qme* q, long long* size);
+/* Hierarchy tables hs.n, hs.ptr_p1, hs.ptr_m1 (hrchy_space.h:18-27), copied
+ * from the device: n is n_hrchy*n_dim, ptr_p1/ptr_m1 are (n_hrchy+1)*n_dim
+ * with the sentinel ptr_void = n_hrchy.  Any pointer may be NULL. */
+heomgb_status heomgb_qme_get_hrchy(const heomgb_qme* q, int* n, int* ptr_p1, int* ptr_m1);
+/* calc_diff_impl(obj, drho_dt, rho, alpha, beta, temp) -- heom_hilb.h:70-215:
+ * drho = beta*drho - alpha*D(rho) with host arrays of main_size() complex.
+ * (The reference's qme_solver::calc_diff is an empty stub, qme_solver.h:37-42;
+ * this is the model-level operator it would call.) */
+heomgb_status heomgb_qme_calc_diff(heomgb_qme* q, double* drho, const double* rho, const double* alpha,
+                                   const double* beta);
+/* Same with device pointers (double2 arrays of main_size()), on the qme stream. */
+heomgb_status heomgb_qme_calc_diff_device(heomgb_qme* q, void* drho, const void* rho, const double* alpha,
+                                          const double* beta);
+
+/* ---- solvers --------------------------------------------------------------- */
+/* rk4<...>(), lsrk4<...>(), rkdp<...>() default constructors. */
+heomgb_status heomgb_solver_create(heomgb_solver_kind kind, heomgb_solver** out);
+heomgb_status heomgb_solver_destroy(heomgb_solver* s);
+
+/* qme_solver(engine, qme, solver) -- qme_solver.h:26-35: allocates the state
+ * and stage buffers of `s` for `q` (solver_base::init, rk4::init, ...). */
+heomgb_status heomgb_qme_solver_create(heomgb_qme* q, heomgb_solver* s, heomgb_qme_solver** out);
+heomgb_status heomgb_qme_solver_destroy(heomgb_qme_solver* qs);
+
+/* qme_solver::solve(rho, t_list, n_t, callback, kwargs) -- qme_solver.h:44-52,
+ * solver_base.h:64-79.  rho: host array of main_size() complex, updated in
+ * place; the state crosses host<->device once per output interval exactly as
+ * in the reference (host2dev before, dev2host after each interval).  The
+ * callback may be NULL. */
+heomgb_status heomgb_qme_solver_solve(heomgb_qme_solver* qs, double* rho, const double* t_list, int n_t,
+                                      heomgb_callback cb, void* user, const heomgb_kwargs* kwargs);
+/* Same with rho already resident on the device (double2 array of main_size());
+ * no host<->device traffic of the state. */
+heomgb_status heomgb_qme_solver_solve_device(heomgb_qme_solver* qs, void* rho, const double* t_list, int n_t,
+                                             heomgb_callback cb, void* user, const heomgb_kwargs* kwargs);
+/* Step statistics of the last solve: right-hand-side evaluations, step
+ * attempts, accepted steps, and the step size kept for the next call
+ * (rkdp's dt_save, adaptive_step_size_solver.h:21,55). */
+heomgb_status heomgb_qme_solver_stats(const heomgb_qme_solver* qs, long long* n_rhs, long long* n_attempts,
+                                      long long* n_accepted, double* dt_save);
+/* Diagnostic without a reference counterpart: device time of the last solve
+ * spent inside graph replays of fused stage kernels (CUDA events on the
+ * solver's stream around every replay batch), and the number of kernels those
+ * replays launched.  busy_ms / kernels is the average stage-kernel duration. */
+heomgb_status heomgb_qme_solver_timing(const heomgb_qme_solver* qs, double* busy_ms, long long* kernels);
+
+/* ---- building blocks ------------------------------------------------------ */
+/* errnrm1(e, x_1, x_2, atol, rtol) -- linalg_engine_cuda.cu:176-201 and
+ * linalg_engine_eigen.h.j2:360-379: sqrt(mean_i (|e_i|/(atol+rtol*max(|x1_i|,|x2_i|)))^2)
+ * over n complex elements, device pointers (double2).  The per-block partial
+ * sums go to a caller-provided device scratch array of heomgb_errnrm1_scratch(n)
+ * doubles; the result is written to *result (host).  stream may be NULL. */
+size_t heomgb_errnrm1_scratch(long long n);
+heomgb_status heomgb_errnrm1_device(const void* e, const void* x1, const void* x2, double atol, double rtol,
+                                    long long n, double* scratch, double* result, void* cuda_stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HEOMGB_H */

@@ -1,0 +1,14 @@
+"""GB300-native HEOM propagation engine.
+
+A drop-in for libheom's propagation path (heom_hilb / heom_liou / heom_ado
+models stepped by rk4 / lsrk4 / rkdp through qme_solver).  The compute path is
+hand-written CUDA for sm_103a behind the C ABI of include/heomgb.h; this package
+is its Python mirror (ctypes) plus the workload definitions.
+"""
+from .params import HeomParams
+from .heom import (heom, heom_hilb, heom_liou, heom_ado, solver_base, rk4, lsrk4, rkdp, qme_solver, from_params,
+                   SOLVERS)
+from ._lib import HeomError, load, launch_count, library_path
+
+__all__ = ["HeomParams", "heom", "heom_hilb", "heom_liou", "heom_ado", "solver_base", "rk4", "lsrk4", "rkdp",
+           "qme_solver", "from_params", "SOLVERS", "HeomError", "load", "launch_count", "library_path"]

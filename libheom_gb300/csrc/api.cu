@@ -1,0 +1,1056 @@
+// C ABI of the engine (include/heomgb.h): parameter ingest, device set-up,
+// and the solver loops that replay CUDA graphs of fused stage launches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "heomgb.h"
+#include "heomgb_impl.cuh"
+
+using cd = std::complex<double>;
+using namespace heomgb;
+
+namespace {
+
+thread_local std::string g_err;
+
+heomgb_status fail(heomgb_status s, const std::string& msg) {
+  g_err = msg;
+  return s;
+}
+
+struct cuda_error : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct arg_error : std::invalid_argument {
+  using std::invalid_argument::invalid_argument;
+};
+struct state_error : std::logic_error {
+  using std::logic_error::logic_error;
+};
+struct unsupported_error : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct numeric_error : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw cuda_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <class F>
+heomgb_status guard(F&& f) {
+  try {
+    f();
+    return HEOMGB_OK;
+  } catch (const arg_error& e) {
+    return fail(HEOMGB_ERR_INVALID_ARGUMENT, e.what());
+  } catch (const state_error& e) {
+    return fail(HEOMGB_ERR_STATE, e.what());
+  } catch (const unsupported_error& e) {
+    return fail(HEOMGB_ERR_UNSUPPORTED, e.what());
+  } catch (const numeric_error& e) {
+    return fail(HEOMGB_ERR_NUMERIC, e.what());
+  } catch (const cuda_error& e) {
+    return fail(HEOMGB_ERR_CUDA, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(HEOMGB_ERR_ALLOC, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(HEOMGB_ERR_INVALID_ARGUMENT, e.what());
+  }
+}
+
+cd C(const double* p, size_t i) { return cd(p[2 * i], p[2 * i + 1]); }
+
+// Device allocations owned by one object, freed together.
+struct DeviceArena {
+  std::vector<void*> ptrs;
+  void* alloc(size_t bytes) {
+    void* p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw cuda_error(std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+    }
+    ptrs.push_back(p);
+    return p;
+  }
+  template <class T>
+  T* upload(const std::vector<T>& v, cudaStream_t s) {
+    T* d = static_cast<T*>(alloc(sizeof(T) * std::max<size_t>(v.size(), 1)));
+    if (!v.empty()) ck(cudaMemcpyAsync(d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s), "upload");
+    return d;
+  }
+  void release() {
+    for (void* p : ptrs) cudaFree(p);
+    ptrs.clear();
+  }
+  ~DeviceArena() { release(); }
+};
+
+// ------------------------------------------------------------------ LIL algebra (set-up only)
+// The reference builds its superoperators in std::map-of-map LIL matrices
+// (lil_matrix.h.j2:22-183); the same container keeps the summation order and
+// the pruning rule of optimize() (entries with |v| <= eps*max are dropped).
+using Lil = std::map<int, std::map<int, cd>>;
+
+void lil_optimize(Lil& m) {
+  double mx = 0.0;
+  for (auto& r : m)
+    for (auto& e : r.second) mx = std::max(mx, std::abs(e.second));
+  if (mx == 0.0) mx = 1.0;
+  const double tol = std::numeric_limits<double>::epsilon() * mx;
+  for (auto it = m.begin(); it != m.end();) {
+    for (auto jt = it->second.begin(); jt != it->second.end();) {
+      if (std::abs(jt->second) <= tol)
+        jt = it->second.erase(jt);
+      else
+        ++jt;
+    }
+    if (it->second.empty())
+      it = m.erase(it);
+    else
+      ++it;
+  }
+}
+
+// Y += alpha * (X (x) 1) and Y += alpha * (1 (x) X^T) on row-major vec(rho).
+void kron_x_1(const std::vector<cd>& X, int n, cd alpha, Lil& Y) {
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) {
+      const cd v = X[r * n + c];
+      if (v == cd(0.0, 0.0)) continue;
+      const cd p = v * alpha;
+      for (int k = 0; k < n; ++k) Y[r * n + k][c * n + k] += p;
+    }
+}
+void kron_1_x_T(const std::vector<cd>& X, int n, cd alpha, Lil& Y) {
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) {
+      const cd v = X[r * n + c];
+      if (v == cd(0.0, 0.0)) continue;
+      const cd p = v * alpha;
+      for (int k = 0; k < n; ++k) Y[k * n + c][k * n + r] += p;
+    }
+}
+Lil lil_gemm(cd alpha, const Lil& A, const Lil& B) {
+  Lil Cm;
+  for (auto& ar : A)
+    for (auto& ae : ar.second) {
+      auto it = B.find(ae.first);
+      if (it == B.end()) continue;
+      for (auto& be : it->second) Cm[ar.first][be.first] += alpha * ae.second * be.second;
+    }
+  lil_optimize(Cm);
+  return Cm;
+}
+void lil_axpy(cd alpha, const Lil& X, Lil& Y) {
+  for (auto& r : X)
+    for (auto& e : r.second) Y[r.first][e.first] += alpha * e.second;
+}
+struct Csr {
+  std::vector<int> ptr, idx;
+  std::vector<cd> val;
+};
+Csr to_csr(const Lil& m, int rows) {
+  Csr c;
+  c.ptr.assign(rows + 1, 0);
+  for (int r = 0; r < rows; ++r) {
+    auto it = m.find(r);
+    if (it != m.end())
+      for (auto& e : it->second) {
+        c.idx.push_back(e.first);
+        c.val.push_back(e.second);
+      }
+    c.ptr[r + 1] = static_cast<int>(c.idx.size());
+  }
+  return c;
+}
+
+std::vector<double2> to_d2(const std::vector<cd>& v) {
+  std::vector<double2> o(v.size());
+  for (size_t i = 0; i < v.size(); ++i) o[i] = make_double2(v[i].real(), v[i].imag());
+  return o;
+}
+std::vector<float2> to_f2(const std::vector<cd>& v) {
+  std::vector<float2> o(v.size());
+  for (size_t i = 0; i < v.size(); ++i)
+    o[i] = make_float2(static_cast<float>(v[i].real()), static_cast<float>(v[i].imag()));
+  return o;
+}
+
+long long binom_sat(long long a, long long b) {
+  if (b < 0 || b > a) return 0;
+  b = std::min(b, a - b);
+  long double r = 1;
+  for (long long i = 1; i <= b; ++i) r = r * (a - b + i) / i;
+  if (r > static_cast<long double>(LLONG_MAX / 4)) return LLONG_MAX / 4;
+  return static_cast<long long>(std::llround(r));
+}
+
+struct Bath {
+  bool set = false;
+  int len = 0;
+  std::vector<cd> V, gamma, phi0, sigma, S, A;
+  cd sdelta;
+};
+
+}  // namespace
+
+// ------------------------------------------------------------------ model object
+struct heomgb_qme {
+  int form = HEOMGB_HILB;
+  int max_depth = 0;
+  int device = 0;
+  int n_sm = 152;
+  int n = 0;
+  std::vector<cd> H;
+  int U = -1;
+  std::vector<Bath> baths;
+  int precision = HEOMGB_FP64;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t user_stream = nullptr;
+  bool user_stream_set = false;
+  bool ready = false;
+  // derived
+  int K = 0, n_hrchy = 0, path = PATH_DIAG;
+  RhsModel dm{};
+  DeviceArena arena;
+  DeviceArena scratch;       // calc_diff host-API buffers
+  double2* sx = nullptr;
+  double2* sy = nullptr;
+  cudaStream_t stream() const { return user_stream_set ? user_stream : own_stream; }
+  long long main_size() const { return static_cast<long long>(n) * n * n_hrchy; }
+};
+
+struct heomgb_solver {
+  int kind = HEOMGB_RK4;
+};
+
+struct heomgb_qme_solver {
+  heomgb_qme* q = nullptr;
+  int kind = HEOMGB_RK4;
+  cudaStream_t stream = nullptr;
+  bool mixed = false;
+  bool separate = false;
+  long long N = 0;
+  DeviceArena arena;
+  double2* S[2] = {nullptr, nullptr};
+  void* Yb[2] = {nullptr, nullptr};
+  void* Ytmp[2] = {nullptr, nullptr};
+  double2* acc = nullptr;
+  void* K[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  DpCtl* ctl = nullptr;
+  DpCtl* ctl_host = nullptr;  // pinned mirror
+  double* partials = nullptr;
+  int grid = 1, block = 32;
+  cudaGraphExec_t g_small = nullptr, g_big = nullptr;
+  int n_small = 0, n_big = 0;           // steps (fixed) or attempts (DP) per graph
+  int nodes_small = 0, nodes_big = 0;
+  double dt_save = -1.0;
+  long long n_rhs = 0, n_attempts = 0, n_accepted = 0;
+  // device time spent inside graph replays of the last solve (CUDA events on
+  // the solver stream around every replay batch), and the kernels replayed
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double busy_ms = 0.0;
+  long long replayed_kernels = 0;
+  ~heomgb_qme_solver() {
+    if (g_small) cudaGraphExecDestroy(g_small);
+    if (g_big) cudaGraphExecDestroy(g_big);
+    if (ctl_host) cudaFreeHost(ctl_host);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+  }
+};
+
+namespace {
+
+void require(bool c, const char* msg) {
+  if (!c) throw arg_error(msg);
+}
+
+// ------------------------------------------------------------------ set_param
+void build_model(heomgb_qme* q) {
+  if (q->n <= 0) throw state_error("set_param: Hamiltonian not set");
+  if (q->U < 0) throw state_error("set_param: alloc_noises not called");
+  for (int u = 0; u < q->U; ++u)
+    if (!q->baths[u].set) throw state_error("set_param: noise " + std::to_string(u) + " not set");
+  ck(cudaSetDevice(q->device), "cudaSetDevice");
+  q->arena.release();
+  q->ready = false;
+  cudaStream_t s = q->stream();
+  const int n = q->n, n2 = n * n, U = q->U;
+  // linear mode index lk (heom.h:65-74) and per-mode coefficients
+  std::vector<int> bath_ptr(U + 1, 0);
+  std::vector<cd> sigma, sv, av, gdiag, sdelta;
+  for (int u = 0; u < U; ++u) {
+    const Bath& b = q->baths[u];
+    bath_ptr[u + 1] = bath_ptr[u] + b.len;
+    for (int k = 0; k < b.len; ++k) {
+      sigma.push_back(b.sigma[k]);
+      gdiag.push_back(b.gamma[static_cast<size_t>(k) * b.len + k]);
+      // s = S*phi_0, a = A*phi_0 (heom.h:124-138): zero entries skipped, j ascending
+      cd s_{0.0, 0.0}, a_{0.0, 0.0};
+      for (int j = 0; j < b.len; ++j) {
+        const cd Sv = b.S[static_cast<size_t>(k) * b.len + j], Av = b.A[static_cast<size_t>(k) * b.len + j];
+        if (Sv != cd(0.0, 0.0)) s_ += Sv * b.phi0[j];
+        if (Av != cd(0.0, 0.0)) a_ += Av * b.phi0[j];
+      }
+      sv.push_back(s_);
+      av.push_back(a_);
+    }
+    sdelta.push_back(b.sdelta);
+  }
+  const int K = bath_ptr[U];
+  const long long count = binom_sat(static_cast<long long>(K) + q->max_depth, q->max_depth);
+  if (count > INT_MAX - 1) throw arg_error("hierarchy too large: more than 2^31-2 ADOs");
+  if (static_cast<long long>(n2) * count > (1LL << 40)) throw arg_error("state vector too large");
+  q->K = K;
+  q->n_hrchy = static_cast<int>(count);
+  const int nh = q->n_hrchy;
+
+  RhsModel& m = q->dm;
+  m = RhsModel{};
+  m.n = n;
+  m.n2 = n2;
+  m.K = K;
+  m.U = U;
+  m.n_hrchy = nh;
+
+  // hierarchy tables on the device (hrchy_space.cc:137-231)
+  int* nidx = static_cast<int*>(q->arena.alloc(sizeof(int) * std::max<size_t>(1, static_cast<size_t>(nh) * K)));
+  int* p1 = static_cast<int*>(q->arena.alloc(sizeof(int) * std::max<size_t>(1, static_cast<size_t>(nh + 1) * K)));
+  int* m1 = static_cast<int*>(q->arena.alloc(sizeof(int) * std::max<size_t>(1, static_cast<size_t>(nh + 1) * K)));
+  if (K > 0) {
+    const int bd = K + q->max_depth + 2;
+    std::vector<long long> bt(static_cast<size_t>(bd) * bd);
+    for (int a = 0; a < bd; ++a)
+      for (int b = 0; b < bd; ++b) bt[static_cast<size_t>(a) * bd + b] = binom_sat(a, b);
+    DeviceArena tmp;
+    long long* dbt = tmp.upload(bt, s);
+    ck(launch_hrchy_build(K, q->max_depth, nh, dbt, bd, nidx, p1, m1, s), "hierarchy build");
+    ck(cudaStreamSynchronize(s), "hierarchy build sync");
+  }
+  m.p1 = p1;
+  m.m1 = m1;
+  m.nidx = nidx;
+  // per-ADO damping sum_k n_k gamma_kk (heom.h:94-104)
+  double2* ngd = static_cast<double2*>(q->arena.alloc(sizeof(double2) * nh));
+  float2* ngd_f = static_cast<float2*>(q->arena.alloc(sizeof(float2) * nh));
+  if (K > 0) {
+    DeviceArena tmp;
+    double2* dg = tmp.upload(to_d2(gdiag), s);
+    ck(launch_ngd(K, nh, nidx, dg, ngd, ngd_f, s), "ngamma");
+    ck(cudaStreamSynchronize(s), "ngamma sync");
+  } else {
+    ck(cudaMemsetAsync(ngd, 0, sizeof(double2) * nh, s), "memset");
+    ck(cudaMemsetAsync(ngd_f, 0, sizeof(float2) * nh, s), "memset");
+  }
+  m.ngd = ngd;
+  m.ngd_f = ngd_f;
+
+  // constants
+  bool h_real = true;
+  for (const cd& v : q->H) h_real = h_real && v.imag() == 0.0;
+  m.h_real = h_real ? 1 : 0;
+  m.H = q->arena.upload(to_d2(q->H), s);
+  m.H_f = q->arena.upload(to_f2(q->H), s);
+  std::vector<cd> Vall;
+  bool diag = true;
+  for (int u = 0; u < U; ++u) {
+    const Bath& b = q->baths[u];
+    Vall.insert(Vall.end(), b.V.begin(), b.V.end());
+    for (int r = 0; r < n; ++r)
+      for (int c = 0; c < n; ++c)
+        if (r != c && b.V[static_cast<size_t>(r) * n + c] != cd(0.0, 0.0)) diag = false;
+  }
+  m.V = q->arena.upload(to_d2(Vall), s);
+  m.V_f = q->arena.upload(to_f2(Vall), s);
+  m.bath_ptr = q->arena.upload(bath_ptr, s);
+  m.sigma = q->arena.upload(to_d2(sigma), s);
+  m.s = q->arena.upload(to_d2(sv), s);
+  m.a = q->arena.upload(to_d2(av), s);
+  m.sdelta = q->arena.upload(to_d2(sdelta), s);
+  m.sigma_f = q->arena.upload(to_f2(sigma), s);
+  m.s_f = q->arena.upload(to_f2(sv), s);
+  m.a_f = q->arena.upload(to_f2(av), s);
+  m.sdelta_f = q->arena.upload(to_f2(sdelta), s);
+
+  if (q->form == HEOMGB_HILB) {
+    q->path = diag ? PATH_DIAG : PATH_GENERAL;
+  } else {
+    q->path = PATH_LIOU;
+  }
+  if (q->path == PATH_DIAG) {
+    // per-element active modes of the elementwise bath terms
+    std::vector<int> pp(n2 + 1, 0), pm(n2 + 1, 0), pmode, mmode;
+    std::vector<cd> cp, cmn, csd(n2, cd(0.0, 0.0));
+    const cd I(0.0, 1.0);
+    for (int a = 0; a < n; ++a)
+      for (int b = 0; b < n; ++b) {
+        const int e = a * n + b;
+        for (int u = 0; u < U; ++u) {
+          const Bath& B = q->baths[u];
+          const cd va = B.V[static_cast<size_t>(a) * n + a], vb = B.V[static_cast<size_t>(b) * n + b];
+          const cd cphi = I * (va - vb), cpsi = va + vb;
+          csd[e] += B.sdelta * (va - vb) * (va - vb);
+          for (int k = bath_ptr[u]; k < bath_ptr[u + 1]; ++k) {
+            const cd c1 = cphi * sigma[k];
+            if (c1 != cd(0.0, 0.0)) {
+              pmode.push_back(k);
+              cp.push_back(c1);
+            }
+            const cd c2 = cphi * sv[k] - cpsi * av[k];
+            if (c2 != cd(0.0, 0.0)) {
+              mmode.push_back(k);
+              cmn.push_back(c2);
+            }
+          }
+        }
+        pp[e + 1] = static_cast<int>(pmode.size());
+        pm[e + 1] = static_cast<int>(mmode.size());
+      }
+    m.plus_ptr = q->arena.upload(pp, s);
+    m.plus_mode = q->arena.upload(pmode, s);
+    m.minus_ptr = q->arena.upload(pm, s);
+    m.minus_mode = q->arena.upload(mmode, s);
+    m.c_plus = q->arena.upload(to_d2(cp), s);
+    m.c_minus = q->arena.upload(to_d2(cmn), s);
+    m.c_plus_f = q->arena.upload(to_f2(cp), s);
+    m.c_minus_f = q->arena.upload(to_f2(cmn), s);
+    m.c_sd = q->arena.upload(to_d2(csd), s);
+    m.c_sd_f = q->arena.upload(to_f2(csd), s);
+  } else if (q->path == PATH_GENERAL) {
+    if (rhs_smem_bytes(m, PATH_GENERAL, false) > 200 * 1024)
+      throw unsupported_error("general-V Hilbert path supports n_level <= 50");
+  } else {
+    if (rhs_smem_bytes(m, PATH_LIOU, false) > 200 * 1024)
+      throw unsupported_error("Liouville path supports n_level <= 56");
+    // superoperators (heom_liou.h:71-99)
+    const cd I(0.0, 1.0), one(1.0, 0.0);
+    Lil L;
+    kron_x_1(q->H, n, I, L);
+    kron_1_x_T(q->H, n, -I, L);
+    Lil R0;
+    lil_axpy(one, L, R0);
+    std::vector<int> phi_ptr, phi_idx, psi_ptr, psi_idx;
+    std::vector<cd> phi_val, psi_val;
+    std::vector<Lil> Xi(U);
+    for (int u = 0; u < U; ++u) {
+      Lil Phi, Psi;
+      kron_x_1(q->baths[u].V, n, I, Phi);
+      kron_1_x_T(q->baths[u].V, n, -I, Phi);
+      lil_optimize(Phi);
+      kron_x_1(q->baths[u].V, n, one, Psi);
+      kron_1_x_T(q->baths[u].V, n, one, Psi);
+      lil_optimize(Psi);
+      Xi[u] = lil_gemm(-q->baths[u].sdelta, Phi, Phi);
+      Csr cph = to_csr(Phi, n2), cps = to_csr(Psi, n2);
+      const int off_ph = static_cast<int>(phi_idx.size()), off_ps = static_cast<int>(psi_idx.size());
+      for (int r = 0; r <= n2; ++r) {
+        phi_ptr.push_back(off_ph + cph.ptr[r]);
+        psi_ptr.push_back(off_ps + cps.ptr[r]);
+      }
+      phi_idx.insert(phi_idx.end(), cph.idx.begin(), cph.idx.end());
+      phi_val.insert(phi_val.end(), cph.val.begin(), cph.val.end());
+      psi_idx.insert(psi_idx.end(), cps.idx.begin(), cps.idx.end());
+      psi_val.insert(psi_val.end(), cps.val.begin(), cps.val.end());
+    }
+    for (int u = 0; u < U; ++u) lil_axpy(one, Xi[u], R0);
+    Csr cr0 = to_csr(R0, n2);
+    m.r0_ptr = q->arena.upload(cr0.ptr, s);
+    m.r0_idx = q->arena.upload(cr0.idx, s);
+    m.r0_val = q->arena.upload(to_d2(cr0.val), s);
+    m.r0_val_f = q->arena.upload(to_f2(cr0.val), s);
+    m.phi_ptr = q->arena.upload(phi_ptr, s);
+    m.phi_idx = q->arena.upload(phi_idx, s);
+    m.phi_val = q->arena.upload(to_d2(phi_val), s);
+    m.phi_val_f = q->arena.upload(to_f2(phi_val), s);
+    m.psi_ptr = q->arena.upload(psi_ptr, s);
+    m.psi_idx = q->arena.upload(psi_idx, s);
+    m.psi_val = q->arena.upload(to_d2(psi_val), s);
+    m.psi_val_f = q->arena.upload(to_f2(psi_val), s);
+  }
+  ck(cudaStreamSynchronize(s), "set_param sync");
+  q->ready = true;
+}
+
+void need_ready(const heomgb_qme* q) {
+  if (!q) throw arg_error("null qme");
+  if (!q->ready) throw state_error("set_param has not completed");
+}
+
+Stage base_stage() {
+  Stage st;
+  std::memset(&st, 0, sizeof(st));
+  return st;
+}
+
+void run_diff(heomgb_qme* q, double2* drho, const double2* rho, const double* alpha, const double* beta) {
+  Stage st = base_stage();
+  st.kind = EPI_DIFF;
+  st.y_sel = 0;
+  st.y_fixed = rho;
+  st.out = drho;
+  st.alpha = make_double2(alpha ? alpha[0] : 1.0, alpha ? alpha[1] : 0.0);
+  st.beta = make_double2(beta ? beta[0] : 0.0, beta ? beta[1] : 0.0);
+  st.beta_zero = (st.beta.x == 0.0 && st.beta.y == 0.0) ? 1 : 0;
+  const int block = rhs_block_size(q->dm, q->path);
+  const int grid = rhs_grid_size(q->dm, q->path, block, q->n_sm);
+  ck(launch_rhs(q->dm, st, q->path, q->precision == HEOMGB_MIXED, true, grid, block, q->stream()), "calc_diff");
+}
+
+// ------------------------------------------------------------------ solvers
+void alloc_solver(heomgb_qme_solver* qs) {
+  heomgb_qme* q = qs->q;
+  const long long N = q->main_size();
+  qs->N = N;
+  qs->mixed = q->precision == HEOMGB_MIXED;
+  qs->separate = qs->mixed;
+  const size_t bd = sizeof(double2) * N;
+  const size_t bb = (qs->mixed ? sizeof(float2) : sizeof(double2)) * N;
+  auto& A = qs->arena;
+  const int nstate = qs->kind == HEOMGB_RK4 ? 1 : 2;
+  for (int i = 0; i < nstate; ++i) {
+    qs->S[i] = static_cast<double2*>(A.alloc(bd));
+    qs->Yb[i] = qs->separate ? A.alloc(bb) : static_cast<void*>(qs->S[i]);
+  }
+  if (qs->kind == HEOMGB_RK4 || qs->kind == HEOMGB_RKDP) {
+    qs->Ytmp[0] = A.alloc(bb);
+    qs->Ytmp[1] = A.alloc(bb);
+  }
+  if (qs->kind == HEOMGB_RK4 || qs->kind == HEOMGB_LSRK4) qs->acc = static_cast<double2*>(A.alloc(bd));
+  if (qs->kind == HEOMGB_RKDP)
+    for (int i = 0; i < 6; ++i) qs->K[i] = A.alloc(bb);
+  qs->ctl = static_cast<DpCtl*>(A.alloc(sizeof(DpCtl)));
+  ck(cudaMemsetAsync(qs->ctl, 0, sizeof(DpCtl), qs->stream), "memset ctl");
+  ck(cudaMallocHost(reinterpret_cast<void**>(&qs->ctl_host), sizeof(DpCtl)), "cudaMallocHost");
+  ck(cudaEventCreate(&qs->ev0), "event create");
+  ck(cudaEventCreate(&qs->ev1), "event create");
+  qs->block = rhs_block_size(q->dm, q->path);
+  qs->grid = rhs_grid_size(q->dm, q->path, qs->block, q->n_sm);
+  qs->partials = static_cast<double*>(A.alloc(sizeof(double) * std::max(qs->grid, 1)));
+}
+
+Stage solver_stage(heomgb_qme_solver* qs) {
+  Stage st = base_stage();
+  st.ctl = qs->ctl;
+  st.S[0] = qs->S[0];
+  st.S[1] = qs->S[1];
+  st.Yb[0] = qs->Yb[0];
+  st.Yb[1] = qs->Yb[1];
+  st.acc = qs->acc;
+  for (int i = 0; i < 6; ++i) st.K[i] = qs->K[i];
+  st.bulk_separate = qs->separate ? 1 : 0;
+  st.partials = qs->partials;
+  return st;
+}
+
+void launch_stage(heomgb_qme_solver* qs, const Stage& st) {
+  ck(launch_rhs(qs->q->dm, st, qs->q->path, qs->mixed, false, qs->grid, qs->block, qs->stream), "stage launch");
+}
+
+// One step (RK4/LSRK4) or one attempt (DP5) as a sequence of fused launches.
+int enqueue_unit(heomgb_qme_solver* qs) {
+  Stage st = solver_stage(qs);
+  if (qs->kind == HEOMGB_RK4) {
+    const int kinds[4] = {EPI_RK4_1, EPI_RK4_2, EPI_RK4_3, EPI_RK4_4};
+    const void* in[4] = {qs->Yb[0], qs->Ytmp[0], qs->Ytmp[1], qs->Ytmp[0]};
+    void* nxt[4] = {qs->Ytmp[0], qs->Ytmp[1], qs->Ytmp[0], nullptr};
+    for (int s = 0; s < 4; ++s) {
+      st.kind = kinds[s];
+      st.y_sel = 0;
+      st.y_fixed = in[s];
+      st.Ynext = nxt[s];
+      launch_stage(qs, st);
+    }
+    return 4;
+  }
+  if (qs->kind == HEOMGB_LSRK4) {  // B = 1/3, 3/4, 2/3, 1/4 (lsrk4.h:39-46)
+    const double B[4] = {1.0 / 3.0, 3.0 / 4.0, 2.0 / 3.0, 1.0 / 4.0};
+    for (int s = 0; s < 4; ++s) {
+      st.kind = EPI_LS;
+      st.ls_in = s & 1;
+      st.ls_first = s == 0;
+      st.coef = B[s];
+      st.y_sel = 0;
+      st.y_fixed = qs->Yb[s & 1];
+      launch_stage(qs, st);
+    }
+    return 4;
+  }
+  for (int s = 0; s < 6; ++s) {
+    st.kind = EPI_DP;
+    st.dp_stage = s;
+    if (s == 0) {
+      st.y_sel = 1;
+    } else {
+      st.y_sel = 0;
+      st.y_fixed = qs->Ytmp[(s - 1) & 1];
+    }
+    st.Ynext = s < 5 ? qs->Ytmp[s & 1] : nullptr;
+    launch_stage(qs, st);
+  }
+  st.kind = EPI_DP7;
+  st.y_sel = 2;
+  st.Ynext = nullptr;
+  launch_stage(qs, st);
+  return 7;
+}
+
+cudaGraphExec_t capture_units(heomgb_qme_solver* qs, int units, int* nodes) {
+  cudaGraph_t g = nullptr;
+  ck(cudaStreamBeginCapture(qs->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+  int launched = 0;
+  const long long before = g_launches;
+  try {
+    for (int i = 0; i < units; ++i) launched += enqueue_unit(qs);
+  } catch (...) {
+    cudaStreamEndCapture(qs->stream, &g);
+    if (g) cudaGraphDestroy(g);
+    throw;
+  }
+  g_launches = before;  // captured launches are counted when the graph replays
+  ck(cudaStreamEndCapture(qs->stream, &g), "end capture");
+  cudaGraphExec_t ex = nullptr;
+  cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  ck(e, "graph instantiate");
+  *nodes = launched;
+  return ex;
+}
+
+void ensure_graphs(heomgb_qme_solver* qs) {
+  if (qs->g_small) return;
+  if (qs->kind == HEOMGB_RKDP) {
+    qs->n_small = 4;
+    qs->n_big = 32;
+  } else {
+    qs->n_small = 1;
+    qs->n_big = 50;
+  }
+  qs->g_small = capture_units(qs, qs->n_small, &qs->nodes_small);
+  qs->g_big = capture_units(qs, qs->n_big, &qs->nodes_big);
+}
+
+void replay(heomgb_qme_solver* qs, bool big) {
+  ck(cudaGraphLaunch(big ? qs->g_big : qs->g_small, qs->stream), "graph launch");
+  const int nodes = big ? qs->nodes_big : qs->nodes_small;
+  g_launches += nodes;
+  qs->replayed_kernels += nodes;
+}
+
+// Busy-time bracket around a batch of replays; collected after a stream sync.
+bool g_busy_open = false;
+void busy_begin(heomgb_qme_solver* qs) { ck(cudaEventRecord(qs->ev0, qs->stream), "event record"); }
+void busy_end(heomgb_qme_solver* qs) {
+  ck(cudaEventRecord(qs->ev1, qs->stream), "event record");
+  g_busy_open = true;
+}
+void busy_collect(heomgb_qme_solver* qs) {
+  if (!g_busy_open) return;
+  float ms = 0.f;
+  ck(cudaEventElapsedTime(&ms, qs->ev0, qs->ev1), "event elapsed");
+  qs->busy_ms += ms;
+  g_busy_open = false;
+}
+
+void state_to_bulk(heomgb_qme_solver* qs, int idx) {
+  if (qs->separate)
+    ck(launch_to_bulk(qs->S[idx], static_cast<float2*>(qs->Yb[idx]), qs->N, qs->stream), "to bulk");
+}
+
+double need_kw(const heomgb_kwargs* kw, int has, double v, const char* key) {
+  if (!kw || !has) throw arg_error(std::string("missing kwarg \"") + key + "\"");
+  return v;
+}
+
+// fixed_step_size_solver::solve_1 (fixed_step_size_solver.h:29-52): the host
+// replays the reference's time loop to get the step sequence (m steps of dt,
+// then the clamped last step), and the device runs it as graph replays.
+void solve_fixed(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwargs* kw) {
+  const double dt = need_kw(kw, kw ? kw->has_dt : 0, kw ? kw->dt : 0, "dt");
+  long long m = 0;
+  double t = t0, d = dt, last = dt;
+  const long long cap = 1LL << 40;
+  while (true) {
+    if (t + d - t1 > -std::numeric_limits<double>::epsilon()) {
+      last = t1 - t;
+      break;
+    }
+    t += d;
+    if (++m > cap) throw numeric_error("fixed-step loop does not terminate");
+  }
+  ensure_graphs(qs);
+  ck(launch_ctl_init(qs->ctl, t0, dt, t1, 0.0, 0.0, 0, qs->stream), "ctl init");
+  busy_begin(qs);
+  for (long long i = 0; i < m / qs->n_big; ++i) replay(qs, true);
+  for (long long i = 0; i < m % qs->n_big; ++i) replay(qs, false);
+  ck(launch_ctl_set_fixed(qs->ctl, last, qs->stream), "ctl dt");
+  replay(qs, false);
+  busy_end(qs);
+  qs->n_rhs += 4 * (m + 1);
+  qs->n_attempts += m + 1;
+  qs->n_accepted += m + 1;
+}
+
+// adaptive_step_size_solver::solve_1 + rkdp::solve_adaptive_step
+// (adaptive_step_size_solver.h:32-56, rkdp.h:81-179) with the controller on
+// the device; the host only polls the `done` flag between graph replays.
+int solve_adaptive(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwargs* kw, int cur) {
+  if (qs->dt_save == -1.0) qs->dt_save = need_kw(kw, kw ? kw->has_dt : 0, kw ? kw->dt : 0, "dt");
+  const double atol = need_kw(kw, kw ? kw->has_atol : 0, kw ? kw->atol : 0, "atol");
+  const double rtol = need_kw(kw, kw ? kw->has_rtol : 0, kw ? kw->rtol : 0, "rtol");
+  double dt = qs->dt_save;
+  if (t0 + dt > t1) dt = t1 - t0;
+  ensure_graphs(qs);
+  ck(launch_ctl_init(qs->ctl, t0, dt, t1, atol, rtol, cur, qs->stream), "ctl init");
+  long long launched = 0;
+  bool big = false;
+  const long long cap = 100000000LL;
+  while (true) {
+    busy_begin(qs);
+    replay(qs, big);
+    busy_end(qs);
+    launched += big ? qs->n_big : qs->n_small;
+    ck(cudaMemcpyAsync(qs->ctl_host, qs->ctl, sizeof(DpCtl), cudaMemcpyDeviceToHost, qs->stream), "ctl read");
+    ck(cudaStreamSynchronize(qs->stream), "solve sync");
+    busy_collect(qs);
+    if (qs->ctl_host->done) break;
+    big = true;
+    if (launched > cap) throw numeric_error("Dormand-Prince attempt cap reached");
+  }
+  if (qs->ctl_host->status) throw numeric_error("non-finite step size in Dormand-Prince control");
+  qs->dt_save = qs->ctl_host->dt;
+  qs->n_attempts += qs->ctl_host->attempts;
+  qs->n_accepted += qs->ctl_host->accepted;
+  qs->n_rhs += 7 * qs->ctl_host->attempts;
+  return qs->ctl_host->cur;
+}
+
+void solve_impl(heomgb_qme_solver* qs, void* rho, bool host, const double* t_list, int n_t, heomgb_callback cb,
+                void* user, const heomgb_kwargs* kw) {
+  if (!qs) throw arg_error("null qme_solver");
+  need_ready(qs->q);
+  if (!rho) throw arg_error("null rho");
+  if (n_t < 1 || !t_list) throw arg_error("t_list must hold at least one time");
+  ck(cudaSetDevice(qs->q->device), "cudaSetDevice");
+  qs->n_rhs = qs->n_attempts = qs->n_accepted = 0;
+  qs->busy_ms = 0.0;
+  qs->replayed_kernels = 0;
+  g_busy_open = false;
+  const size_t bytes = sizeof(double2) * qs->N;
+  const cudaMemcpyKind in_kind = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  const cudaMemcpyKind out_kind = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  // solver_base::solve (solver_base.h:64-79)
+  for (int i = 0; i < n_t - 1; ++i) {
+    if (cb) {
+      if (!host) ck(cudaStreamSynchronize(qs->stream), "sync before callback");
+      cb(t_list[i], user);
+    }
+    ck(cudaMemcpyAsync(qs->S[0], rho, bytes, in_kind, qs->stream), "state in");
+    state_to_bulk(qs, 0);
+    int cur = 0;
+    if (qs->kind == HEOMGB_RKDP)
+      cur = solve_adaptive(qs, t_list[i], t_list[i + 1], kw, 0);
+    else
+      solve_fixed(qs, t_list[i], t_list[i + 1], kw);
+    ck(cudaMemcpyAsync(rho, qs->S[cur], bytes, out_kind, qs->stream), "state out");
+    ck(cudaStreamSynchronize(qs->stream), "interval sync");
+    busy_collect(qs);
+  }
+  if (cb) cb(t_list[n_t - 1], user);
+}
+
+}  // namespace
+
+// ======================================================================= C ABI
+extern "C" {
+
+const char* heomgb_last_error(void) { return g_err.c_str(); }
+const char* heomgb_version(void) { return "0.1.0"; }
+int heomgb_abi_version(void) { return 1; }
+long long heomgb_launch_count(void) { return g_launches; }
+
+heomgb_status heomgb_qme_create(heomgb_form form, int max_depth, int n_inner_threads, int n_outer_threads,
+                                heomgb_qme** out) {
+  (void)n_inner_threads;
+  (void)n_outer_threads;
+  return guard([&] {
+    require(out != nullptr, "null out");
+    require(form == HEOMGB_HILB || form == HEOMGB_LIOU || form == HEOMGB_ADO, "unknown form");
+    require(max_depth >= 0, "max_depth must be >= 0");
+    auto q = std::make_unique<heomgb_qme>();
+    q->form = form;
+    q->max_depth = max_depth;
+    ck(cudaGetDevice(&q->device), "cudaGetDevice");
+    ck(cudaDeviceGetAttribute(&q->n_sm, cudaDevAttrMultiProcessorCount, q->device), "device attribute");
+    ck(cudaStreamCreateWithFlags(&q->own_stream, cudaStreamNonBlocking), "stream create");
+    *out = q.release();
+  });
+}
+
+heomgb_status heomgb_qme_destroy(heomgb_qme* q) {
+  if (!q) return HEOMGB_OK;
+  cudaSetDevice(q->device);
+  if (q->own_stream) cudaStreamSynchronize(q->own_stream);
+  if (q->user_stream_set) cudaStreamSynchronize(q->user_stream);
+  q->arena.release();
+  q->scratch.release();
+  if (q->own_stream) cudaStreamDestroy(q->own_stream);
+  delete q;
+  return HEOMGB_OK;
+}
+
+heomgb_status heomgb_qme_set_hamiltonian(heomgb_qme* q, int n_level, const double* H) {
+  return guard([&] {
+    require(q && H, "null argument");
+    require(n_level > 0, "n_level must be > 0");
+    q->n = n_level;
+    q->H.resize(static_cast<size_t>(n_level) * n_level);
+    for (size_t i = 0; i < q->H.size(); ++i) q->H[i] = C(H, i);
+    q->ready = false;
+  });
+}
+
+heomgb_status heomgb_qme_alloc_noises(heomgb_qme* q, int n_noise) {
+  return guard([&] {
+    require(q != nullptr, "null qme");
+    require(n_noise >= 0, "n_noise must be >= 0");
+    q->U = n_noise;
+    q->baths.assign(n_noise, Bath{});
+    q->ready = false;
+  });
+}
+
+heomgb_status heomgb_qme_set_noise(heomgb_qme* q, int u, const double* V, int len_gamma, const double* gamma,
+                                   const double* phi_0, const double* sigma, const double* S, const double* A,
+                                   const double* s_delta) {
+  return guard([&] {
+    require(q != nullptr, "null qme");
+    if (q->U < 0) throw state_error("alloc_noises must precede set_noise");
+    require(u >= 0 && u < q->U, "bath index out of range");
+    require(q->n > 0, "set the Hamiltonian (n_level) before the noises");
+    require(len_gamma >= 0, "len_gamma must be >= 0");
+    require(V && s_delta, "null V or s_delta");
+    require(len_gamma == 0 || (gamma && phi_0 && sigma && S && A), "null noise array");
+    Bath b;
+    b.set = true;
+    b.len = len_gamma;
+    const size_t n2 = static_cast<size_t>(q->n) * q->n, L = len_gamma, L2 = L * L;
+    b.V.resize(n2);
+    for (size_t i = 0; i < n2; ++i) b.V[i] = C(V, i);
+    b.gamma.resize(L2);
+    b.S.resize(L2);
+    b.A.resize(L2);
+    for (size_t i = 0; i < L2; ++i) {
+      b.gamma[i] = C(gamma, i);
+      b.S[i] = C(S, i);
+      b.A[i] = C(A, i);
+    }
+    b.phi0.resize(L);
+    b.sigma.resize(L);
+    for (size_t i = 0; i < L; ++i) {
+      b.phi0[i] = C(phi_0, i);
+      b.sigma[i] = C(sigma, i);
+    }
+    b.sdelta = C(s_delta, 0);
+    q->baths[u] = std::move(b);
+    q->ready = false;
+  });
+}
+
+heomgb_status heomgb_qme_set_precision(heomgb_qme* q, heomgb_precision p) {
+  return guard([&] {
+    require(q != nullptr, "null qme");
+    require(p == HEOMGB_FP64 || p == HEOMGB_MIXED, "unknown precision");
+    q->precision = p;
+  });
+}
+
+heomgb_status heomgb_qme_set_stream(heomgb_qme* q, void* cuda_stream) {
+  return guard([&] {
+    require(q != nullptr, "null qme");
+    q->user_stream = static_cast<cudaStream_t>(cuda_stream);
+    q->user_stream_set = cuda_stream != nullptr;
+  });
+}
+
+heomgb_status heomgb_qme_set_param(heomgb_qme* q) {
+  return guard([&] {
+    require(q != nullptr, "null qme");
+    build_model(q);
+  });
+}
+
+heomgb_status heomgb_qme_get_n_hrchy(const heomgb_qme* q, int* n_hrchy) {
+  return guard([&] {
+    need_ready(q);
+    require(n_hrchy != nullptr, "null out");
+    *n_hrchy = q->n_hrchy;
+  });
+}
+
+heomgb_status heomgb_qme_get_n_dim(const heomgb_qme* q, int* n_dim) {
+  return guard([&] {
+    need_ready(q);
+    require(n_dim != nullptr, "null out");
+    *n_dim = q->K;
+  });
+}
+
+heomgb_status heomgb_qme_main_size(const heomgb_qme* q, long long* size) {
+  return guard([&] {
+    need_ready(q);
+    require(size != nullptr, "null out");
+    *size = q->main_size();
+  });
+}
+
+heomgb_status heomgb_qme_get_hrchy(const heomgb_qme* q, int* n, int* ptr_p1, int* ptr_m1) {
+  return guard([&] {
+    need_ready(q);
+    ck(cudaSetDevice(q->device), "cudaSetDevice");
+    const size_t K = q->K, nh = q->n_hrchy;
+    cudaStream_t s = q->stream();
+    if (K == 0) return;
+    if (n) ck(cudaMemcpyAsync(n, q->dm.nidx, sizeof(int) * nh * K, cudaMemcpyDeviceToHost, s), "copy n");
+    if (ptr_p1) ck(cudaMemcpyAsync(ptr_p1, q->dm.p1, sizeof(int) * (nh + 1) * K, cudaMemcpyDeviceToHost, s), "copy p1");
+    if (ptr_m1) ck(cudaMemcpyAsync(ptr_m1, q->dm.m1, sizeof(int) * (nh + 1) * K, cudaMemcpyDeviceToHost, s), "copy m1");
+    ck(cudaStreamSynchronize(s), "hierarchy copy sync");
+  });
+}
+
+heomgb_status heomgb_qme_calc_diff(heomgb_qme* q, double* drho, const double* rho, const double* alpha,
+                                   const double* beta) {
+  return guard([&] {
+    need_ready(q);
+    require(drho && rho, "null rho/drho");
+    require(drho != rho, "drho and rho must not alias");
+    ck(cudaSetDevice(q->device), "cudaSetDevice");
+    cudaStream_t s = q->stream();
+    const size_t bytes = sizeof(double2) * q->main_size();
+    if (!q->sx) {
+      q->sx = static_cast<double2*>(q->scratch.alloc(bytes));
+      q->sy = static_cast<double2*>(q->scratch.alloc(bytes));
+    }
+    const bool beta_zero = !beta || (beta[0] == 0.0 && beta[1] == 0.0);
+    ck(cudaMemcpyAsync(q->sx, rho, bytes, cudaMemcpyHostToDevice, s), "rho in");
+    if (!beta_zero) ck(cudaMemcpyAsync(q->sy, drho, bytes, cudaMemcpyHostToDevice, s), "drho in");
+    run_diff(q, q->sy, q->sx, alpha, beta);
+    ck(cudaMemcpyAsync(drho, q->sy, bytes, cudaMemcpyDeviceToHost, s), "drho out");
+    ck(cudaStreamSynchronize(s), "calc_diff sync");
+  });
+}
+
+heomgb_status heomgb_qme_calc_diff_device(heomgb_qme* q, void* drho, const void* rho, const double* alpha,
+                                          const double* beta) {
+  return guard([&] {
+    need_ready(q);
+    require(drho && rho, "null rho/drho");
+    require(drho != rho, "drho and rho must not alias");
+    ck(cudaSetDevice(q->device), "cudaSetDevice");
+    run_diff(q, static_cast<double2*>(drho), static_cast<const double2*>(rho), alpha, beta);
+  });
+}
+
+heomgb_status heomgb_solver_create(heomgb_solver_kind kind, heomgb_solver** out) {
+  return guard([&] {
+    require(out != nullptr, "null out");
+    require(kind == HEOMGB_RK4 || kind == HEOMGB_LSRK4 || kind == HEOMGB_RKDP, "unknown solver");
+    auto s = std::make_unique<heomgb_solver>();
+    s->kind = kind;
+    *out = s.release();
+  });
+}
+
+heomgb_status heomgb_solver_destroy(heomgb_solver* s) {
+  delete s;
+  return HEOMGB_OK;
+}
+
+heomgb_status heomgb_qme_solver_create(heomgb_qme* q, heomgb_solver* s, heomgb_qme_solver** out) {
+  return guard([&] {
+    need_ready(q);
+    require(s && out, "null argument");
+    ck(cudaSetDevice(q->device), "cudaSetDevice");
+    auto qs = std::make_unique<heomgb_qme_solver>();
+    qs->q = q;
+    qs->kind = s->kind;
+    qs->stream = q->stream();
+    alloc_solver(qs.get());
+    ck(cudaStreamSynchronize(qs->stream), "solver init sync");
+    *out = qs.release();
+  });
+}
+
+heomgb_status heomgb_qme_solver_destroy(heomgb_qme_solver* qs) {
+  if (!qs) return HEOMGB_OK;
+  cudaSetDevice(qs->q->device);
+  cudaStreamSynchronize(qs->stream);
+  delete qs;
+  return HEOMGB_OK;
+}
+
+heomgb_status heomgb_qme_solver_solve(heomgb_qme_solver* qs, double* rho, const double* t_list, int n_t,
+                                      heomgb_callback cb, void* user, const heomgb_kwargs* kwargs) {
+  return guard([&] { solve_impl(qs, rho, true, t_list, n_t, cb, user, kwargs); });
+}
+
+heomgb_status heomgb_qme_solver_solve_device(heomgb_qme_solver* qs, void* rho, const double* t_list, int n_t,
+                                             heomgb_callback cb, void* user, const heomgb_kwargs* kwargs) {
+  return guard([&] { solve_impl(qs, rho, false, t_list, n_t, cb, user, kwargs); });
+}
+
+heomgb_status heomgb_qme_solver_stats(const heomgb_qme_solver* qs, long long* n_rhs, long long* n_attempts,
+                                      long long* n_accepted, double* dt_save) {
+  return guard([&] {
+    require(qs != nullptr, "null qme_solver");
+    if (n_rhs) *n_rhs = qs->n_rhs;
+    if (n_attempts) *n_attempts = qs->n_attempts;
+    if (n_accepted) *n_accepted = qs->n_accepted;
+    if (dt_save) *dt_save = qs->dt_save;
+  });
+}
+
+size_t heomgb_errnrm1_scratch(long long n) { return static_cast<size_t>(errnrm1_grid(n > 0 ? n : 1)) + 2; }
+
+heomgb_status heomgb_qme_solver_timing(const heomgb_qme_solver* qs, double* busy_ms, long long* kernels) {
+  return guard([&] {
+    require(qs != nullptr, "null qme_solver");
+    if (busy_ms) *busy_ms = qs->busy_ms;
+    if (kernels) *kernels = qs->replayed_kernels;
+  });
+}
+
+heomgb_status heomgb_errnrm1_device(const void* e, const void* x1, const void* x2, double atol, double rtol,
+                                    long long n, double* scratch, double* result, void* cuda_stream) {
+  return guard([&] {
+    require(e && x1 && x2 && scratch && result, "null argument");
+    require(n > 0, "n must be > 0");
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    const int grid = errnrm1_grid(n);
+    double* out = scratch + grid;
+    unsigned int* counter = reinterpret_cast<unsigned int*>(scratch + grid + 1);
+    ck(cudaMemsetAsync(counter, 0, sizeof(unsigned int), s), "memset counter");
+    ck(launch_errnrm1(static_cast<const double2*>(e), static_cast<const double2*>(x1),
+                      static_cast<const double2*>(x2), atol, rtol, n, scratch, out, counter, grid, s),
+       "errnrm1");
+    ck(cudaMemcpyAsync(result, out, sizeof(double), cudaMemcpyDeviceToHost, s), "errnrm1 result");
+    ck(cudaStreamSynchronize(s), "errnrm1 sync");
+  });
+}
+
+}  // extern "C"

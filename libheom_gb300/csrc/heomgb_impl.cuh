@@ -1,0 +1,133 @@
+// Internal declarations shared by the kernels (kernels.cu) and the C ABI (api.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace heomgb {
+
+// Which epilogue a right-hand-side launch runs after computing D for its elements.
+//   DIFF   out = beta*out - alpha*D                        (heom_hilb.h:354-355)
+//   RK4_s  classic RK4 stage s, accumulation fused         (solver/rk4.h:40-65)
+//   LS     2N-storage RK4 stage                            (solver/lsrk4.h:32-47)
+//   DP     Dormand-Prince stage 1..6                       (solver/rkdp.h:111-132)
+//   DP7    Dormand-Prince stage 7 + error norm + control   (solver/rkdp.h:136-177)
+enum EpiKind : int { EPI_DIFF = 0, EPI_RK4_1, EPI_RK4_2, EPI_RK4_3, EPI_RK4_4, EPI_LS, EPI_DP, EPI_DP7 };
+
+// Device-resident step control state.  The Dormand-Prince controller
+// (rkdp.h:150-177, adaptive_step_size_solver.h:45-55) runs on the device in
+// the last CTA of the stage-7 launch, so an attempt needs no host round trip.
+struct DpCtl {
+  double t, dt, t_bound, atol, rtol, err;
+  double dt_fixed;          // step of the fixed-step integrators
+  int cur;                  // index of the current state buffer (0/1)
+  int count;                // attempts in the current step (give up after 1000)
+  int done;                 // the output interval is finished
+  int status;               // 0 ok; nonzero: numeric failure
+  long long attempts, accepted;
+  unsigned int arrive;      // CTA arrival counter of the error-norm reduction
+  unsigned int pad;
+};
+
+// Per-model constants of the right-hand side (all device pointers).
+struct RhsModel {
+  int n, n2, K, U, n_hrchy;
+  int h_real;                       // H has zero imaginary part
+  const int* p1;                    // (n_hrchy+1)*K, sentinel n_hrchy
+  const int* m1;                    // (n_hrchy+1)*K
+  const int* nidx;                  // n_hrchy*K
+  const double2* ngd;               // n_hrchy: sum_k n_k gamma_kk
+  const float2* ngd_f;
+  const double2* H;                 // n2
+  const float2* H_f;
+  // diagonal-V path: per element e=(a,b), the modes whose bath couples e,
+  // with nonzero coefficients only:
+  //   +1 term  c_plus  = i(v_a - v_b) sigma_k                      (plus_ptr/plus_mode)
+  //   -1 term  c_minus = i(v_a - v_b) s_k - (v_a + v_b) a_k, x n_k  (minus_ptr/minus_mode)
+  const int* plus_ptr;              // n2+1
+  const int* plus_mode;
+  const int* minus_ptr;             // n2+1
+  const int* minus_mode;
+  const double2* c_plus;
+  const double2* c_minus;
+  const float2* c_plus_f;
+  const float2* c_minus_f;
+  const double2* c_sd;              // n2: sum_u s_delta_u (v_ua - v_ub)^2
+  const float2* c_sd_f;
+  // general-V and Liouville paths
+  const double2* V;                 // U*n2
+  const float2* V_f;
+  const int* bath_ptr;              // U+1: linear modes of bath u
+  const double2* sigma;             // K
+  const double2* s;                 // K
+  const double2* a;                 // K
+  const double2* sdelta;            // U
+  const float2* sigma_f;
+  const float2* s_f;
+  const float2* a_f;
+  const float2* sdelta_f;
+  // Liouville path: CSR superoperators (n2 x n2): R_0 = L + sum_u Xi_u, Phi_u, Psi_u
+  const int* r0_ptr;                // n2+1
+  const int* r0_idx;
+  const double2* r0_val;
+  const float2* r0_val_f;
+  const int* phi_ptr;               // U*(n2+1), offsets into phi_idx/phi_val
+  const int* phi_idx;
+  const double2* phi_val;
+  const float2* phi_val_f;
+  const int* psi_ptr;
+  const int* psi_idx;
+  const double2* psi_val;
+  const float2* psi_val_f;
+};
+
+// Arguments of one fused right-hand-side + stage launch.
+struct Stage {
+  int kind;                  // EpiKind
+  int dp_stage;              // EPI_DP: 0..5
+  int y_sel;                 // RHS input: 0 y_fixed, 1 Yb[cur], 2 Yb[1-cur]
+  int beta_zero;             // EPI_DIFF: beta == 0 (output not read)
+  const void* y_fixed;
+  double2 alpha, beta;       // EPI_DIFF
+  double2* out;              // EPI_DIFF
+  DpCtl* ctl;                // dt, cur, reduction state (solver stages)
+  double2* S[2];             // FP64 state buffers
+  void* Yb[2];               // bulk-precision copies of S (alias S in FP64 mode)
+  void* Ynext;               // bulk stage input written by this stage
+  double2* acc;              // RK4 accumulator / LSRK4 buffer (FP64)
+  void* K[6];                // Dormand-Prince stage vectors (bulk precision)
+  double coef;               // LSRK4 stage weight
+  int ls_first;              // LSRK4 stage 1 (beta = 0)
+  int ls_in;                 // LSRK4 input buffer index
+  int bulk_separate;         // Yb are separate (mixed precision) buffers
+  double* partials;          // EPI_DP7 per-CTA partial sums
+};
+
+enum Path : int { PATH_DIAG = 0, PATH_GENERAL = 1, PATH_LIOU = 2 };
+
+// Launchers (kernels.cu).  `mixed` selects FP32 bulk arithmetic; `in_double`
+// says the RHS input is a double2 array even in mixed mode.
+cudaError_t launch_rhs(const RhsModel& m, const Stage& st, int path, bool mixed, bool in_double, int grid,
+                       int block, cudaStream_t s);
+int rhs_block_size(const RhsModel& m, int path);
+int rhs_grid_size(const RhsModel& m, int path, int block, int n_sm);
+size_t rhs_smem_bytes(const RhsModel& m, int path, bool mixed);
+
+cudaError_t launch_hrchy_build(int K, int depth, int n_hrchy, const long long* binom, int binom_dim, int* nidx,
+                               int* p1, int* m1, cudaStream_t s);
+cudaError_t launch_ngd(int K, int n_hrchy, const int* nidx, const double2* gdiag, double2* ngd, float2* ngd_f,
+                       cudaStream_t s);
+cudaError_t launch_to_bulk(const double2* src, float2* dst, long long n, cudaStream_t s);
+cudaError_t launch_ctl_init(DpCtl* c, double t, double dt, double t_bound, double atol, double rtol, int cur,
+                            cudaStream_t s);
+cudaError_t launch_ctl_set_fixed(DpCtl* c, double dt, cudaStream_t s);
+cudaError_t launch_errnrm1(const double2* e, const double2* x1, const double2* x2, double atol, double rtol,
+                           long long n, double* partials, double* out, unsigned int* counter, int grid,
+                           cudaStream_t s);
+int errnrm1_grid(long long n);
+
+extern long long g_launches;  // kernels launched (incremented by the launchers / graph replays)
+
+}  // namespace heomgb

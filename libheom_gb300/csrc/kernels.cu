@@ -1,0 +1,798 @@
+// Device kernels of the HEOM engine: hierarchy construction, the fused
+// right-hand side with its Runge-Kutta stage epilogues, the Dormand-Prince
+// error norm and step control, and small helpers.
+//
+// Layout in HBM (the reference's `main` vector, heom_hilb.h:45-49): ADO l's
+// n x n matrix is contiguous, row-major, at offset l*n^2; element e = a*n+b.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <type_traits>
+
+#include "heomgb_impl.cuh"
+
+namespace heomgb {
+
+long long g_launches = 0;
+
+// ------------------------------------------------------------------ complex helpers
+template <typename T> struct CT;
+template <> struct CT<double> { using type = double2; };
+template <> struct CT<float> { using type = float2; };
+template <typename T> using cx_t = typename CT<T>::type;
+
+template <typename T> __device__ __forceinline__ cx_t<T> cx(T re, T im);
+template <> __device__ __forceinline__ double2 cx<double>(double re, double im) { return make_double2(re, im); }
+template <> __device__ __forceinline__ float2 cx<float>(float re, float im) { return make_float2(re, im); }
+
+template <typename TC> __device__ __forceinline__ cx_t<TC> ldc(const double2* p) {
+  const double2 v = __ldg(p);
+  return cx<TC>(static_cast<TC>(v.x), static_cast<TC>(v.y));
+}
+template <typename TC> __device__ __forceinline__ cx_t<TC> ldc(const float2* p) {
+  const float2 v = __ldg(p);
+  return cx<TC>(static_cast<TC>(v.x), static_cast<TC>(v.y));
+}
+// acc += a*b
+template <typename C> __device__ __forceinline__ void cfma(C& acc, C a, C b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+}
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 to_d(double2 v) { return v; }
+__device__ __forceinline__ double2 to_d(float2 v) { return make_double2(v.x, v.y); }
+
+template <typename TC> __device__ __forceinline__ const cx_t<TC>* pick(const double2* d, const float2* f);
+template <> __device__ __forceinline__ const double2* pick<double>(const double2* d, const float2*) { return d; }
+template <> __device__ __forceinline__ const float2* pick<float>(const double2*, const float2* f) { return f; }
+
+// bulk-precision vector access: bulk is float2 in mixed mode, double2 otherwise
+template <typename TC> __device__ __forceinline__ void st_bulk(void* base, size_t g, double2 v) {
+  if constexpr (std::is_same<TC, double>::value) {
+    static_cast<double2*>(base)[g] = v;
+  } else {
+    static_cast<float2*>(base)[g] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+  }
+}
+template <typename TC> __device__ __forceinline__ double2 ld_bulk(const void* base, size_t g) {
+  if constexpr (std::is_same<TC, double>::value) {
+    return static_cast<const double2*>(base)[g];
+  } else {
+    return to_d(static_cast<const float2*>(base)[g]);
+  }
+}
+// value a bulk vector will hold after a store (rounding in mixed mode)
+template <typename TC> __device__ __forceinline__ double2 as_bulk(double2 v) {
+  if constexpr (std::is_same<TC, double>::value) {
+    return v;
+  } else {
+    return make_double2(static_cast<float>(v.x), static_cast<float>(v.y));
+  }
+}
+
+// ------------------------------------------------------------------ Dormand-Prince tableau (rkdp.h:21-57)
+__constant__ double c_dpA[7][6] = {
+    {0, 0, 0, 0, 0, 0},
+    {1.0 / 5, 0, 0, 0, 0, 0},
+    {3.0 / 40, 9.0 / 40, 0, 0, 0, 0},
+    {44.0 / 45, -56.0 / 15, 32.0 / 9, 0, 0, 0},
+    {19372.0 / 6561, -25360.0 / 2187, 64448.0 / 6561, -212.0 / 729, 0, 0},
+    {9017.0 / 3168, -355.0 / 33, 46732.0 / 5247, 49.0 / 176, -5103.0 / 18656, 0},
+    {35.0 / 384, 0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84}};
+__constant__ double c_dpE[7] = {-71.0 / 57600, 0, 71.0 / 16695, -71.0 / 1920, 17253.0 / 339200, -22.0 / 525,
+                                1.0 / 40};
+
+// ------------------------------------------------------------------ step control
+// rkdp.h:150-177 and adaptive_step_size_solver.h:45-55, one thread.
+__device__ void dp_control(DpCtl* c, double sumsq, long long n) {
+  const double err = sqrt(sumsq) / sqrt(static_cast<double>(n));
+  c->err = err;
+  c->attempts += 1;
+  c->count += 1;
+  const double fac = pow(err, -0.2);
+  if (err < 1.0) {
+    c->t += c->dt;
+    c->dt *= 0.9 * ((fac < 10.0) ? fac : 10.0);
+    c->cur ^= 1;
+    c->accepted += 1;
+    c->count = 0;
+    if (c->t >= c->t_bound) c->done = 1;
+  } else {
+    c->dt *= 0.9 * ((0.2 < fac) ? fac : 0.2);
+    if (c->dt < 1e-16) c->dt = 1e-16;
+    if (c->count >= 1000) {  // the 1001st attempt gives up (rkdp.h:98-102)
+      c->t = c->t_bound;
+      c->count = 0;
+      c->done = 1;
+    }
+  }
+  if (!c->done && c->t + c->dt > c->t_bound) c->dt = c->t_bound - c->t;
+  if (!isfinite(c->dt) || !isfinite(c->t)) {
+    c->status = 1;
+    c->done = 1;
+  }
+}
+
+// ------------------------------------------------------------------ fused stage epilogue
+// D is the operator value of heom_hilb.h:96-353 at element g; every solver
+// stage uses k = -dt*D (calc_diff_impl with alpha = dt, beta = 0).  Returns
+// the element's squared scaled error for EPI_DP7, else 0.
+template <typename TC>
+__device__ __forceinline__ double epilogue(const Stage& st, size_t g, double2 D, double dt, int cur) {
+  switch (st.kind) {
+    case EPI_DIFF: {
+      double2 o = st.beta_zero ? make_double2(0.0, 0.0) : cmul(st.beta, st.out[g]);
+      const double2 ad = cmul(st.alpha, D);
+      st.out[g] = make_double2(o.x - ad.x, o.y - ad.y);
+      return 0.0;
+    }
+    case EPI_RK4_1: {  // rho_n = rho + k1/2 ; acc = rho + k1/6
+      const double2 k = make_double2(-dt * D.x, -dt * D.y);
+      const double2 s = st.S[0][g];
+      st_bulk<TC>(st.Ynext, g, make_double2(s.x + 0.5 * k.x, s.y + 0.5 * k.y));
+      st.acc[g] = make_double2(s.x + (1.0 / 6.0) * k.x, s.y + (1.0 / 6.0) * k.y);
+      return 0.0;
+    }
+    case EPI_RK4_2:
+    case EPI_RK4_3: {  // rho_n = rho + c*k ; acc += k/3   (2/6 applied to k2+k3)
+      const double2 k = make_double2(-dt * D.x, -dt * D.y);
+      const double2 s = st.S[0][g];
+      const double c = st.kind == EPI_RK4_2 ? 0.5 : 1.0;
+      st_bulk<TC>(st.Ynext, g, make_double2(s.x + c * k.x, s.y + c * k.y));
+      double2 a = st.acc[g];
+      st.acc[g] = make_double2(a.x + (2.0 / 6.0) * k.x, a.y + (2.0 / 6.0) * k.y);
+      return 0.0;
+    }
+    case EPI_RK4_4: {  // rho = acc + k4/6
+      const double2 k = make_double2(-dt * D.x, -dt * D.y);
+      const double2 a = st.acc[g];
+      const double2 v = make_double2(a.x + (1.0 / 6.0) * k.x, a.y + (1.0 / 6.0) * k.y);
+      st.S[0][g] = v;
+      if (st.bulk_separate) st_bulk<TC>(st.Yb[0], g, v);
+      return 0.0;
+    }
+    case EPI_LS: {  // buff = -buff + k (beta=-1) or k (beta=0); rho += B*buff
+      const double2 k = make_double2(-dt * D.x, -dt * D.y);
+      double2 b = k;
+      if (!st.ls_first) {
+        const double2 o = st.acc[g];
+        b = make_double2(-o.x + k.x, -o.y + k.y);
+      }
+      st.acc[g] = b;
+      const double2 s = st.S[st.ls_in][g];
+      const double2 v = make_double2(s.x + st.coef * b.x, s.y + st.coef * b.y);
+      st.S[1 - st.ls_in][g] = v;
+      if (st.bulk_separate) st_bulk<TC>(st.Yb[1 - st.ls_in], g, v);
+      return 0.0;
+    }
+    case EPI_DP: {  // store k_s; next stage input rho + sum_j A[s+1][j] k_j
+      const int s_ = st.dp_stage;
+      const double2 k = as_bulk<TC>(make_double2(-dt * D.x, -dt * D.y));
+      st_bulk<TC>(st.K[s_], g, k);
+      double2 y = st.S[cur][g];
+      for (int j = 0; j < s_; ++j) {
+        const double c = c_dpA[s_ + 1][j];
+        const double2 kj = ld_bulk<TC>(st.K[j], g);
+        y.x += c * kj.x;
+        y.y += c * kj.y;
+      }
+      const double c = c_dpA[s_ + 1][s_];
+      y.x += c * k.x;
+      y.y += c * k.y;
+      if (s_ < 5) {
+        st_bulk<TC>(st.Ynext, g, y);
+      } else {  // the candidate state rho + sum B_j k_j
+        st.S[1 - cur][g] = y;
+        if (st.bulk_separate) st_bulk<TC>(st.Yb[1 - cur], g, y);
+      }
+      return 0.0;
+    }
+    case EPI_DP7: {  // e = sum_j E_j k_j ; scaled squared error (linalg_engine_cuda.cu:102-146)
+      const double2 k7 = make_double2(-dt * D.x, -dt * D.y);
+      const double2 k0 = ld_bulk<TC>(st.K[0], g);
+      double2 e = make_double2(c_dpE[0] * k0.x, c_dpE[0] * k0.y);
+      for (int j = 1; j < 6; ++j) {
+        const double2 kj = ld_bulk<TC>(st.K[j], g);
+        e.x += c_dpE[j] * kj.x;
+        e.y += c_dpE[j] * kj.y;
+      }
+      e.x += c_dpE[6] * k7.x;
+      e.y += c_dpE[6] * k7.y;
+      const double2 x1 = st.S[1 - cur][g];
+      const double2 x2 = st.S[cur][g];
+      const double m = fmax(hypot(x1.x, x1.y), hypot(x2.x, x2.y));
+      const double q = hypot(e.x, e.y) / (st.ctl->atol + st.ctl->rtol * m);
+      return q * q;
+    }
+    default:
+      return 0.0;
+  }
+}
+
+// Block-level sum of `v`; result valid in thread 0.
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double warp_part[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) warp_part[w] = v;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  v = 0.0;
+  if (w == 0) {
+    v = lane < nw ? warp_part[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  }
+  __syncthreads();
+  return v;
+}
+
+// Grid-level finish of the stage-7 error norm: every CTA deposits its partial
+// sum; the last CTA to arrive adds them in index order (deterministic) and
+// runs the step controller.  No CTA waits on another.
+__device__ void dp7_finish(const Stage& st, double local, long long n_total) {
+  const double part = block_sum(local);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    st.partials[blockIdx.x] = part;
+    __threadfence();
+    const unsigned int ticket = atomicAdd(&st.ctl->arrive, 1u);
+    last = (ticket == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double v = 0.0;
+  for (int i = threadIdx.x; i < static_cast<int>(gridDim.x); i += blockDim.x) v += __ldcg(st.partials + i);
+  v = block_sum(v);
+  if (threadIdx.x == 0) {
+    st.ctl->arrive = 0;
+    dp_control(st.ctl, v, n_total);
+  }
+}
+
+template <typename TB>
+__device__ __forceinline__ const TB* stage_input(const Stage& st, int cur) {
+  if (st.y_sel == 1) return static_cast<const TB*>(st.Yb[cur]);
+  if (st.y_sel == 2) return static_cast<const TB*>(st.Yb[1 - cur]);
+  return static_cast<const TB*>(st.y_fixed);
+}
+
+// Reads the step size and the current buffer index; false if the launch has
+// nothing to do (interval finished or failed).
+__device__ __forceinline__ bool stage_prologue(const Stage& st, double& dt, int& cur) {
+  dt = 0.0;
+  cur = 0;
+  if (st.ctl) {
+    if (st.ctl->done || st.ctl->status) return false;
+    dt = (st.kind == EPI_DP || st.kind == EPI_DP7) ? st.ctl->dt : st.ctl->dt_fixed;
+    cur = st.ctl->cur;
+  }
+  return true;
+}
+
+// ------------------------------------------------------------------ RHS, diagonal V
+// For every bath u with diagonal V_u the coupling terms are elementwise:
+// [V,X]_ab = (v_a - v_b) X_ab and {V,X}_ab = (v_a + v_b) X_ab, so element e
+// only needs the neighbour ADOs of the modes whose bath couples e.
+template <typename TC, typename TB, bool HREAL>
+__global__ void __launch_bounds__(256) k_rhs_diag(const RhsModel m, const Stage st) {
+  using C = cx_t<TC>;
+  double dt;
+  int cur;
+  if (!stage_prologue(st, dt, cur)) return;
+  const TB* __restrict__ y = stage_input<TB>(st, cur);
+  const int n = m.n, n2 = m.n2, K = m.K, void_idx = m.n_hrchy;
+  const long long total = static_cast<long long>(m.n_hrchy) * n2;
+  const C* __restrict__ H = pick<TC>(m.H, m.H_f);
+  const C* __restrict__ ngd = pick<TC>(m.ngd, m.ngd_f);
+  const C* __restrict__ cpl = pick<TC>(m.c_plus, m.c_plus_f);
+  const C* __restrict__ cmi = pick<TC>(m.c_minus, m.c_minus_f);
+  const C* __restrict__ csd = pick<TC>(m.c_sd, m.c_sd_f);
+  double local = 0.0;
+  for (long long g = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; g < total;
+       g += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int l = static_cast<int>(g / n2);
+    const int e = static_cast<int>(g - static_cast<long long>(l) * n2);
+    const int a = e / n, b = e - a * n;
+    const TB* __restrict__ yl = y + static_cast<size_t>(l) * n2;
+    // i[H, rho]
+    C acc = cx<TC>(0, 0);
+    if (HREAL) {
+      for (int c = 0; c < n; ++c) {
+        const TC hac = H[a * n + c].x, hcb = H[c * n + b].x;
+        const C ycb = ldc<TC>(yl + c * n + b), yac = ldc<TC>(yl + a * n + c);
+        acc.x = fma(hac, ycb.x, acc.x);
+        acc.x = fma(-hcb, yac.x, acc.x);
+        acc.y = fma(hac, ycb.y, acc.y);
+        acc.y = fma(-hcb, yac.y, acc.y);
+      }
+    } else {
+      C neg = cx<TC>(0, 0);
+      for (int c = 0; c < n; ++c) {
+        cfma(acc, H[a * n + c], ldc<TC>(yl + c * n + b));
+        cfma(neg, ldc<TC>(yl + a * n + c), H[c * n + b]);
+      }
+      acc.x -= neg.x;
+      acc.y -= neg.y;
+    }
+    C D = cx<TC>(-acc.y, acc.x);
+    // (sum_k n_k gamma_k + sum_u s_delta_u (v_a - v_b)^2) rho
+    const C ye = ldc<TC>(yl + e);
+    const C g0 = ngd[l], g1 = csd[e];
+    cfma(D, cx<TC>(g0.x + g1.x, g0.y + g1.y), ye);
+    // bath couplings of this element's modes
+    const int* __restrict__ p1row = m.p1 + static_cast<size_t>(l) * K;
+    const int* __restrict__ m1row = m.m1 + static_cast<size_t>(l) * K;
+    const int* __restrict__ nrow = m.nidx + static_cast<size_t>(l) * K;
+    const int pe = __ldg(m.plus_ptr + e + 1);
+    for (int p = __ldg(m.plus_ptr + e); p < pe; ++p) {
+      const int lp = __ldg(p1row + __ldg(m.plus_mode + p));
+      if (lp != void_idx) cfma(D, cpl[p], ldc<TC>(y + static_cast<size_t>(lp) * n2 + e));
+    }
+    const int me = __ldg(m.minus_ptr + e + 1);
+    for (int p = __ldg(m.minus_ptr + e); p < me; ++p) {
+      const int k = __ldg(m.minus_mode + p);
+      const int lm = __ldg(m1row + k);
+      if (lm != void_idx) {
+        const TC nk = static_cast<TC>(__ldg(nrow + k));
+        const C cm = cmi[p];
+        cfma(D, cx<TC>(nk * cm.x, nk * cm.y), ldc<TC>(y + static_cast<size_t>(lm) * n2 + e));
+      }
+    }
+    local += epilogue<TC>(st, static_cast<size_t>(g), to_d(D), dt, cur);
+  }
+  if (st.kind == EPI_DP7) dp7_finish(st, local, total);
+}
+
+// ------------------------------------------------------------------ RHS, general V
+// One CTA per ADO at a time; Phi_u / Psi_u (heom_hilb.h:311-342) and the
+// commutators are formed in shared memory for any dense V_u.
+template <typename TC, typename TB>
+__global__ void __launch_bounds__(256) k_rhs_general(const RhsModel m, const Stage st) {
+  using C = cx_t<TC>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double dt;
+  int cur;
+  if (!stage_prologue(st, dt, cur)) return;
+  const TB* __restrict__ y = stage_input<TB>(st, cur);
+  const int n = m.n, n2 = m.n2, K = m.K, void_idx = m.n_hrchy;
+  C* ys = reinterpret_cast<C*>(smem_raw);
+  C* Dm = ys + n2;
+  C* Phi = Dm + n2;
+  C* Psi = Phi + n2;
+  C* T = Psi + n2;
+  const C* __restrict__ H = pick<TC>(m.H, m.H_f);
+  const C* __restrict__ Vall = pick<TC>(m.V, m.V_f);
+  const C* __restrict__ ngd = pick<TC>(m.ngd, m.ngd_f);
+  const C* __restrict__ sig = pick<TC>(m.sigma, m.sigma_f);
+  const C* __restrict__ sv = pick<TC>(m.s, m.s_f);
+  const C* __restrict__ av = pick<TC>(m.a, m.a_f);
+  const C* __restrict__ sd = pick<TC>(m.sdelta, m.sdelta_f);
+  double local = 0.0;
+  for (int l = blockIdx.x; l < m.n_hrchy; l += gridDim.x) {
+    const TB* yl = y + static_cast<size_t>(l) * n2;
+    for (int e = threadIdx.x; e < n2; e += blockDim.x) ys[e] = ldc<TC>(yl + e);
+    __syncthreads();
+    const C gl = ngd[l];
+    for (int e = threadIdx.x; e < n2; e += blockDim.x) {
+      const int a = e / n, b = e - a * n;
+      C acc = cx<TC>(0, 0), neg = cx<TC>(0, 0);
+      for (int c = 0; c < n; ++c) {
+        cfma(acc, H[a * n + c], ys[c * n + b]);
+        cfma(neg, ys[a * n + c], H[c * n + b]);
+      }
+      C D = cx<TC>(-(acc.y - neg.y), acc.x - neg.x);
+      cfma(D, gl, ys[e]);
+      Dm[e] = D;
+    }
+    for (int u = 0; u < m.U; ++u) {
+      const C* V = Vall + static_cast<size_t>(u) * n2;
+      const C sdu = sd[u];
+      __syncthreads();
+      if (sdu.x != TC(0) || sdu.y != TC(0)) {  // s_delta [V, [V, rho]]
+        for (int e = threadIdx.x; e < n2; e += blockDim.x) {
+          const int a = e / n, b = e - a * n;
+          C acc = cx<TC>(0, 0), neg = cx<TC>(0, 0);
+          for (int c = 0; c < n; ++c) {
+            cfma(acc, V[a * n + c], ys[c * n + b]);
+            cfma(neg, ys[a * n + c], V[c * n + b]);
+          }
+          T[e] = cx<TC>(acc.x - neg.x, acc.y - neg.y);
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < n2; e += blockDim.x) {
+          const int a = e / n, b = e - a * n;
+          C acc = cx<TC>(0, 0), neg = cx<TC>(0, 0);
+          for (int c = 0; c < n; ++c) {
+            cfma(acc, V[a * n + c], T[c * n + b]);
+            cfma(neg, T[a * n + c], V[c * n + b]);
+          }
+          cfma(Dm[e], sdu, cx<TC>(acc.x - neg.x, acc.y - neg.y));
+        }
+      }
+      // Phi = sum sigma_k rho_{n+1_k} + n_k s_k rho_{n-1_k};  Psi = -sum n_k a_k rho_{n-1_k}
+      const int k0 = __ldg(m.bath_ptr + u), k1 = __ldg(m.bath_ptr + u + 1);
+      for (int e = threadIdx.x; e < n2; e += blockDim.x) {
+        C ph = cx<TC>(0, 0), ps = cx<TC>(0, 0);
+        for (int k = k0; k < k1; ++k) {
+          const int lp = __ldg(m.p1 + static_cast<size_t>(l) * K + k);
+          if (lp != void_idx) cfma(ph, sig[k], ldc<TC>(y + static_cast<size_t>(lp) * n2 + e));
+        }
+        for (int k = k0; k < k1; ++k) {
+          const int lm = __ldg(m.m1 + static_cast<size_t>(l) * K + k);
+          if (lm != void_idx) {
+            const TC nk = static_cast<TC>(__ldg(m.nidx + static_cast<size_t>(l) * K + k));
+            const C r = ldc<TC>(y + static_cast<size_t>(lm) * n2 + e);
+            cfma(ph, cx<TC>(nk * sv[k].x, nk * sv[k].y), r);
+            cfma(ps, cx<TC>(-nk * av[k].x, -nk * av[k].y), r);
+          }
+        }
+        Phi[e] = ph;
+        Psi[e] = ps;
+      }
+      __syncthreads();
+      // i[V, Phi] + {V, Psi}
+      for (int e = threadIdx.x; e < n2; e += blockDim.x) {
+        const int a = e / n, b = e - a * n;
+        C c1 = cx<TC>(0, 0), c1n = cx<TC>(0, 0), c2 = cx<TC>(0, 0);
+        for (int c = 0; c < n; ++c) {
+          const C vac = V[a * n + c], vcb = V[c * n + b];
+          cfma(c1, vac, Phi[c * n + b]);
+          cfma(c1n, Phi[a * n + c], vcb);
+          cfma(c2, vac, Psi[c * n + b]);
+          cfma(c2, Psi[a * n + c], vcb);
+        }
+        C D = Dm[e];
+        D.x += -(c1.y - c1n.y) + c2.x;
+        D.y += (c1.x - c1n.x) + c2.y;
+        Dm[e] = D;
+      }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n2; e += blockDim.x)
+      local += epilogue<TC>(st, static_cast<size_t>(l) * n2 + e, to_d(Dm[e]), dt, cur);
+    __syncthreads();
+  }
+  if (st.kind == EPI_DP7) dp7_finish(st, local, static_cast<long long>(m.n_hrchy) * n2);
+}
+
+// ------------------------------------------------------------------ RHS, Liouville (block-sparse SpMV)
+// heom_liou (heom_liou.h:121-258) and heom_ado (heom_ado.h:191-202): block
+// row l of the global generator is (ngamma_l I + R_0) on ADO l, sigma_k Phi_u
+// on ADO n+1_k and n_k (s_k Phi_u - a_k Psi_u) on ADO n-1_k.  The blocks are
+// the shared CSR superoperators scaled by per-ADO scalars, so the block
+// pattern comes from the hierarchy tables and R is never materialised.
+template <typename TC, typename TB>
+__global__ void __launch_bounds__(256) k_rhs_liou(const RhsModel m, const Stage st) {
+  using C = cx_t<TC>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double dt;
+  int cur;
+  if (!stage_prologue(st, dt, cur)) return;
+  const TB* __restrict__ y = stage_input<TB>(st, cur);
+  const int n2 = m.n2, K = m.K, void_idx = m.n_hrchy;
+  C* ys = reinterpret_cast<C*>(smem_raw);
+  C* Dm = ys + n2;
+  C* TPhi = Dm + n2;
+  C* TPsi = TPhi + n2;
+  const C* __restrict__ ngd = pick<TC>(m.ngd, m.ngd_f);
+  const C* __restrict__ r0v = pick<TC>(m.r0_val, m.r0_val_f);
+  const C* __restrict__ phv = pick<TC>(m.phi_val, m.phi_val_f);
+  const C* __restrict__ psv = pick<TC>(m.psi_val, m.psi_val_f);
+  const C* __restrict__ sig = pick<TC>(m.sigma, m.sigma_f);
+  const C* __restrict__ sv = pick<TC>(m.s, m.s_f);
+  const C* __restrict__ av = pick<TC>(m.a, m.a_f);
+  double local = 0.0;
+  for (int l = blockIdx.x; l < m.n_hrchy; l += gridDim.x) {
+    const TB* yl = y + static_cast<size_t>(l) * n2;
+    for (int e = threadIdx.x; e < n2; e += blockDim.x) ys[e] = ldc<TC>(yl + e);
+    __syncthreads();
+    const C gl = ngd[l];
+    for (int r = threadIdx.x; r < n2; r += blockDim.x) {
+      C D = cx<TC>(0, 0);
+      for (int p = __ldg(m.r0_ptr + r); p < __ldg(m.r0_ptr + r + 1); ++p) cfma(D, r0v[p], ys[__ldg(m.r0_idx + p)]);
+      cfma(D, gl, ys[r]);
+      Dm[r] = D;
+    }
+    for (int u = 0; u < m.U; ++u) {
+      const int k0 = __ldg(m.bath_ptr + u), k1 = __ldg(m.bath_ptr + u + 1);
+      for (int e = threadIdx.x; e < n2; e += blockDim.x) {
+        C ph = cx<TC>(0, 0), ps = cx<TC>(0, 0);
+        for (int k = k0; k < k1; ++k) {
+          const int lp = __ldg(m.p1 + static_cast<size_t>(l) * K + k);
+          if (lp != void_idx) cfma(ph, sig[k], ldc<TC>(y + static_cast<size_t>(lp) * n2 + e));
+        }
+        for (int k = k0; k < k1; ++k) {
+          const int lm = __ldg(m.m1 + static_cast<size_t>(l) * K + k);
+          if (lm != void_idx) {
+            const TC nk = static_cast<TC>(__ldg(m.nidx + static_cast<size_t>(l) * K + k));
+            const C r = ldc<TC>(y + static_cast<size_t>(lm) * n2 + e);
+            cfma(ph, cx<TC>(nk * sv[k].x, nk * sv[k].y), r);
+            cfma(ps, cx<TC>(-nk * av[k].x, -nk * av[k].y), r);
+          }
+        }
+        TPhi[e] = ph;
+        TPsi[e] = ps;
+      }
+      __syncthreads();
+      const int* pp = m.phi_ptr + static_cast<size_t>(u) * (n2 + 1);
+      const int* qp = m.psi_ptr + static_cast<size_t>(u) * (n2 + 1);
+      for (int r = threadIdx.x; r < n2; r += blockDim.x) {
+        C D = Dm[r];
+        for (int p = __ldg(pp + r); p < __ldg(pp + r + 1); ++p) cfma(D, phv[p], TPhi[__ldg(m.phi_idx + p)]);
+        for (int p = __ldg(qp + r); p < __ldg(qp + r + 1); ++p) cfma(D, psv[p], TPsi[__ldg(m.psi_idx + p)]);
+        Dm[r] = D;
+      }
+      __syncthreads();
+    }
+    for (int e = threadIdx.x; e < n2; e += blockDim.x)
+      local += epilogue<TC>(st, static_cast<size_t>(l) * n2 + e, to_d(Dm[e]), dt, cur);
+    __syncthreads();
+  }
+  if (st.kind == EPI_DP7) dp7_finish(st, local, static_cast<long long>(m.n_hrchy) * n2);
+}
+
+// ------------------------------------------------------------------ launch configuration
+int rhs_block_size(const RhsModel& m, int path) {
+  if (path != PATH_DIAG) {
+    int b = 32;
+    while (b < m.n2 && b < 256) b <<= 1;
+    return b;
+  }
+  // spread small problems over many SMs: the FP64 pipe per SM is narrow
+  const long long total = static_cast<long long>(m.n_hrchy) * m.n2;
+  int b = 32;
+  while (b < 256 && total / (2 * b) >= 152 * 4) b <<= 1;
+  return b;
+}
+
+int rhs_grid_size(const RhsModel& m, int path, int block, int n_sm) {
+  if (path != PATH_DIAG) {
+    const int per_sm = 4;
+    return static_cast<int>(std::min<long long>(m.n_hrchy, static_cast<long long>(n_sm) * per_sm * 4));
+  }
+  const long long total = static_cast<long long>(m.n_hrchy) * m.n2;
+  const long long want = (total + block - 1) / block;
+  const long long cap = static_cast<long long>(n_sm) * (2048 / block);
+  return static_cast<int>(std::max<long long>(1, std::min(want, cap)));
+}
+
+size_t rhs_smem_bytes(const RhsModel& m, int path, bool mixed) {
+  const size_t cb = mixed ? sizeof(float2) : sizeof(double2);
+  if (path == PATH_GENERAL) return 5 * cb * m.n2;
+  if (path == PATH_LIOU) return 4 * cb * m.n2;
+  return 0;
+}
+
+template <typename TC, typename TB>
+static cudaError_t launch_typed(const RhsModel& m, const Stage& st, int path, int grid, int block, cudaStream_t s) {
+  const size_t smem = rhs_smem_bytes(m, path, std::is_same<TC, float>::value);
+  if (path == PATH_DIAG) {
+    if (m.h_real)
+      k_rhs_diag<TC, TB, true><<<grid, block, 0, s>>>(m, st);
+    else
+      k_rhs_diag<TC, TB, false><<<grid, block, 0, s>>>(m, st);
+  } else if (path == PATH_GENERAL) {
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(k_rhs_general<TC, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(smem));
+      if (e != cudaSuccess) return e;
+    }
+    k_rhs_general<TC, TB><<<grid, block, smem, s>>>(m, st);
+  } else {
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(k_rhs_liou<TC, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(smem));
+      if (e != cudaSuccess) return e;
+    }
+    k_rhs_liou<TC, TB><<<grid, block, smem, s>>>(m, st);
+  }
+  ++g_launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rhs(const RhsModel& m, const Stage& st, int path, bool mixed, bool in_double, int grid,
+                       int block, cudaStream_t s) {
+  if (!mixed) return launch_typed<double, double2>(m, st, path, grid, block, s);
+  if (in_double) return launch_typed<float, double2>(m, st, path, grid, block, s);
+  return launch_typed<float, float2>(m, st, path, grid, block, s);
+}
+
+// ------------------------------------------------------------------ hierarchy on the device
+// Order of the reference's breadth-first enumeration (hrchy_space.cc:160-198):
+// tier |n| ascending, and within a tier descending lexicographic order of n.
+// binom is a (dim x dim) table of C(a, b), saturated where it would overflow.
+__device__ __forceinline__ long long binom_at(const long long* t, int dim, int a, int b) {
+  if (a < 0 || b < 0 || b > a) return 0;
+  return t[static_cast<size_t>(a) * dim + b];
+}
+
+// Rank of multi-index row (with `delta` added at mode `kk`) of total `tier`.
+__device__ int rank_of(const int* row, int K, int kk, int delta, int tier, const long long* bt, int bd) {
+  long long r = tier > 0 ? binom_at(bt, bd, K + tier - 1, K) : 0;
+  int s = tier;
+  for (int i = 0; i < K - 1; ++i) {
+    const int mi = row[i] + (i == kk ? delta : 0);
+    const int p = K - i - 1;
+    const int x = s - mi - 1;
+    if (x >= 0) r += binom_at(bt, bd, x + p, p);
+    s -= mi;
+    if (s == 0) break;
+  }
+  return static_cast<int>(r);
+}
+
+__global__ void k_hrchy_unrank(int K, int n_hrchy, const long long* bt, int bd, int* nidx) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= n_hrchy) return;
+  int* row = nidx + static_cast<size_t>(l) * K;
+  int d = 0;
+  while (binom_at(bt, bd, K + d, K) <= l) ++d;
+  long long r = l - (d > 0 ? binom_at(bt, bd, K + d - 1, K) : 0);
+  int s = d;
+  for (int i = 0; i < K; ++i) {
+    const int p = K - i - 1;
+    if (p == 0) {
+      row[i] = s;
+      break;
+    }
+    int v = s;
+    for (; v > 0; --v) {
+      const long long cnt = binom_at(bt, bd, s - v + p - 1, p - 1);
+      if (r < cnt) break;
+      r -= cnt;
+    }
+    row[i] = v;
+    s -= v;
+  }
+}
+
+__global__ void k_hrchy_links(int K, int depth, int n_hrchy, const long long* bt, int bd, const int* nidx, int* p1,
+                              int* m1) {
+  const long long gid = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  const long long total = static_cast<long long>(n_hrchy + 1) * K;
+  if (gid >= total) return;
+  const int l = static_cast<int>(gid / K), k = static_cast<int>(gid - static_cast<long long>(l) * K);
+  if (l == n_hrchy) {  // sentinel row
+    p1[gid] = n_hrchy;
+    m1[gid] = n_hrchy;
+    return;
+  }
+  const int* row = nidx + static_cast<size_t>(l) * K;
+  int tier = 0;
+  for (int i = 0; i < K; ++i) tier += row[i];
+  p1[gid] = (tier + 1 <= depth) ? rank_of(row, K, k, +1, tier + 1, bt, bd) : n_hrchy;
+  m1[gid] = (row[k] > 0) ? rank_of(row, K, k, -1, tier - 1, bt, bd) : n_hrchy;
+}
+
+cudaError_t launch_hrchy_build(int K, int depth, int n_hrchy, const long long* binom, int binom_dim, int* nidx,
+                               int* p1, int* m1, cudaStream_t s) {
+  if (K > 0) {
+    k_hrchy_unrank<<<(n_hrchy + 127) / 128, 128, 0, s>>>(K, n_hrchy, binom, binom_dim, nidx);
+    ++g_launches;
+    const long long total = static_cast<long long>(n_hrchy + 1) * K;
+    k_hrchy_links<<<static_cast<unsigned>((total + 255) / 256), 256, 0, s>>>(K, depth, n_hrchy, binom, binom_dim,
+                                                                            nidx, p1, m1);
+    ++g_launches;
+  }
+  return cudaGetLastError();
+}
+
+// ngamma_diag[l] = sum_k n_k gamma_kk, mode by mode without contraction (heom.h:94-104).
+__global__ void k_ngd(int K, int n_hrchy, const int* nidx, const double2* gdiag, double2* ngd, float2* ngd_f) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= n_hrchy) return;
+  double re = 0.0, im = 0.0;
+  for (int k = 0; k < K; ++k) {
+    const double nk = static_cast<double>(nidx[static_cast<size_t>(l) * K + k]);
+    re = __dadd_rn(re, __dmul_rn(nk, gdiag[k].x));
+    im = __dadd_rn(im, __dmul_rn(nk, gdiag[k].y));
+  }
+  ngd[l] = make_double2(re, im);
+  ngd_f[l] = make_float2(static_cast<float>(re), static_cast<float>(im));
+}
+
+cudaError_t launch_ngd(int K, int n_hrchy, const int* nidx, const double2* gdiag, double2* ngd, float2* ngd_f,
+                       cudaStream_t s) {
+  k_ngd<<<(n_hrchy + 127) / 128, 128, 0, s>>>(K, n_hrchy, nidx, gdiag, ngd, ngd_f);
+  ++g_launches;
+  return cudaGetLastError();
+}
+
+__global__ void k_to_bulk(const double2* src, float2* dst, long long n) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const double2 v = src[i];
+    dst[i] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+  }
+}
+
+cudaError_t launch_to_bulk(const double2* src, float2* dst, long long n, cudaStream_t s) {
+  const int grid = static_cast<int>(std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 8)));
+  k_to_bulk<<<grid, 256, 0, s>>>(src, dst, n);
+  ++g_launches;
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ controller set-up
+// Written by a kernel (stream-ordered, capturable) rather than by a host copy.
+__global__ void k_ctl_init(DpCtl* c, double t, double dt, double t_bound, double atol, double rtol, int cur) {
+  c->t = t;
+  c->dt = dt;
+  c->t_bound = t_bound;
+  c->atol = atol;
+  c->rtol = rtol;
+  c->err = 0.0;
+  c->dt_fixed = dt;
+  c->cur = cur;
+  c->count = 0;
+  c->done = 0;
+  c->status = 0;
+  c->attempts = 0;
+  c->accepted = 0;
+  c->arrive = 0;
+}
+
+__global__ void k_ctl_set_fixed(DpCtl* c, double dt) { c->dt_fixed = dt; }
+
+cudaError_t launch_ctl_init(DpCtl* c, double t, double dt, double t_bound, double atol, double rtol, int cur,
+                            cudaStream_t s) {
+  k_ctl_init<<<1, 1, 0, s>>>(c, t, dt, t_bound, atol, rtol, cur);
+  ++g_launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ctl_set_fixed(DpCtl* c, double dt, cudaStream_t s) {
+  k_ctl_set_fixed<<<1, 1, 0, s>>>(c, dt);
+  ++g_launches;
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ standalone error norm
+// errnrm1 of linalg_engine_cuda.cu:102-201 in one launch: per-CTA partials,
+// last CTA adds them in order and writes sqrt(sum/n).
+__global__ void k_errnrm1(const double2* e, const double2* x1, const double2* x2, double atol, double rtol,
+                          long long n, double* partials, double* out, unsigned int* counter) {
+  double local = 0.0;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const double2 a = e[i], b = x1[i], c = x2[i];
+    const double q = hypot(a.x, a.y) / (atol + rtol * fmax(hypot(b.x, b.y), hypot(c.x, c.y)));
+    local += q * q;
+  }
+  const double part = block_sum(local);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = part;
+    __threadfence();
+    last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double v = 0.0;
+  for (int i = threadIdx.x; i < static_cast<int>(gridDim.x); i += blockDim.x) v += __ldcg(partials + i);
+  v = block_sum(v);
+  if (threadIdx.x == 0) {
+    *out = sqrt(v / static_cast<double>(n));
+    *counter = 0;
+  }
+}
+
+int errnrm1_grid(long long n) {
+  return static_cast<int>(std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 4)));
+}
+
+cudaError_t launch_errnrm1(const double2* e, const double2* x1, const double2* x2, double atol, double rtol,
+                           long long n, double* partials, double* out, unsigned int* counter, int grid,
+                           cudaStream_t s) {
+  k_errnrm1<<<grid, 256, 0, s>>>(e, x1, x2, atol, rtol, n, partials, out, counter);
+  ++g_launches;
+  return cudaGetLastError();
+}
+
+}  // namespace heomgb

@@ -1,0 +1,308 @@
+"""Python mirror of libheom's model / solver interface over the C ABI.
+
+Same class names, public members and call order as the reference:
+
+    qme = heom_hilb(max_depth, n_inner_threads, n_outer_threads)   # heom_hilb.h:41-43
+    qme.n_level = n; qme.n_level_2 = n*n; qme.H = H                 # qme_base.h:32-36
+    qme.alloc_noises(U)                                             # qme_base.h:47-60
+    qme.V[u] = ...; qme.len_gamma[u] = ...; qme.gamma[u] = ...      # qme_base.h:38-45
+    qme.phi_0[u], qme.sigma[u], qme.S[u], qme.A[u], qme.s_delta[u]
+    qme.set_param()                                                 # heom_hilb.h:57-68
+    solver = rk4()        # or lsrk4(), rkdp()
+    qs = qme_solver(qme, solver)                                    # qme_solver.h:26-35
+    qs.solve(rho, t_list, callback, {"dt": 0.005})                  # qme_solver.h:44-52
+
+The engine argument of the reference (a linalg_engine*) has no counterpart:
+the device path is the only path.  Errors raise HeomError (the reference
+throws std::out_of_range for a missing kwarg and exits on CUDA errors).
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Callable, Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import CALLBACK, Kwargs, check
+
+_FORMS = {"hilb": 0, "liou": 1, "ado": 2}
+_PRECISION = {"fp64": 0, "mixed": 1}
+
+
+def _c128(a, shape=None) -> np.ndarray:
+    arr = np.ascontiguousarray(np.asarray(a, dtype=np.complex128))
+    if shape is not None:
+        arr = arr.reshape(shape)
+    return arr
+
+
+class heom:
+    """Common base of heom_hilb / heom_liou / heom_ado (heom.h:21-139)."""
+
+    form = "hilb"
+
+    def __init__(self, max_depth: int, n_inner_threads: int = 1, n_outer_threads: int = 1):
+        if int(max_depth) < 0:
+            raise ValueError("max_depth must be >= 0")
+        self.max_depth = int(max_depth)
+        self.n_inner_threads = n_inner_threads
+        self.n_outer_threads = n_outer_threads
+        self.n_level = 0
+        self.n_level_2 = 0
+        self.H = None
+        self.n_noise = 0
+        self.V, self.len_gamma, self.gamma, self.phi_0, self.sigma = [], [], [], [], []
+        self.S, self.A, self.s_delta = [], [], []
+        self.precision = "fp64"
+        self.stream = None  # optional cudaStream_t handle (int)
+        self._h = ctypes.c_void_p()
+        self._lib = _lib.load()
+
+    # -- qme_base ------------------------------------------------------------
+    def alloc_noises(self, n_noise: int) -> None:
+        n_noise = int(n_noise)
+        if n_noise < 0:
+            raise ValueError("n_noise must be >= 0")
+        self.n_noise = n_noise
+        self.V = [None] * n_noise
+        self.len_gamma = [0] * n_noise
+        self.gamma = [None] * n_noise
+        self.phi_0 = [None] * n_noise
+        self.sigma = [None] * n_noise
+        self.S = [None] * n_noise
+        self.A = [None] * n_noise
+        self.s_delta = [0j] * n_noise
+
+    def set_param(self, engine=None) -> None:
+        lib = self._lib
+        self.close()
+        n = int(self.n_level)
+        if n <= 0 or self.H is None:
+            raise ValueError("set n_level and H before set_param")
+        if self.n_level_2 and int(self.n_level_2) != n * n:
+            raise ValueError("n_level_2 must equal n_level**2")
+        h = ctypes.c_void_p()
+        check(lib.heomgb_qme_create(_FORMS[self.form], self.max_depth, int(self.n_inner_threads),
+                                    int(self.n_outer_threads), ctypes.byref(h)))
+        self._h = h
+        H = _c128(self.H, (n, n))
+        check(lib.heomgb_qme_set_hamiltonian(h, n, H.ctypes.data))
+        check(lib.heomgb_qme_alloc_noises(h, self.n_noise))
+        for u in range(self.n_noise):
+            L = int(self.len_gamma[u])
+            V = _c128(self.V[u], (n, n))
+            g = _c128(self.gamma[u], (L, L))
+            p = _c128(self.phi_0[u], (L,))
+            s = _c128(self.sigma[u], (L,))
+            Sm = _c128(self.S[u], (L, L))
+            Am = _c128(self.A[u], (L, L))
+            sd = _c128([self.s_delta[u]])
+            check(lib.heomgb_qme_set_noise(h, u, V.ctypes.data, L, g.ctypes.data, p.ctypes.data, s.ctypes.data,
+                                           Sm.ctypes.data, Am.ctypes.data, sd.ctypes.data))
+        check(lib.heomgb_qme_set_precision(h, _PRECISION[self.precision]))
+        if self.stream:
+            check(lib.heomgb_qme_set_stream(h, ctypes.c_void_p(int(self.stream))))
+        check(lib.heomgb_qme_set_param(h))
+
+    def _need(self):
+        if not self._h:
+            raise RuntimeError("set_param has not been called")
+
+    def get_n_hrchy(self) -> int:
+        self._need()
+        v = ctypes.c_int()
+        check(self._lib.heomgb_qme_get_n_hrchy(self._h, ctypes.byref(v)))
+        return v.value
+
+    def get_n_dim(self) -> int:
+        self._need()
+        v = ctypes.c_int()
+        check(self._lib.heomgb_qme_get_n_dim(self._h, ctypes.byref(v)))
+        return v.value
+
+    def main_size(self) -> int:
+        self._need()
+        v = ctypes.c_longlong()
+        check(self._lib.heomgb_qme_main_size(self._h, ctypes.byref(v)))
+        return v.value
+
+    def hrchy(self):
+        """(n, ptr_p1, ptr_m1) tables of hs (hrchy_space.h:18-27), from the device."""
+        nh, K = self.get_n_hrchy(), self.get_n_dim()
+        n = np.zeros((nh, K), dtype=np.int32)
+        p1 = np.zeros((nh + 1, K), dtype=np.int32)
+        m1 = np.zeros((nh + 1, K), dtype=np.int32)
+        check(self._lib.heomgb_qme_get_hrchy(self._h, n.ctypes.data, p1.ctypes.data, m1.ctypes.data))
+        return n, p1, m1
+
+    def calc_diff_impl(self, drho_dt: np.ndarray, rho: np.ndarray, alpha=1.0, beta=0.0) -> None:
+        """drho_dt = beta*drho_dt - alpha*D(rho), in place (heom_hilb.h:70-215)."""
+        self._need()
+        if not (isinstance(drho_dt, np.ndarray) and drho_dt.dtype == np.complex128 and drho_dt.flags.c_contiguous):
+            raise TypeError("drho_dt must be a C-contiguous complex128 array")
+        rho = _c128(rho)
+        if rho.size != self.main_size() or drho_dt.size != self.main_size():
+            raise ValueError("rho / drho_dt must hold main_size() elements")
+        a = np.array([complex(alpha).real, complex(alpha).imag])
+        b = np.array([complex(beta).real, complex(beta).imag])
+        check(self._lib.heomgb_qme_calc_diff(self._h, drho_dt.ctypes.data, rho.ctypes.data, a.ctypes.data,
+                                             b.ctypes.data))
+
+    def calc_diff(self, rho, alpha=1.0, beta=0.0, drho=None) -> np.ndarray:
+        out = np.zeros(np.shape(rho), dtype=np.complex128) if drho is None else np.array(drho, np.complex128)
+        self.calc_diff_impl(out, rho, alpha, beta)
+        return out
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.heomgb_qme_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class heom_hilb(heom):
+    """Hilbert-space HEOM (heom_hilb.h:18-216)."""
+    form = "hilb"
+
+
+class heom_liou(heom):
+    """Liouville-space HEOM with per-ADO superoperators (heom_liou.h:18-259)."""
+    form = "liou"
+
+
+class heom_ado(heom):
+    """ADO-space HEOM: one global block-sparse generator (heom_ado.h:18-204)."""
+    form = "ado"
+
+
+class solver_base:
+    kind = -1
+
+    def __init__(self):
+        self._h = ctypes.c_void_p()
+        lib = _lib.load()
+        check(lib.heomgb_solver_create(self.kind, ctypes.byref(self._h)))
+        self._lib = lib
+
+    def __del__(self):
+        try:
+            if self._h:
+                self._lib.heomgb_solver_destroy(self._h)
+        except Exception:
+            pass
+
+
+class rk4(solver_base):
+    """Classic RK4 (solver/rk4.h:15-66)."""
+    kind = 0
+
+
+class lsrk4(solver_base):
+    """2N-storage RK4 (solver/lsrk4.h:15-48)."""
+    kind = 1
+
+
+class rkdp(solver_base):
+    """Dormand-Prince 5(4) with error control (solver/rkdp.h:15-180)."""
+    kind = 2
+
+
+def _kwargs(kw: Optional[dict]) -> Kwargs:
+    k = Kwargs()
+    kw = kw or {}
+    for key in ("dt", "atol", "rtol"):
+        if key in kw:
+            v = kw[key]
+            if not isinstance(v, (float, int, np.floating, np.integer)) or isinstance(v, bool):
+                raise TypeError(f"kwarg {key!r} must be a real number")
+            setattr(k, key, float(v))
+            setattr(k, "has_" + key, 1)
+    return k
+
+
+class qme_solver:
+    """Facade wiring a model and an integrator (qme_solver.h:18-53)."""
+
+    def __init__(self, qme: heom, solver: solver_base, engine=None):
+        qme._need()
+        self.qme, self.solver = qme, solver
+        self._lib = qme._lib
+        self._h = ctypes.c_void_p()
+        check(self._lib.heomgb_qme_solver_create(qme._h, solver._h, ctypes.byref(self._h)))
+
+    def solve(self, rho: np.ndarray, t_list, callback: Optional[Callable[[float], None]] = None,
+              kwargs: Optional[dict] = None) -> None:
+        """Propagate the host array rho in place through t_list (qme_solver.h:44-52)."""
+        if not (isinstance(rho, np.ndarray) and rho.dtype == np.complex128 and rho.flags.c_contiguous):
+            raise TypeError("rho must be a C-contiguous complex128 array")
+        if rho.size != self.qme.main_size():
+            raise ValueError("rho must hold main_size() elements")
+        t = np.ascontiguousarray(t_list, dtype=np.float64)
+        cb = CALLBACK(lambda tt, _u: callback(tt)) if callback else CALLBACK()
+        kw = _kwargs(kwargs)
+        check(self._lib.heomgb_qme_solver_solve(self._h, rho.ctypes.data, t.ctypes.data, len(t), cb, None,
+                                                ctypes.byref(kw)))
+
+    def solve_device(self, rho_ptr: int, t_list, callback=None, kwargs: Optional[dict] = None) -> None:
+        """Same as solve with rho a device pointer (double2 array of main_size())."""
+        t = np.ascontiguousarray(t_list, dtype=np.float64)
+        cb = CALLBACK(lambda tt, _u: callback(tt)) if callback else CALLBACK()
+        kw = _kwargs(kwargs)
+        check(self._lib.heomgb_qme_solver_solve_device(self._h, ctypes.c_void_p(int(rho_ptr)), t.ctypes.data,
+                                                       len(t), cb, None, ctypes.byref(kw)))
+
+    def stats(self) -> dict:
+        r, a, c = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        d = ctypes.c_double()
+        check(self._lib.heomgb_qme_solver_stats(self._h, ctypes.byref(r), ctypes.byref(a), ctypes.byref(c),
+                                                ctypes.byref(d)))
+        return dict(rhs=r.value, attempts=a.value, accepted=c.value, dt_save=d.value)
+
+    def timing(self) -> dict:
+        """Device time of the last solve inside stage-kernel graph replays."""
+        ms, k = ctypes.c_double(), ctypes.c_longlong()
+        check(self._lib.heomgb_qme_solver_timing(self._h, ctypes.byref(ms), ctypes.byref(k)))
+        return dict(busy_ms=ms.value, kernels=k.value)
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.heomgb_qme_solver_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def from_params(p, form: str = "hilb", precision: str = "fp64", stream=None) -> heom:
+    """Build and set up a model from a HeomParams."""
+    cls = {"hilb": heom_hilb, "liou": heom_liou, "ado": heom_ado}[form]
+    q = cls(p.max_depth, 1, 1)
+    q.n_level = p.n_level
+    q.n_level_2 = p.n_level ** 2
+    q.H = p.H
+    q.alloc_noises(p.n_noise)
+    for u in range(p.n_noise):
+        q.V[u] = p.V[u]
+        q.len_gamma[u] = p.len_gamma[u]
+        q.gamma[u] = p.gamma[u]
+        q.phi_0[u] = p.phi_0[u]
+        q.sigma[u] = p.sigma[u]
+        q.S[u] = p.S[u]
+        q.A[u] = p.A[u]
+        q.s_delta[u] = p.s_delta[u]
+    q.precision = precision
+    q.stream = stream
+    q.set_param()
+    return q
+
+
+SOLVERS = {"rk4": rk4, "lsrk4": lsrk4, "rkdp": rkdp}

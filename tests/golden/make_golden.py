@@ -1,0 +1,98 @@
+"""Generate the golden fixtures of tests/golden/ from the reference's own code.
+
+Runs the reference's unmodified hierarchy / model / integrator sources, built
+by `make -C oracle ref` from the reference tree with the plain-loop harness
+engine, on small seeded cases and stores inputs and outputs as .npz files.
+Needs the reference tree, so it runs where that tree exists; the fixtures it
+writes are committed and are all the tests need elsewhere.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from libheom_gb300 import configs  # noqa: E402
+from libheom_gb300.params import HeomParams  # noqa: E402
+
+sys.path.insert(0, os.path.dirname(HERE))
+from _cases import generic_case, projector_case, params_to_dict  # noqa: E402
+
+
+def hrchy_fixture(ref: oracle.Oracle):
+    out = {}
+    for K, N in [(3, 10), (14, 4), (5, 3), (4, 6), (1, 5), (2, 0), (6, 5), (7, 2)]:
+        n, p1, m1 = ref.hrchy(K, N)
+        out[f"n_{K}_{N}"] = n
+        out[f"p1_{K}_{N}"] = p1
+        out[f"m1_{K}_{N}"] = m1
+    for K, N in [(48, 3), (14, 6)]:
+        n, p1, m1 = ref.hrchy(K, N)
+        h = hashlib.sha256()
+        for a in (n, p1, m1):
+            h.update(np.ascontiguousarray(a, dtype="<i4").tobytes())
+        out[f"sha_{K}_{N}"] = np.frombuffer(h.digest(), dtype=np.uint8)
+        out[f"count_{K}_{N}"] = np.array(n.shape[0])
+    np.savez_compressed(os.path.join(HERE, "hrchy.npz"), **out)
+
+
+def diff_fixture(ref, name, p: HeomParams, seed):
+    rng = np.random.default_rng(seed)
+    shape = (p.n_hrchy(), p.n_level, p.n_level)
+    rho = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    drho = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    alpha, beta = 0.7 - 0.2j, 0.3 + 0.1j
+    out = dict(params_to_dict(p), rho=rho, drho=drho, alpha=np.array(alpha), beta=np.array(beta))
+    for form in ("hilb", "liou", "ado"):
+        out[f"out_{form}"] = ref.calc_diff(p, rho, drho, alpha, beta, form=form, threads=4)
+        out[f"out0_{form}"] = ref.calc_diff(p, rho, None, 1.0, 0.0, form=form, threads=4)
+    np.savez_compressed(os.path.join(HERE, f"diff_{name}.npz"), **out)
+
+
+def solve_fixture(ref, name, p: HeomParams, solver, t_list, dt, atol=1e-8, rtol=1e-8, forms=("hilb",), rho0=None):
+    rho0 = p.rho0_ground() if rho0 is None else rho0
+    out = dict(params_to_dict(p), rho0=rho0, t_list=np.asarray(t_list, float), dt=np.array(dt),
+               atol=np.array(atol), rtol=np.array(rtol), solver=np.array(solver))
+    for form in forms:
+        out[f"rho_t_{form}"] = ref.solve(p, rho0, t_list, solver=solver, dt=dt, atol=atol, rtol=rtol, form=form,
+                                         threads=4)
+    np.savez_compressed(os.path.join(HERE, f"solve_{name}.npz"), **out)
+
+
+def main():
+    oracle.build("ref")
+    ref = oracle.Oracle("ref")
+    hrchy_fixture(ref)
+    diff_fixture(ref, "generic", generic_case(), 11)
+    diff_fixture(ref, "projector", projector_case(), 12)
+    diff_fixture(ref, "spin_boson", configs.spin_boson(depth=4), 13)
+    sb = configs.spin_boson()
+    solve_fixture(ref, "spin_boson_rk4", sb, "rk4", [0.0, 0.25, 0.5], 0.005, forms=("hilb", "liou", "ado"))
+    solve_fixture(ref, "spin_boson_lsrk4", sb, "lsrk4", [0.0, 0.25, 0.5], 0.005)
+    solve_fixture(ref, "spin_boson_rkdp", sb, "rkdp", [0.0, 0.5, 1.0], 0.01, atol=1e-8, rtol=1e-6)
+    sbx = configs.spin_boson(eps=0.5, coupling="x", depth=6)
+    solve_fixture(ref, "spin_boson_x_rk4", sbx, "rk4", [0.0, 0.2, 0.4], 0.01, forms=("hilb", "liou"))
+    ex = configs.exciton_7site(depth=2)
+    solve_fixture(ref, "exciton7_rkdp", ex, "rkdp", [0.0, 10.0, 20.0], 0.1, atol=1e-8, rtol=1e-8)
+    g = generic_case()
+    rng = np.random.default_rng(21)
+    r0 = np.zeros((g.n_hrchy(), g.n_level, g.n_level), complex)
+    v = rng.standard_normal(g.n_level) + 1j * rng.standard_normal(g.n_level)
+    r0[0] = np.outer(v, v.conj()) / np.vdot(v, v).real
+    solve_fixture(ref, "generic_rk4", g, "rk4", [0.0, 0.1, 0.2], 0.01, forms=("hilb", "liou", "ado"), rho0=r0)
+    solve_fixture(ref, "generic_rkdp", g, "rkdp", [0.0, 0.2, 0.4], 0.02, atol=1e-9, rtol=1e-7, rho0=r0)
+    solve_fixture(ref, "generic_lsrk4", g, "lsrk4", [0.0, 0.1, 0.2], 0.01, rho0=r0)
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

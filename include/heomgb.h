@@ -77,6 +77,7 @@ long long heomgb_launch_count(void);
  * are accepted for interface parity; the device path does not use them. */
 heomgb_status heomgb_qme_create(heomgb_form form, int max_depth, int n_inner_threads, int n_outer_threads,
                                 heomgb_qme** out);
+/* Fails with HEOMGB_ERR_STATE while qme_solvers created from q still exist. */
 heomgb_status heomgb_qme_destroy(heomgb_qme* q);
 
 /* Public members n_level / n_level_2 / H (qme_base.h:32-36).  H: n*n complex. */
@@ -96,7 +97,9 @@ heomgb_status heomgb_qme_set_precision(heomgb_qme* q, heomgb_precision p);
 heomgb_status heomgb_qme_set_stream(heomgb_qme* q, void* cuda_stream);
 /* set_param(engine) -- heom_hilb.h:57-68 / heom.h:57-139 / heom_liou.h:66-119 /
  * heom_ado.h:62-189.  Builds the hierarchy tables on the device, uploads H/V and
- * the per-ADO damping, and builds the superoperators of the Liouville forms. */
+ * the per-ADO damping, and builds the superoperators of the Liouville forms.
+ * Fails with HEOMGB_ERR_STATE while qme_solvers created from q still exist
+ * (their captured launches hold the model's device pointers). */
 heomgb_status heomgb_qme_set_param(heomgb_qme* q);
 /* get_n_hrchy() -- heom.h:52-55. */
 heomgb_status heomgb_qme_get_n_hrchy(const heomgb_qme* q, int* n_hrchy);

@@ -224,6 +224,7 @@ struct heomgb_qme {
   cudaStream_t user_stream = nullptr;
   bool user_stream_set = false;
   bool ready = false;
+  int live_solvers = 0;      // qme_solvers holding device pointers of this model
   // derived
   int K = 0, n_hrchy = 0, path = PATH_DIAG;
   RhsModel dm{};
@@ -287,6 +288,7 @@ void build_model(heomgb_qme* q) {
   if (q->U < 0) throw state_error("set_param: alloc_noises not called");
   for (int u = 0; u < q->U; ++u)
     if (!q->baths[u].set) throw state_error("set_param: noise " + std::to_string(u) + " not set");
+  if (q->live_solvers > 0) throw state_error("set_param: destroy the qme_solvers of this model first");
   ck(cudaSetDevice(q->device), "cudaSetDevice");
   q->arena.release();
   q->ready = false;
@@ -719,7 +721,7 @@ int solve_adaptive(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwa
   ck(launch_ctl_init(qs->ctl, t0, dt, t1, atol, rtol, cur, qs->stream), "ctl init");
   long long launched = 0;
   bool big = false;
-  const long long cap = 100000000LL;
+  const long long cap = 2000000LL;
   while (true) {
     busy_begin(qs);
     replay(qs, big);
@@ -804,6 +806,7 @@ heomgb_status heomgb_qme_create(heomgb_form form, int max_depth, int n_inner_thr
 
 heomgb_status heomgb_qme_destroy(heomgb_qme* q) {
   if (!q) return HEOMGB_OK;
+  if (q->live_solvers > 0) return fail(HEOMGB_ERR_STATE, "destroy the qme_solvers of this model first");
   cudaSetDevice(q->device);
   if (q->own_stream) cudaStreamSynchronize(q->own_stream);
   if (q->user_stream_set) cudaStreamSynchronize(q->user_stream);
@@ -992,6 +995,7 @@ heomgb_status heomgb_qme_solver_create(heomgb_qme* q, heomgb_solver* s, heomgb_q
     qs->stream = q->stream();
     alloc_solver(qs.get());
     ck(cudaStreamSynchronize(qs->stream), "solver init sync");
+    q->live_solvers += 1;
     *out = qs.release();
   });
 }
@@ -1000,6 +1004,7 @@ heomgb_status heomgb_qme_solver_destroy(heomgb_qme_solver* qs) {
   if (!qs) return HEOMGB_OK;
   cudaSetDevice(qs->q->device);
   cudaStreamSynchronize(qs->stream);
+  qs->q->live_solvers -= 1;
   delete qs;
   return HEOMGB_OK;
 }

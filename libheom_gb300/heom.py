@@ -19,6 +19,7 @@ throws std::out_of_range for a missing kwarg and exits on CUDA errors).
 from __future__ import annotations
 
 import ctypes
+import weakref
 from typing import Callable, Optional
 
 import numpy as np
@@ -58,6 +59,7 @@ class heom:
         self.stream = None  # optional cudaStream_t handle (int)
         self._h = ctypes.c_void_p()
         self._lib = _lib.load()
+        self._solvers = weakref.WeakSet()
 
     # -- qme_base ------------------------------------------------------------
     def alloc_noises(self, n_noise: int) -> None:
@@ -155,8 +157,10 @@ class heom:
         return out
 
     def close(self) -> None:
+        for s in list(self._solvers):
+            s.close()
         if self._h:
-            self._lib.heomgb_qme_destroy(self._h)
+            check(self._lib.heomgb_qme_destroy(self._h))
             self._h = ctypes.c_void_p()
 
     def __del__(self):
@@ -235,10 +239,16 @@ class qme_solver:
         self._lib = qme._lib
         self._h = ctypes.c_void_p()
         check(self._lib.heomgb_qme_solver_create(qme._h, solver._h, ctypes.byref(self._h)))
+        qme._solvers.add(self)
+
+    def _need(self):
+        if not self._h:
+            raise RuntimeError("this qme_solver was closed (its model was set up again or closed)")
 
     def solve(self, rho: np.ndarray, t_list, callback: Optional[Callable[[float], None]] = None,
               kwargs: Optional[dict] = None) -> None:
         """Propagate the host array rho in place through t_list (qme_solver.h:44-52)."""
+        self._need()
         if not (isinstance(rho, np.ndarray) and rho.dtype == np.complex128 and rho.flags.c_contiguous):
             raise TypeError("rho must be a C-contiguous complex128 array")
         if rho.size != self.qme.main_size():
@@ -251,6 +261,7 @@ class qme_solver:
 
     def solve_device(self, rho_ptr: int, t_list, callback=None, kwargs: Optional[dict] = None) -> None:
         """Same as solve with rho a device pointer (double2 array of main_size())."""
+        self._need()
         t = np.ascontiguousarray(t_list, dtype=np.float64)
         cb = CALLBACK(lambda tt, _u: callback(tt)) if callback else CALLBACK()
         kw = _kwargs(kwargs)

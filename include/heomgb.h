@@ -153,6 +153,10 @@ heomgb_status heomgb_qme_solver_stats(const heomgb_qme_solver* qs, long long* n_
  * replays launched.  busy_ms / kernels is the average stage-kernel duration. */
 heomgb_status heomgb_qme_solver_timing(const heomgb_qme_solver* qs, double* busy_ms, long long* kernels);
 
+/* Diagnostic without a reference counterpart: FP64 and FP32 FMA throughput of
+ * the current GPU in TFLOP/s, from register-only FMA chains (a few ms). */
+heomgb_status heomgb_probe_fma_peaks(double* fp64_tflops, double* fp32_tflops);
+
 /* ---- building blocks ------------------------------------------------------ */
 /* errnrm1(e, x_1, x_2, atol, rtol) -- linalg_engine_cuda.cu:176-201 and
  * linalg_engine_eigen.h.j2:360-379: sqrt(mean_i (|e_i|/(atol+rtol*max(|x1_i|,|x2_i|)))^2)

@@ -68,6 +68,7 @@ SIGNATURES = {
                                                       ctypes.POINTER(Kwargs)]),
     "heomgb_qme_solver_stats": (ctypes.c_int, [ctypes.c_void_p, c_ll_p, c_ll_p, c_ll_p, c_double_p]),
     "heomgb_qme_solver_timing": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_ll_p]),
+    "heomgb_probe_fma_peaks": (ctypes.c_int, [c_double_p, c_double_p]),
     "heomgb_errnrm1_scratch": (ctypes.c_size_t, [ctypes.c_longlong]),
     "heomgb_errnrm1_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
                                              ctypes.c_double, ctypes.c_longlong, ctypes.c_void_p, c_double_p,
@@ -108,3 +109,10 @@ def check(status: int) -> None:
 
 def launch_count() -> int:
     return int(load().heomgb_launch_count())
+
+
+def probe_fma_peaks():
+    """(FP64, FP32) FMA throughput of the current GPU in TFLOP/s."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    check(load().heomgb_probe_fma_peaks(ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value

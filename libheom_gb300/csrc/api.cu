@@ -396,6 +396,11 @@ void build_model(heomgb_qme* q) {
     q->path = PATH_LIOU;
   }
   if (q->path == PATH_DIAG) {
+    // tile of ADOs per CTA: about four elements per thread, within 200 KB of shared memory
+    m.tile = rhs_tile(m, rhs_block_size(m, PATH_DIAG));
+    while (m.tile > 1 && rhs_smem_bytes(m, PATH_DIAG, false) > 200 * 1024) m.tile /= 2;
+    if (rhs_smem_bytes(m, PATH_DIAG, false) > 200 * 1024)
+      throw unsupported_error("diagonal-coupling path: one ADO tile exceeds shared memory");
     // per-element active modes of the elementwise bath terms
     std::vector<int> pp(n2 + 1, 0), pm(n2 + 1, 0), pmode, mmode;
     std::vector<cd> cp, cmn, csd(n2, cd(0.0, 0.0));
@@ -1027,6 +1032,20 @@ heomgb_status heomgb_qme_solver_stats(const heomgb_qme_solver* qs, long long* n_
     if (n_attempts) *n_attempts = qs->n_attempts;
     if (n_accepted) *n_accepted = qs->n_accepted;
     if (dt_save) *dt_save = qs->dt_save;
+  });
+}
+
+heomgb_status heomgb_probe_fma_peaks(double* fp64_tflops, double* fp32_tflops) {
+  return guard([&] {
+    require(fp64_tflops && fp32_tflops, "null out");
+    int dev = 0, n_sm = 0;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    ck(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+    cudaStream_t s = nullptr;
+    ck(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream create");
+    const cudaError_t e = probe_fma_peaks(n_sm, fp64_tflops, fp32_tflops, s);
+    cudaStreamDestroy(s);
+    ck(e, "fma probe");
   });
 }
 

@@ -35,6 +35,7 @@ struct DpCtl {
 struct RhsModel {
   int n, n2, K, U, n_hrchy;
   int h_real;                       // H has zero imaginary part
+  int tile;                         // ADOs per CTA tile (diagonal-coupling kernel)
   const int* p1;                    // (n_hrchy+1)*K, sentinel n_hrchy
   const int* m1;                    // (n_hrchy+1)*K
   const int* nidx;                  // n_hrchy*K
@@ -112,6 +113,7 @@ enum Path : int { PATH_DIAG = 0, PATH_GENERAL = 1, PATH_LIOU = 2 };
 cudaError_t launch_rhs(const RhsModel& m, const Stage& st, int path, bool mixed, bool in_double, int grid,
                        int block, cudaStream_t s);
 int rhs_block_size(const RhsModel& m, int path);
+int rhs_tile(const RhsModel& m, int block);
 int rhs_grid_size(const RhsModel& m, int path, int block, int n_sm);
 size_t rhs_smem_bytes(const RhsModel& m, int path, bool mixed);
 
@@ -127,6 +129,7 @@ cudaError_t launch_errnrm1(const double2* e, const double2* x1, const double2* x
                            long long n, double* partials, double* out, unsigned int* counter, int grid,
                            cudaStream_t s);
 int errnrm1_grid(long long n);
+cudaError_t probe_fma_peaks(int n_sm, double* fp64_tflops, double* fp32_tflops, cudaStream_t s);
 
 extern long long g_launches;  // kernels launched (incremented by the launchers / graph replays)
 

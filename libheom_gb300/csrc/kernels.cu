@@ -121,8 +121,16 @@ __device__ void dp_control(DpCtl* c, double sumsq, long long n) {
 // D is the operator value of heom_hilb.h:96-353 at element g; every solver
 // stage uses k = -dt*D (calc_diff_impl with alpha = dt, beta = 0).  Returns
 // the element's squared scaled error for EPI_DP7, else 0.
+//
+// FP64 form (TC = double): the reference's operation order (rk4.h:40-65,
+// lsrk4.h:32-47, rkdp.h:111-153).  Mixed form (TC = float): stage inputs of
+// the next right-hand side are formed in FP32 from the bulk copy of the
+// state; the state, the RK4 accumulator, the LSRK4 buffer, the candidate
+// state rho + sum_j B_j k_j and the error vector e = sum_j E_j k_j are FP64.
 template <typename TC>
-__device__ __forceinline__ double epilogue(const Stage& st, size_t g, double2 D, double dt, int cur) {
+__device__ __forceinline__ double epilogue(const Stage& st, size_t g, cx_t<TC> Dc, double dt, int cur) {
+  constexpr bool MIX = std::is_same<TC, float>::value;
+  const double2 D = to_d(Dc);
   switch (st.kind) {
     case EPI_DIFF: {
       double2 o = st.beta_zero ? make_double2(0.0, 0.0) : cmul(st.beta, st.out[g]);
@@ -130,27 +138,41 @@ __device__ __forceinline__ double epilogue(const Stage& st, size_t g, double2 D,
       st.out[g] = make_double2(o.x - ad.x, o.y - ad.y);
       return 0.0;
     }
-    case EPI_RK4_1: {  // rho_n = rho + k1/2 ; acc = rho + k1/6
-      const double2 k = make_double2(-dt * D.x, -dt * D.y);
-      const double2 s = st.S[0][g];
-      st_bulk<TC>(st.Ynext, g, make_double2(s.x + 0.5 * k.x, s.y + 0.5 * k.y));
-      st.acc[g] = make_double2(s.x + (1.0 / 6.0) * k.x, s.y + (1.0 / 6.0) * k.y);
-      return 0.0;
-    }
+    case EPI_RK4_1:
     case EPI_RK4_2:
-    case EPI_RK4_3: {  // rho_n = rho + c*k ; acc += k/3   (2/6 applied to k2+k3)
-      const double2 k = make_double2(-dt * D.x, -dt * D.y);
-      const double2 s = st.S[0][g];
-      const double c = st.kind == EPI_RK4_2 ? 0.5 : 1.0;
-      st_bulk<TC>(st.Ynext, g, make_double2(s.x + c * k.x, s.y + c * k.y));
-      double2 a = st.acc[g];
-      st.acc[g] = make_double2(a.x + (2.0 / 6.0) * k.x, a.y + (2.0 / 6.0) * k.y);
+    case EPI_RK4_3: {  // rho_n = rho + c*k ; acc = rho + k/6 or acc += k/3 (2/6 on k2+k3)
+      const double c = st.kind == EPI_RK4_3 ? 1.0 : 0.5;
+      const double w = st.kind == EPI_RK4_1 ? (1.0 / 6.0) : (2.0 / 6.0);
+      double2 a = st.kind == EPI_RK4_1 ? st.S[0][g] : st.acc[g];
+      if constexpr (MIX) {
+        const float fdt = static_cast<float>(dt);
+        const float2 k = make_float2(-fdt * Dc.x, -fdt * Dc.y);
+        const float2 s = static_cast<const float2*>(st.Yb[0])[g];
+        static_cast<float2*>(st.Ynext)[g] = make_float2(s.x + static_cast<float>(c) * k.x,
+                                                        s.y + static_cast<float>(c) * k.y);
+        a.x += static_cast<double>(static_cast<float>(w) * k.x);
+        a.y += static_cast<double>(static_cast<float>(w) * k.y);
+      } else {
+        const double2 k = make_double2(-dt * D.x, -dt * D.y);
+        const double2 s = st.S[0][g];
+        st_bulk<TC>(st.Ynext, g, make_double2(s.x + c * k.x, s.y + c * k.y));
+        a.x += w * k.x;
+        a.y += w * k.y;
+      }
+      st.acc[g] = a;
       return 0.0;
     }
     case EPI_RK4_4: {  // rho = acc + k4/6
-      const double2 k = make_double2(-dt * D.x, -dt * D.y);
       const double2 a = st.acc[g];
-      const double2 v = make_double2(a.x + (1.0 / 6.0) * k.x, a.y + (1.0 / 6.0) * k.y);
+      double2 v;
+      if constexpr (MIX) {
+        const float fdt = static_cast<float>(dt);
+        v = make_double2(a.x + static_cast<double>((1.0f / 6.0f) * (-fdt * Dc.x)),
+                         a.y + static_cast<double>((1.0f / 6.0f) * (-fdt * Dc.y)));
+      } else {
+        const double2 k = make_double2(-dt * D.x, -dt * D.y);
+        v = make_double2(a.x + (1.0 / 6.0) * k.x, a.y + (1.0 / 6.0) * k.y);
+      }
       st.S[0][g] = v;
       if (st.bulk_separate) st_bulk<TC>(st.Yb[0], g, v);
       return 0.0;
@@ -171,28 +193,63 @@ __device__ __forceinline__ double epilogue(const Stage& st, size_t g, double2 D,
     }
     case EPI_DP: {  // store k_s; next stage input rho + sum_j A[s+1][j] k_j
       const int s_ = st.dp_stage;
-      const double2 k = as_bulk<TC>(make_double2(-dt * D.x, -dt * D.y));
-      st_bulk<TC>(st.K[s_], g, k);
-      double2 y = st.S[cur][g];
-      for (int j = 0; j < s_; ++j) {
-        const double c = c_dpA[s_ + 1][j];
-        const double2 kj = ld_bulk<TC>(st.K[j], g);
-        y.x += c * kj.x;
-        y.y += c * kj.y;
-      }
-      const double c = c_dpA[s_ + 1][s_];
-      y.x += c * k.x;
-      y.y += c * k.y;
-      if (s_ < 5) {
-        st_bulk<TC>(st.Ynext, g, y);
-      } else {  // the candidate state rho + sum B_j k_j
-        st.S[1 - cur][g] = y;
-        if (st.bulk_separate) st_bulk<TC>(st.Yb[1 - cur], g, y);
+      if constexpr (MIX) {
+        const float fdt = static_cast<float>(dt);
+        const float2 k = make_float2(-fdt * Dc.x, -fdt * Dc.y);
+        static_cast<float2*>(st.K[s_])[g] = k;
+        if (s_ < 5) {
+          float2 y = static_cast<const float2*>(st.Yb[cur])[g];
+          for (int j = 0; j < s_; ++j) {
+            const float c = static_cast<float>(c_dpA[s_ + 1][j]);
+            const float2 kj = static_cast<const float2*>(st.K[j])[g];
+            y.x = fmaf(c, kj.x, y.x);
+            y.y = fmaf(c, kj.y, y.y);
+          }
+          const float c = static_cast<float>(c_dpA[s_ + 1][s_]);
+          y.x = fmaf(c, k.x, y.x);
+          y.y = fmaf(c, k.y, y.y);
+          static_cast<float2*>(st.Ynext)[g] = y;
+        } else {  // candidate state rho + sum_j B_j k_j in FP64
+          double2 y = st.S[cur][g];
+          for (int j = 0; j < 5; ++j) {
+            const double c = c_dpA[6][j];
+            const float2 kj = static_cast<const float2*>(st.K[j])[g];
+            y.x += c * static_cast<double>(kj.x);
+            y.y += c * static_cast<double>(kj.y);
+          }
+          y.x += c_dpA[6][5] * static_cast<double>(k.x);
+          y.y += c_dpA[6][5] * static_cast<double>(k.y);
+          st.S[1 - cur][g] = y;
+          static_cast<float2*>(st.Yb[1 - cur])[g] = make_float2(static_cast<float>(y.x), static_cast<float>(y.y));
+        }
+      } else {
+        const double2 k = make_double2(-dt * D.x, -dt * D.y);
+        st_bulk<TC>(st.K[s_], g, k);
+        double2 y = st.S[cur][g];
+        for (int j = 0; j < s_; ++j) {
+          const double c = c_dpA[s_ + 1][j];
+          const double2 kj = ld_bulk<TC>(st.K[j], g);
+          y.x += c * kj.x;
+          y.y += c * kj.y;
+        }
+        const double c = c_dpA[s_ + 1][s_];
+        y.x += c * k.x;
+        y.y += c * k.y;
+        if (s_ < 5)
+          st_bulk<TC>(st.Ynext, g, y);
+        else
+          st.S[1 - cur][g] = y;
       }
       return 0.0;
     }
     case EPI_DP7: {  // e = sum_j E_j k_j ; scaled squared error (linalg_engine_cuda.cu:102-146)
-      const double2 k7 = make_double2(-dt * D.x, -dt * D.y);
+      double2 k7;
+      if constexpr (MIX) {
+        const float fdt = static_cast<float>(dt);
+        k7 = make_double2(static_cast<double>(-fdt * Dc.x), static_cast<double>(-fdt * Dc.y));
+      } else {
+        k7 = make_double2(-dt * D.x, -dt * D.y);
+      }
       const double2 k0 = ld_bulk<TC>(st.K[0], g);
       double2 e = make_double2(c_dpE[0] * k0.x, c_dpE[0] * k0.y);
       for (int j = 1; j < 6; ++j) {
@@ -202,11 +259,20 @@ __device__ __forceinline__ double epilogue(const Stage& st, size_t g, double2 D,
       }
       e.x += c_dpE[6] * k7.x;
       e.y += c_dpE[6] * k7.y;
-      const double2 x1 = st.S[1 - cur][g];
-      const double2 x2 = st.S[cur][g];
-      const double m = fmax(hypot(x1.x, x1.y), hypot(x2.x, x2.y));
-      const double q = hypot(e.x, e.y) / (st.ctl->atol + st.ctl->rtol * m);
-      return q * q;
+      const double e2 = e.x * e.x + e.y * e.y;
+      if constexpr (MIX) {  // scale from the bulk copies of both states
+        const float2 x1 = static_cast<const float2*>(st.Yb[1 - cur])[g];
+        const float2 x2 = static_cast<const float2*>(st.Yb[cur])[g];
+        const float m = sqrtf(fmaxf(x1.x * x1.x + x1.y * x1.y, x2.x * x2.x + x2.y * x2.y));
+        const float s = static_cast<float>(st.ctl->atol) + static_cast<float>(st.ctl->rtol) * m;
+        return e2 * static_cast<double>(1.0f / (s * s));
+      } else {
+        const double2 x1 = st.S[1 - cur][g];
+        const double2 x2 = st.S[cur][g];
+        const double m = sqrt(fmax(x1.x * x1.x + x1.y * x1.y, x2.x * x2.x + x2.y * x2.y));
+        const double s = st.ctl->atol + st.ctl->rtol * m;
+        return e2 / (s * s);
+      }
     }
     default:
       return 0.0;
@@ -278,74 +344,103 @@ __device__ __forceinline__ bool stage_prologue(const Stage& st, double& dt, int&
 // For every bath u with diagonal V_u the coupling terms are elementwise:
 // [V,X]_ab = (v_a - v_b) X_ab and {V,X}_ab = (v_a + v_b) X_ab, so element e
 // only needs the neighbour ADOs of the modes whose bath couples e.
+//
+// A CTA owns a tile of `tile` consecutive ADOs (contiguous in HBM).  The
+// tile's RHS input, H and the tile's hierarchy rows (neighbour indices and
+// occupation numbers) are staged in shared memory with coalesced loads; the
+// commutator then reads shared memory only, and every bath term costs one
+// global load of the neighbour's element.
 template <typename TC, typename TB, bool HREAL>
 __global__ void __launch_bounds__(256) k_rhs_diag(const RhsModel m, const Stage st) {
   using C = cx_t<TC>;
+  const int tile = m.tile;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   double dt;
   int cur;
   if (!stage_prologue(st, dt, cur)) return;
   const TB* __restrict__ y = stage_input<TB>(st, cur);
-  const int n = m.n, n2 = m.n2, K = m.K, void_idx = m.n_hrchy;
-  const long long total = static_cast<long long>(m.n_hrchy) * n2;
-  const C* __restrict__ H = pick<TC>(m.H, m.H_f);
+  const int n = m.n, n2 = m.n2, K = m.K, nh = m.n_hrchy, void_idx = m.n_hrchy;
+  C* Hs = reinterpret_cast<C*>(smem_raw);        // n2
+  C* yt = Hs + n2;                                // tile*n2
+  int* p1s = reinterpret_cast<int*>(yt + static_cast<size_t>(tile) * n2);  // tile*K
+  int* m1s = p1s + tile * K;                      // tile*K
+  int* nks = m1s + tile * K;                      // tile*K
+  const C* __restrict__ Hg = pick<TC>(m.H, m.H_f);
   const C* __restrict__ ngd = pick<TC>(m.ngd, m.ngd_f);
   const C* __restrict__ cpl = pick<TC>(m.c_plus, m.c_plus_f);
   const C* __restrict__ cmi = pick<TC>(m.c_minus, m.c_minus_f);
   const C* __restrict__ csd = pick<TC>(m.c_sd, m.c_sd_f);
+  for (int i = threadIdx.x; i < n2; i += blockDim.x) Hs[i] = Hg[i];
+  const int n_tiles = (nh + tile - 1) / tile;
   double local = 0.0;
-  for (long long g = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; g < total;
-       g += static_cast<long long>(gridDim.x) * blockDim.x) {
-    const int l = static_cast<int>(g / n2);
-    const int e = static_cast<int>(g - static_cast<long long>(l) * n2);
-    const int a = e / n, b = e - a * n;
-    const TB* __restrict__ yl = y + static_cast<size_t>(l) * n2;
-    // i[H, rho]
-    C acc = cx<TC>(0, 0);
-    if (HREAL) {
-      for (int c = 0; c < n; ++c) {
-        const TC hac = H[a * n + c].x, hcb = H[c * n + b].x;
-        const C ycb = ldc<TC>(yl + c * n + b), yac = ldc<TC>(yl + a * n + c);
-        acc.x = fma(hac, ycb.x, acc.x);
-        acc.x = fma(-hcb, yac.x, acc.x);
-        acc.y = fma(hac, ycb.y, acc.y);
-        acc.y = fma(-hcb, yac.y, acc.y);
-      }
-    } else {
-      C neg = cx<TC>(0, 0);
-      for (int c = 0; c < n; ++c) {
-        cfma(acc, H[a * n + c], ldc<TC>(yl + c * n + b));
-        cfma(neg, ldc<TC>(yl + a * n + c), H[c * n + b]);
-      }
-      acc.x -= neg.x;
-      acc.y -= neg.y;
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const int l0 = t * tile;
+    const int nt = min(tile, nh - l0);
+    const int ne = nt * n2;
+    const TB* __restrict__ ysrc = y + static_cast<size_t>(l0) * n2;
+    for (int i = threadIdx.x; i < ne; i += blockDim.x) yt[i] = ldc<TC>(ysrc + i);
+    for (int i = threadIdx.x; i < nt * K; i += blockDim.x) {
+      const size_t gi = static_cast<size_t>(l0) * K + i;
+      p1s[i] = __ldg(m.p1 + gi);
+      m1s[i] = __ldg(m.m1 + gi);
+      nks[i] = __ldg(m.nidx + gi);
     }
-    C D = cx<TC>(-acc.y, acc.x);
-    // (sum_k n_k gamma_k + sum_u s_delta_u (v_a - v_b)^2) rho
-    const C ye = ldc<TC>(yl + e);
-    const C g0 = ngd[l], g1 = csd[e];
-    cfma(D, cx<TC>(g0.x + g1.x, g0.y + g1.y), ye);
-    // bath couplings of this element's modes
-    const int* __restrict__ p1row = m.p1 + static_cast<size_t>(l) * K;
-    const int* __restrict__ m1row = m.m1 + static_cast<size_t>(l) * K;
-    const int* __restrict__ nrow = m.nidx + static_cast<size_t>(l) * K;
-    const int pe = __ldg(m.plus_ptr + e + 1);
-    for (int p = __ldg(m.plus_ptr + e); p < pe; ++p) {
-      const int lp = __ldg(p1row + __ldg(m.plus_mode + p));
-      if (lp != void_idx) cfma(D, cpl[p], ldc<TC>(y + static_cast<size_t>(lp) * n2 + e));
-    }
-    const int me = __ldg(m.minus_ptr + e + 1);
-    for (int p = __ldg(m.minus_ptr + e); p < me; ++p) {
-      const int k = __ldg(m.minus_mode + p);
-      const int lm = __ldg(m1row + k);
-      if (lm != void_idx) {
-        const TC nk = static_cast<TC>(__ldg(nrow + k));
-        const C cm = cmi[p];
-        cfma(D, cx<TC>(nk * cm.x, nk * cm.y), ldc<TC>(y + static_cast<size_t>(lm) * n2 + e));
+    __syncthreads();
+    for (int i = threadIdx.x; i < ne; i += blockDim.x) {
+      const int lt = i / n2;
+      const int e = i - lt * n2;
+      const int a = e / n, b = e - a * n;
+      const C* yl = yt + lt * n2;
+      // i[H, rho]
+      C acc = cx<TC>(0, 0);
+      if (HREAL) {
+#pragma unroll 4
+        for (int c = 0; c < n; ++c) {
+          const TC hac = Hs[a * n + c].x, hcb = Hs[c * n + b].x;
+          const C ycb = yl[c * n + b], yac = yl[a * n + c];
+          acc.x = fma(hac, ycb.x, acc.x);
+          acc.x = fma(-hcb, yac.x, acc.x);
+          acc.y = fma(hac, ycb.y, acc.y);
+          acc.y = fma(-hcb, yac.y, acc.y);
+        }
+      } else {
+        C neg = cx<TC>(0, 0);
+#pragma unroll 4
+        for (int c = 0; c < n; ++c) {
+          cfma(acc, Hs[a * n + c], yl[c * n + b]);
+          cfma(neg, yl[a * n + c], Hs[c * n + b]);
+        }
+        acc.x -= neg.x;
+        acc.y -= neg.y;
       }
+      C D = cx<TC>(-acc.y, acc.x);
+      // (sum_k n_k gamma_k + sum_u s_delta_u (v_a - v_b)^2) rho
+      const C g0 = ngd[l0 + lt], g1 = csd[e];
+      cfma(D, cx<TC>(g0.x + g1.x, g0.y + g1.y), yl[e]);
+      // bath couplings of this element's modes
+      const int* p1row = p1s + lt * K;
+      const int* m1row = m1s + lt * K;
+      const int* nrow = nks + lt * K;
+      const int pb = __ldg(m.plus_ptr + e), pe = __ldg(m.plus_ptr + e + 1);
+      for (int p = pb; p < pe; ++p) {
+        const int lp = p1row[__ldg(m.plus_mode + p)];
+        if (lp != void_idx) cfma(D, cpl[p], ldc<TC>(y + static_cast<size_t>(lp) * n2 + e));
+      }
+      const int mb = __ldg(m.minus_ptr + e), me = __ldg(m.minus_ptr + e + 1);
+      for (int p = mb; p < me; ++p) {
+        const int k = __ldg(m.minus_mode + p);
+        const int lm = m1row[k];
+        if (lm != void_idx) {
+          const TC nk = static_cast<TC>(nrow[k]);
+          const C cm = cmi[p];
+          cfma(D, cx<TC>(nk * cm.x, nk * cm.y), ldc<TC>(y + static_cast<size_t>(lm) * n2 + e));
+        }
+      }
+      local += epilogue<TC>(st, static_cast<size_t>(l0) * n2 + i, D, dt, cur);
     }
-    local += epilogue<TC>(st, static_cast<size_t>(g), to_d(D), dt, cur);
+    __syncthreads();
   }
-  if (st.kind == EPI_DP7) dp7_finish(st, local, total);
+  if (st.kind == EPI_DP7) dp7_finish(st, local, static_cast<long long>(nh) * n2);
 }
 
 // ------------------------------------------------------------------ RHS, general V
@@ -454,7 +549,7 @@ __global__ void __launch_bounds__(256) k_rhs_general(const RhsModel m, const Sta
     }
     __syncthreads();
     for (int e = threadIdx.x; e < n2; e += blockDim.x)
-      local += epilogue<TC>(st, static_cast<size_t>(l) * n2 + e, to_d(Dm[e]), dt, cur);
+      local += epilogue<TC>(st, static_cast<size_t>(l) * n2 + e, Dm[e], dt, cur);
     __syncthreads();
   }
   if (st.kind == EPI_DP7) dp7_finish(st, local, static_cast<long long>(m.n_hrchy) * n2);
@@ -530,7 +625,7 @@ __global__ void __launch_bounds__(256) k_rhs_liou(const RhsModel m, const Stage 
       __syncthreads();
     }
     for (int e = threadIdx.x; e < n2; e += blockDim.x)
-      local += epilogue<TC>(st, static_cast<size_t>(l) * n2 + e, to_d(Dm[e]), dt, cur);
+      local += epilogue<TC>(st, static_cast<size_t>(l) * n2 + e, Dm[e], dt, cur);
     __syncthreads();
   }
   if (st.kind == EPI_DP7) dp7_finish(st, local, static_cast<long long>(m.n_hrchy) * n2);
@@ -543,39 +638,48 @@ int rhs_block_size(const RhsModel& m, int path) {
     while (b < m.n2 && b < 256) b <<= 1;
     return b;
   }
-  // spread small problems over many SMs: the FP64 pipe per SM is narrow
-  const long long total = static_cast<long long>(m.n_hrchy) * m.n2;
-  int b = 32;
-  while (b < 256 && total / (2 * b) >= 152 * 4) b <<= 1;
-  return b;
+  return 128;
 }
+
+// ADOs per tile of the diagonal-coupling kernel: about four elements per thread.
+int rhs_tile(const RhsModel& m, int block) { return std::max(1, (4 * block) / std::max(1, m.n2)); }
 
 int rhs_grid_size(const RhsModel& m, int path, int block, int n_sm) {
   if (path != PATH_DIAG) {
     const int per_sm = 4;
     return static_cast<int>(std::min<long long>(m.n_hrchy, static_cast<long long>(n_sm) * per_sm * 4));
   }
-  const long long total = static_cast<long long>(m.n_hrchy) * m.n2;
-  const long long want = (total + block - 1) / block;
+  const int tile = m.tile > 0 ? m.tile : rhs_tile(m, block);
+  const long long tiles = (static_cast<long long>(m.n_hrchy) + tile - 1) / tile;
   const long long cap = static_cast<long long>(n_sm) * (2048 / block);
-  return static_cast<int>(std::max<long long>(1, std::min(want, cap)));
+  return static_cast<int>(std::max<long long>(1, std::min(tiles, cap)));
 }
 
 size_t rhs_smem_bytes(const RhsModel& m, int path, bool mixed) {
   const size_t cb = mixed ? sizeof(float2) : sizeof(double2);
   if (path == PATH_GENERAL) return 5 * cb * m.n2;
   if (path == PATH_LIOU) return 4 * cb * m.n2;
-  return 0;
+  const size_t tile = m.tile > 0 ? m.tile : 1;
+  return cb * m.n2 * (1 + tile) + 3 * sizeof(int) * tile * m.K;
 }
 
 template <typename TC, typename TB>
 static cudaError_t launch_typed(const RhsModel& m, const Stage& st, int path, int grid, int block, cudaStream_t s) {
   const size_t smem = rhs_smem_bytes(m, path, std::is_same<TC, float>::value);
   if (path == PATH_DIAG) {
+    if (smem > 48 * 1024) {
+      cudaError_t e = m.h_real ? cudaFuncSetAttribute(k_rhs_diag<TC, TB, true>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      static_cast<int>(smem))
+                               : cudaFuncSetAttribute(k_rhs_diag<TC, TB, false>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      static_cast<int>(smem));
+      if (e != cudaSuccess) return e;
+    }
     if (m.h_real)
-      k_rhs_diag<TC, TB, true><<<grid, block, 0, s>>>(m, st);
+      k_rhs_diag<TC, TB, true><<<grid, block, smem, s>>>(m, st);
     else
-      k_rhs_diag<TC, TB, false><<<grid, block, 0, s>>>(m, st);
+      k_rhs_diag<TC, TB, false><<<grid, block, smem, s>>>(m, st);
   } else if (path == PATH_GENERAL) {
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(k_rhs_general<TC, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -716,6 +820,57 @@ cudaError_t launch_to_bulk(const double2* src, float2* dst, long long n, cudaStr
   k_to_bulk<<<grid, 256, 0, s>>>(src, dst, n);
   ++g_launches;
   return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ arithmetic peak probe
+// Register-only FMA chains (8 independent per thread, one store per thread):
+// the FP64 and FP32 FMA rates of this GPU, the denominators of the
+// compute-bound roofline of the plain FP64 form.
+template <typename T>
+__global__ void k_fma_chain(T* out, int iters, T a, T b) {
+  T x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b);
+    x1 = fma(x1, a, b);
+    x2 = fma(x2, a, b);
+    x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b);
+    x5 = fma(x5, a, b);
+    x6 = fma(x6, a, b);
+    x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+template <typename T>
+static cudaError_t time_fma(int n_sm, double* tflops, cudaStream_t s) {
+  const int grid = n_sm * 8, block = 256, iters = 2048, reps = 3;
+  T* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(T) * grid * block);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_fma_chain<T><<<grid, block, 0, s>>>(d, iters, static_cast<T>(0.999), static_cast<T>(0.001));
+  cudaEventRecord(e0, s);
+  for (int r = 0; r < reps; ++r)
+    k_fma_chain<T><<<grid, block, 0, s>>>(d, iters, static_cast<T>(0.999), static_cast<T>(0.001));
+  cudaEventRecord(e1, s);
+  e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  g_launches += reps + 1;
+  *tflops = static_cast<double>(reps) * grid * block * iters * 8.0 * 2.0 / (ms * 1e-3) / 1e12;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
+cudaError_t probe_fma_peaks(int n_sm, double* fp64_tflops, double* fp32_tflops, cudaStream_t s) {
+  cudaError_t e = time_fma<double>(n_sm, fp64_tflops, s);
+  if (e != cudaSuccess) return e;
+  return time_fma<float>(n_sm, fp32_tflops, s);
 }
 
 // ------------------------------------------------------------------ controller set-up

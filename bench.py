@@ -11,7 +11,8 @@ Default workload: the 7-site exciton aggregate (n=7, 14 modes, depth 4,
 Hamiltonian.  The chosen form is mixed precision (FP32 bulk products, FP64
 state / accumulation / error norm / step control); its final state is
 checked against the FP64 path (max |delta rho| <= 1e-6), and the FP64 plain
-form is timed beside it.
+form is timed beside it.  Other workloads: --workload spin_boson | batched |
+aggregate24.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -35,8 +36,10 @@ WORKLOADS = {
     "exciton7": dict(maker="exciton_7site", solver="rkdp", t_final=1000.0, kw=dict(dt=0.1, atol=1e-8, rtol=1e-8),
                      cpu_sample_t=1000.0),
     "spin_boson": dict(maker="spin_boson", solver="rk4", t_final=10.0, kw=dict(dt=0.005), cpu_sample_t=10.0),
+    "batched": dict(maker="batched_sweep", solver="rk4", t_final=20.0, kw=dict(dt=0.005), cpu_sample_t=1.0,
+                    cpu_sample_instances=24),
     "aggregate24": dict(maker="aggregate_24site", solver="lsrk4", t_final=1000.0, kw=dict(dt=0.5),
-                        cpu_sample_t=1.0),
+                        cpu_sample_t=0.5),
 }
 L2_FLUSH_BYTES = 512 << 20
 
@@ -136,44 +139,108 @@ def profile_traffic(workload, form):
     return d.get(f"{workload}/{form}")
 
 
-def cpu_baseline(wl, p, seconds_hint=True):
+class Workload:
+    """The instances of a workload (one model, or a batch) and their sizes."""
+
+    def __init__(self, name, rank=0):
+        from libheom_gb300 import configs
+        from libheom_gb300.dist import shard_seed
+        self.name = name
+        self.wl = WORKLOADS[name]
+        maker = getattr(configs, self.wl["maker"])
+        # a batched sweep gives every rank its own seeded shard (weak scaling);
+        # a single model is replicated
+        made = maker(seed=shard_seed(2, rank)) if self.wl["maker"] == "batched_sweep" else maker()
+        self.ps = made if isinstance(made, list) else [made]
+        self.batched = len(self.ps) > 1
+        self.n_hrchy = sum(p.n_hrchy() for p in self.ps)
+        self.N = sum(p.n_hrchy() * p.n_level ** 2 for p in self.ps)
+
+    def rho0(self):
+        return np.concatenate([p.rho0_ground().ravel() for p in self.ps])
+
+    def make(self, precision, stream):
+        import libheom_gb300 as lh
+        qmes = [lh.from_params(p, precision=precision, stream=stream) for p in self.ps]
+        solver = lh.SOLVERS[self.wl["solver"]]()
+        qs = lh.batch_solver(qmes, solver) if self.batched else lh.qme_solver(qmes[0], solver)
+        return qmes, qs
+
+    def errors(self, got, ref):
+        """Accuracy of `got` against the FP64 result `ref` (flat concatenated states).
+
+        rho0: max |delta rho_0| (system density matrix) over the instances whose
+        FP64 rho_0 stays bounded (|rho_0| <= 2; some seeded batch instances are
+        unstable under the reference's algorithm itself); all_ados: the same
+        over every ADO element of those instances."""
+        off = 0
+        e0, ea, stable = 0.0, 0.0, 0
+        for p in self.ps:
+            n2 = p.n_level ** 2
+            size = p.n_hrchy() * n2
+            r, g = ref[off:off + size], got[off:off + size]
+            off += size
+            if not np.all(np.isfinite(r)) or np.abs(r[:n2]).max() > 2.0:
+                continue
+            stable += 1
+            e0 = max(e0, float(np.abs(g[:n2] - r[:n2]).max()))
+            ea = max(ea, float(np.abs(g - r).max()))
+        return {"rho0": e0, "all_ados": ea, "instances_checked": stable, "instances": len(self.ps)}
+
+    def flops_per_launch(self):
+        from libheom_gb300 import roofline
+        return sum(roofline.flops_per_element(p) * p.n_hrchy() * p.n_level ** 2 for p in self.ps)
+
+    def describe(self):
+        if not self.batched:
+            p = self.ps[0]
+            return {"n_level": p.n_level, "n_modes": p.n_modes, "max_depth": p.max_depth, "n_hrchy": p.n_hrchy()}
+        counts = [p.n_hrchy() for p in self.ps]
+        return {"instances": len(self.ps), "n_level": sorted({p.n_level for p in self.ps}),
+                "max_depth": [min(p.max_depth for p in self.ps), max(p.max_depth for p in self.ps)],
+                "n_hrchy_total": self.n_hrchy, "n_hrchy_per_instance": [min(counts), max(counts)]}
+
+
+def cpu_baseline(w: Workload):
     """The CPU restatement of the reference path (oracle port) on a bounded sample."""
     import oracle
     cores = os.cpu_count() or 1
     orc = oracle.Oracle("port")
+    wl = w.wl
     t_s = wl["cpu_sample_t"]
+    ps = w.ps[:wl.get("cpu_sample_instances", 1)] if w.batched else w.ps
+    rhs_upd = 0
     t0 = time.perf_counter()
-    _, st = orc.solve(p, p.rho0_ground(), [0.0, t_s], solver=wl["solver"], threads=cores, with_stats=True,
-                      **wl["kw"])
+    for p in ps:
+        _, st = orc.solve(p, p.rho0_ground(), [0.0, t_s], solver=wl["solver"], threads=cores, with_stats=True,
+                          **wl["kw"])
+        rhs_upd += st["rhs"] * p.n_hrchy()
     el = time.perf_counter() - t0
-    rate = st["rhs"] * p.n_hrchy() / el
-    return {"value": rate, "unit": "ADO-updates/s", "cores": cores, "kind": "port", "seconds": el,
-            "sample": f"{wl['maker']} {wl['solver']} t=0..{t_s} ({st['rhs']} RHS x {p.n_hrchy()} ADOs, "
-                      f"{el:.2f} s)"}
+    return {"value": rhs_upd / el, "unit": "ADO-updates/s", "cores": cores, "kind": "port", "seconds": el,
+            "sample": f"{w.name}: {len(ps)} instance(s), {wl['solver']} t=0..{t_s}, {rhs_upd} ADO-updates, "
+                      f"{el:.2f} s"}
 
 
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from libheom_gb300 import configs
-    wl = WORKLOADS[args.workload]
-    p = getattr(configs, wl["maker"])()
+    w = Workload(args.workload)
     vals, secs = [], []
     cb = None
     for i in range(max(args.warmup, 0) + args.steps):
-        cb = cpu_baseline(wl, p)
+        cb = cpu_baseline(w)
         if i >= args.warmup:
             vals.append(cb["value"])
             secs.append(cb["seconds"])
     v = float(np.mean(vals))
-    ms = 1000.0 * float(np.mean(secs))
     line = {"impl": "reference", "metric": "ADO-updates/s", "value": v, "unit": "ADO-updates/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * float(np.mean(secs)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)",
             "data": "synthetic (seeded)",
-            "config": {"workload": args.workload, "n_hrchy": p.n_hrchy(), "n_level": p.n_level,
-                       "solver": wl["solver"], "sample": "bounded CPU sample per step"},
+            "config": {"workload": args.workload, "solver": w.wl["solver"], **w.describe(),
+                       "sample": "bounded CPU sample per step"},
             "cpu_baseline": {**cb, "value": v},
             "e2e": {"value": v, "unit": "ADO-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -183,30 +250,26 @@ def run_ours(args):
     import torch
 
     import libheom_gb300 as lh
-    from libheom_gb300 import configs, roofline
+    from libheom_gb300 import roofline
 
+    from libheom_gb300.dist import job_throughput
     rank, world, local = dist_env()
+    torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    wl = WORKLOADS[args.workload]
-    p = getattr(configs, wl["maker"])()
-    nh, n2 = p.n_hrchy(), p.n_level ** 2
-    N = nh * n2
+    w = Workload(args.workload, rank)
+    wl = w.wl
+    N = w.N
     mixed = args.form == "mixed"
     stream = torch.cuda.Stream(device=dev)
-
-    def make(form_prec):
-        q = lh.from_params(p, precision=form_prec, stream=stream.cuda_stream)
-        return q, lh.qme_solver(q, lh.SOLVERS[wl["solver"]]())
-
-    q, qs = make("mixed" if mixed else "fp64")
-    rho0 = torch.from_numpy(p.rho0_ground()).to(dev)
+    qmes, qs = w.make("mixed" if mixed else "fp64", stream.cuda_stream)
+    rho0 = torch.from_numpy(w.rho0()).to(dev)
     rho = torch.empty_like(rho0)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
     t_list = [0.0, wl["t_final"]]
+    per_rhs = 7 if wl["solver"] == "rkdp" else 4
 
     def step(solver_obj):
         with torch.cuda.stream(stream):
@@ -218,14 +281,14 @@ def run_ours(args):
     max_err = None
     plain = None
     if mixed and not args.no_plain:
-        q64, qs64 = make("fp64")
+        q64, qs64 = w.make("fp64", stream.cuda_stream)
         step(qs64)
         torch.cuda.synchronize()
         ref_final = rho.clone()
         st64 = qs64.stats()
         step(qs)
         torch.cuda.synchronize()
-        max_err = float((rho - ref_final).abs().max().item())
+        max_err = w.errors(rho.cpu().numpy(), ref_final.cpu().numpy())
         # plain FP64 form timed once (after its warm-up above)
         with torch.cuda.stream(stream):
             flush.zero_()
@@ -237,11 +300,12 @@ def run_ours(args):
         ms64 = e0.elapsed_time(e1)
         tm64 = qs64.timing()
         avg64 = 1e-3 * tm64["busy_ms"] / max(tm64["kernels"], 1)
-        fl64 = roofline.flops_per_element(p) * N / avg64 / 1e12
-        plain = {"value": st64["rhs"] * nh / (ms64 / 1e3), "ms_per_step": ms64, "attempts": st64["attempts"],
-                 "avg_stage_kernel_us": 1e6 * avg64,
+        fl64 = w.flops_per_launch() / avg64 / 1e12
+        plain = {"value": st64["rhs"] * w.n_hrchy / (ms64 / 1e3), "ms_per_step": ms64,
+                 "attempts": st64["attempts"], "avg_stage_kernel_us": 1e6 * avg64, "tuning": qs64.tuning(),
                  "roofline": {"bound": "fp64 pipe", "achieved": fl64, "peak": fma_peaks[0], "unit": "TFLOP/s",
                               "frac": fl64 / fma_peaks[0], "peak_source": "measured (heomgb_probe_fma_peaks)"}}
+        qs64.close()
         del qs64, q64
 
     for _ in range(args.warmup):
@@ -258,7 +322,7 @@ def run_ours(args):
     times, rhs, busy, kernels = [], 0, 0.0, 0
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
-            flush.zero_()  # inputs are L2-resident otherwise: flush between steps
+            flush.zero_()  # the state would stay L2-resident otherwise: flush between steps
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         step(qs)
@@ -275,25 +339,21 @@ def run_ours(args):
     if world > 1:
         torch.distributed.barrier()
     clocks = sampler.stop()
-    total_ms = float(sum(times))
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    updates = rhs * nh * world
-    value = updates / (total_ms / 1e3)
+    # units of all ranks over the slowest rank's time (no collective touches the state)
+    value, total_s = job_throughput(rhs * w.n_hrchy, float(sum(times)) / 1e3)
+    total_ms = 1e3 * total_s
 
     # end to end through the public API with host buffers (pinned), copies inside
     rho_h = torch.empty(rho0.shape, dtype=torch.complex128, pin_memory=True)
     e2e_ms = []
-    for i in range(max(1, min(3, args.steps))):
-        rho_h.copy_(torch.from_numpy(p.rho0_ground()))
+    for _ in range(max(1, min(3, args.steps))):
+        rho_h.copy_(torch.from_numpy(w.rho0()))
         arr = rho_h.numpy()
         t0 = time.perf_counter()
         qs.solve(arr, t_list, None, wl["kw"])
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
     e2e_rhs = qs.stats()["rhs"]
-    e2e = {"value": e2e_rhs * nh * world / (statistics.median(e2e_ms) / 1e3), "unit": "ADO-updates/s",
+    e2e = {"value": e2e_rhs * w.n_hrchy * world / (statistics.median(e2e_ms) / 1e3), "unit": "ADO-updates/s",
            "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N}
 
     # roofline of the fused stage kernel
@@ -302,28 +362,27 @@ def run_ours(args):
     avg_launch_s = (busy / 1e3) / max(kernels, 1)
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes_per_launch / avg_launch_s / 1e9
-    flops = roofline.flops_per_element(p) * N
+    flops = w.flops_per_launch()
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": profile_traffic(args.workload, args.form), "peak_source": peak_kind,
             "kernel": "k_rhs_diag (fused RHS + stage epilogue)",
             "alg_bytes_per_launch": alg_bytes_per_launch, "avg_launch_us": avg_launch_s * 1e6,
-            "alg_flops_per_launch": flops,
-            "achieved_tflops": flops / avg_launch_s / 1e12,
+            "alg_flops_per_launch": flops, "achieved_tflops": flops / avg_launch_s / 1e12,
             "fma_peaks_tflops": {"fp64": fma_peaks[0], "fp32": fma_peaks[1]},
-            "note": "state is L2-resident within a propagation; avg launch time includes intra-graph gaps"}
+            "note": "avg launch time = CUDA-event time of graph replays / kernels replayed (includes "
+                    "intra-graph gaps); the 7-site state is L2-resident within a propagation"}
     line = {"metric": "ADO-updates/s", "value": value, "unit": "ADO-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "c64 bulk / c128 state" if mixed else "c128 (f64)", "data": "synthetic (seeded)",
-            "config": {"workload": args.workload, "n_level": p.n_level, "n_modes": p.n_modes,
-                       "max_depth": p.max_depth, "n_hrchy": nh, "solver": wl["solver"], "t_final": wl["t_final"],
+            "config": {"workload": args.workload, **w.describe(), "solver": wl["solver"], "t_final": wl["t_final"],
                        "kwargs": wl["kw"], "form": args.form, "parallelism": f"replicas x{world}",
                        "l2": "flushed between steps (512 MiB write)"},
-            "max_abs_err_vs_fp64": max_err, "plain_fp64": plain,
-            "attempts_per_step": rhs // max(1, args.steps) // (7 if wl["solver"] == "rkdp" else 4),
+            "max_abs_err_vs_fp64": max_err, "plain_fp64": plain, "tuning": qs.tuning(),
+            "attempts_per_step": rhs // max(1, args.steps) // per_rhs,
             "gpu_launches": launches, "e2e": e2e, "roofline": roof, "clocks": clocks}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(wl, p)
+        line["cpu_baseline"] = cpu_baseline(w)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -131,6 +131,21 @@ heomgb_status heomgb_solver_destroy(heomgb_solver* s);
 heomgb_status heomgb_qme_solver_create(heomgb_qme* q, heomgb_solver* s, heomgb_qme_solver** out);
 heomgb_status heomgb_qme_solver_destroy(heomgb_qme_solver* qs);
 
+/* Batched form without a reference counterpart: one qme_solver over `count`
+ * set-up heom_hilb models with diagonal couplings (uneven n_level and depth
+ * allowed) that share a precision; every stage of every instance runs in the
+ * same kernel launch.  The state passed to solve is the concatenation of the
+ * models' states in the given order (heomgb_qme_solver_main_size elements).
+ * rk4 / lsrk4 only (one dt for all instances). */
+heomgb_status heomgb_batch_solver_create(heomgb_qme* const* qmes, int count, heomgb_solver* s,
+                                         heomgb_qme_solver** out);
+/* Elements of the state a solve of qs expects (main_size(), summed over a batch). */
+heomgb_status heomgb_qme_solver_main_size(const heomgb_qme_solver* qs, long long* size);
+/* Tile shape the autotuner picked for the diagonal-coupling kernel: CTA size,
+ * elements per thread and number of tiles (0 for the other kernels). */
+heomgb_status heomgb_qme_solver_tuning(const heomgb_qme_solver* qs, int* block, int* elems_per_thread,
+                                       int* n_tiles);
+
 /* qme_solver::solve(rho, t_list, n_t, callback, kwargs) -- qme_solver.h:44-52,
  * solver_base.h:64-79.  rho: host array of main_size() complex, updated in
  * place; the state crosses host<->device once per output interval exactly as
@@ -156,6 +171,39 @@ heomgb_status heomgb_qme_solver_timing(const heomgb_qme_solver* qs, double* busy
 /* Diagnostic without a reference counterpart: FP64 and FP32 FMA throughput of
  * the current GPU in TFLOP/s, from register-only FMA chains (a few ms). */
 heomgb_status heomgb_probe_fma_peaks(double* fp64_tflops, double* fp32_tflops);
+
+/* ---- learned terminator (no reference counterpart) --------------------------
+ * A small MLP x(d_in) -> Linear(d_hidden) -> GELU -> Linear(d_hidden) -> GELU ->
+ * Linear(d_out), FP32 master weights + BF16 copies, FP32 accumulation, trained
+ * with this library's forward / backward / Adam kernels.  Parameters are packed
+ * [W1 (h x d_in), b1, W2 (h x h), b2, W3 (d_out x h), b3], row-major, FP32.
+ * As a terminator of a model with n_level n and n_dim K it maps
+ * [Re rho_n / s, Im rho_n / s, onehot(k), Re A / s, Im A / s] (4n^2 + K) of a
+ * tier-N ADO, with A the adiabatic estimate of rho_{n+1_k} (its own time
+ * derivative and the commutator with H dropped) and
+ * s = max_e |rho_n[e]|, to rho_{n+1_k} / s (2n^2), i.e. it stands in for the
+ * ADOs that plain truncation drops (ptr_p1 == ptr_void). */
+typedef struct heomgb_mlp heomgb_mlp;
+heomgb_status heomgb_mlp_create(int d_in, int d_hidden, int d_out, unsigned long long seed, heomgb_mlp** out);
+heomgb_status heomgb_mlp_destroy(heomgb_mlp* mlp);
+heomgb_status heomgb_mlp_sizes(const heomgb_mlp* mlp, int* d_in, int* d_hidden, int* d_out, long long* n_params);
+heomgb_status heomgb_mlp_get_params(heomgb_mlp* mlp, float* params);       /* host, n_params floats */
+heomgb_status heomgb_mlp_set_params(heomgb_mlp* mlp, const float* params); /* host, n_params floats */
+/* y = mlp(x) for `batch` rows; x_dev / y_dev are device float arrays. */
+heomgb_status heomgb_mlp_forward(heomgb_mlp* mlp, const float* x_dev, float* y_dev, int batch);
+/* Gradient of mean((mlp(x) - t)^2) with respect to the packed parameters
+ * (grad_host: n_params floats, may be NULL) and the loss; no update. */
+heomgb_status heomgb_mlp_gradients(heomgb_mlp* mlp, const float* x_dev, const float* t_dev, int batch,
+                                   float* grad_host, float* loss);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on that loss. */
+heomgb_status heomgb_mlp_train_step(heomgb_mlp* mlp, const float* x_dev, const float* t_dev, int batch, float lr,
+                                    float* loss);
+/* Use `mlp` (not owned; must outlive the model's solvers) for the truncated
+ * tier of q: an inference launch before every right-hand side fills the
+ * predicted tier-(N+1) ADOs that the +1 coupling term reads.  NULL restores
+ * plain truncation.  heom_hilb with diagonal V only; fails while solvers of q
+ * exist. */
+heomgb_status heomgb_qme_set_terminator(heomgb_qme* q, heomgb_mlp* mlp);
 
 /* ---- building blocks ------------------------------------------------------ */
 /* errnrm1(e, x_1, x_2, atol, rtol) -- linalg_engine_cuda.cu:176-201 and

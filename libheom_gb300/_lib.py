@@ -61,6 +61,10 @@ SIGNATURES = {
     "heomgb_solver_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "heomgb_qme_solver_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "heomgb_qme_solver_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "heomgb_batch_solver_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                                  ctypes.POINTER(ctypes.c_void_p)]),
+    "heomgb_qme_solver_main_size": (ctypes.c_int, [ctypes.c_void_p, c_ll_p]),
+    "heomgb_qme_solver_tuning": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p]),
     "heomgb_qme_solver_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                                CALLBACK, ctypes.c_void_p, ctypes.POINTER(Kwargs)]),
     "heomgb_qme_solver_solve_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -69,6 +73,18 @@ SIGNATURES = {
     "heomgb_qme_solver_stats": (ctypes.c_int, [ctypes.c_void_p, c_ll_p, c_ll_p, c_ll_p, c_double_p]),
     "heomgb_qme_solver_timing": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_ll_p]),
     "heomgb_probe_fma_peaks": (ctypes.c_int, [c_double_p, c_double_p]),
+    "heomgb_mlp_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong,
+                                         ctypes.POINTER(ctypes.c_void_p)]),
+    "heomgb_mlp_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "heomgb_mlp_sizes": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p, c_ll_p]),
+    "heomgb_mlp_get_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "heomgb_mlp_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "heomgb_mlp_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "heomgb_mlp_gradients": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                            ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
+    "heomgb_mlp_train_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                             ctypes.c_float, ctypes.POINTER(ctypes.c_float)]),
+    "heomgb_qme_set_terminator": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "heomgb_errnrm1_scratch": (ctypes.c_size_t, [ctypes.c_longlong]),
     "heomgb_errnrm1_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
                                              ctypes.c_double, ctypes.c_longlong, ctypes.c_void_p, c_double_p,

@@ -207,6 +207,46 @@ struct Bath {
   cd sdelta;
 };
 
+// Tiles of the diagonal-coupling kernel over a list of instances, with the
+// device copies of the instance descriptors and the tile list.
+struct DiagPlan {
+  std::vector<DiagInst> inst;
+  DeviceArena arena;
+  DiagSet ds{};
+  int block = 128, ept = 4, grid = 1;
+};
+
+void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int ept, bool mixed, int n_sm,
+                cudaStream_t s) {
+  P.arena.release();
+  P.inst = insts;
+  std::vector<DiagTile> tiles;
+  size_t smem = 0;
+  long long total = 0;
+  const size_t cap = 200 * 1024;
+  for (size_t i = 0; i < P.inst.size(); ++i) {
+    DiagInst& I = P.inst[i];
+    int tile = std::max(1, (ept * block) / std::max(1, I.n2));
+    while (tile > 1 && diag_tile_smem(I.n2, I.K, tile, mixed) > cap) tile /= 2;
+    if (diag_tile_smem(I.n2, I.K, tile, mixed) > cap)
+      throw unsupported_error("diagonal-coupling path: one ADO tile exceeds shared memory");
+    I.tile = tile;
+    smem = std::max(smem, diag_tile_smem(I.n2, I.K, tile, mixed));
+    for (int l0 = 0; l0 < I.nh; l0 += tile) tiles.push_back(DiagTile{static_cast<int>(i), l0, std::min(tile, I.nh - l0), 0});
+    total = std::max(total, I.elem_off + static_cast<long long>(I.n2) * I.nh);
+  }
+  P.ds.inst = P.arena.upload(P.inst, s);
+  P.ds.tiles = P.arena.upload(tiles, s);
+  P.ds.n_tiles = static_cast<int>(tiles.size());
+  P.ds.total = total;
+  P.ds.smem = smem;
+  P.block = block;
+  P.ept = ept;
+  P.grid = static_cast<int>(std::max<long long>(
+      1, std::min<long long>(static_cast<long long>(tiles.size()), static_cast<long long>(n_sm) * (2048 / block))));
+  ck(cudaStreamSynchronize(s), "plan upload");
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ model object
@@ -228,6 +268,11 @@ struct heomgb_qme {
   // derived
   int K = 0, n_hrchy = 0, path = PATH_DIAG;
   RhsModel dm{};
+  DiagInst dinst{};          // diagonal-coupling instance (PATH_DIAG), device pointers into arena
+  DiagPlan diff_plan;        // tiles for calc_diff
+  heomgb_mlp* term = nullptr;  // learned terminator (not owned); null = plain truncation
+  TermBuffers diff_tb;       // terminator buffers for calc_diff
+  DeviceArena term_arena;
   DeviceArena arena;
   DeviceArena scratch;       // calc_diff host-API buffers
   double2* sx = nullptr;
@@ -241,7 +286,11 @@ struct heomgb_solver {
 };
 
 struct heomgb_qme_solver {
-  heomgb_qme* q = nullptr;
+  heomgb_qme* q = nullptr;             // first (or only) model
+  std::vector<heomgb_qme*> qmes;       // all models of a batch (one entry otherwise)
+  DiagPlan plan;                       // tiles of the diagonal-coupling kernel (autotuned)
+  heomgb_mlp* term = nullptr;          // learned terminator of the model, if any
+  TermBuffers tb;                      // its per-solver inference buffers
   int kind = HEOMGB_RK4;
   cudaStream_t stream = nullptr;
   bool mixed = false;
@@ -291,6 +340,9 @@ void build_model(heomgb_qme* q) {
   if (q->live_solvers > 0) throw state_error("set_param: destroy the qme_solvers of this model first");
   ck(cudaSetDevice(q->device), "cudaSetDevice");
   q->arena.release();
+  q->term_arena.release();
+  q->term = nullptr;  // a rebuilt model starts with plain truncation
+  q->diff_tb = TermBuffers{};
   q->ready = false;
   cudaStream_t s = q->stream();
   const int n = q->n, n2 = n * n, U = q->U;
@@ -385,6 +437,7 @@ void build_model(heomgb_qme* q) {
   m.s = q->arena.upload(to_d2(sv), s);
   m.a = q->arena.upload(to_d2(av), s);
   m.sdelta = q->arena.upload(to_d2(sdelta), s);
+  m.gdiag = q->arena.upload(to_d2(gdiag), s);
   m.sigma_f = q->arena.upload(to_f2(sigma), s);
   m.s_f = q->arena.upload(to_f2(sv), s);
   m.a_f = q->arena.upload(to_f2(av), s);
@@ -396,11 +449,6 @@ void build_model(heomgb_qme* q) {
     q->path = PATH_LIOU;
   }
   if (q->path == PATH_DIAG) {
-    // tile of ADOs per CTA: about four elements per thread, within 200 KB of shared memory
-    m.tile = rhs_tile(m, rhs_block_size(m, PATH_DIAG));
-    while (m.tile > 1 && rhs_smem_bytes(m, PATH_DIAG, false) > 200 * 1024) m.tile /= 2;
-    if (rhs_smem_bytes(m, PATH_DIAG, false) > 200 * 1024)
-      throw unsupported_error("diagonal-coupling path: one ADO tile exceeds shared memory");
     // per-element active modes of the elementwise bath terms
     std::vector<int> pp(n2 + 1, 0), pm(n2 + 1, 0), pmode, mmode;
     std::vector<cd> cp, cmn, csd(n2, cd(0.0, 0.0));
@@ -439,6 +487,32 @@ void build_model(heomgb_qme* q) {
     m.c_minus_f = q->arena.upload(to_f2(cmn), s);
     m.c_sd = q->arena.upload(to_d2(csd), s);
     m.c_sd_f = q->arena.upload(to_f2(csd), s);
+    DiagInst& di = q->dinst;
+    di = DiagInst{};
+    di.n = n;
+    di.n2 = n2;
+    di.K = K;
+    di.nh = nh;
+    di.h_real = m.h_real;
+    di.elem_off = 0;
+    di.p1 = m.p1;
+    di.m1 = m.m1;
+    di.nidx = m.nidx;
+    di.ngd = m.ngd;
+    di.ngd_f = m.ngd_f;
+    di.H = m.H;
+    di.H_f = m.H_f;
+    di.plus_ptr = m.plus_ptr;
+    di.plus_mode = m.plus_mode;
+    di.minus_ptr = m.minus_ptr;
+    di.minus_mode = m.minus_mode;
+    di.c_plus = m.c_plus;
+    di.c_minus = m.c_minus;
+    di.c_plus_f = m.c_plus_f;
+    di.c_minus_f = m.c_minus_f;
+    di.c_sd = m.c_sd;
+    di.c_sd_f = m.c_sd_f;
+    build_plan(q->diff_plan, {di}, 128, 4, q->precision == HEOMGB_MIXED, q->n_sm, s);
   } else if (q->path == PATH_GENERAL) {
     if (rhs_smem_bytes(m, PATH_GENERAL, false) > 200 * 1024)
       throw unsupported_error("general-V Hilbert path supports n_level <= 50");
@@ -505,6 +579,42 @@ Stage base_stage() {
   return st;
 }
 
+// Inference buffers of the terminator for the tier-N ADOs of q (the last
+// C(K+N-1, N) ADOs in the breadth-first order).
+void alloc_term(DeviceArena& A, const heomgb_qme* q, TermBuffers& tb) {
+  int din = 0, h = 0, dout = 0;
+  mlp_dims(q->term, &din, &h, &dout);
+  const int K = q->K, N = q->max_depth;
+  const long long n_tier = N == 0 ? 1 : binom_sat(static_cast<long long>(K) + N - 1, N);
+  tb = TermBuffers{};
+  tb.n_tier = static_cast<int>(n_tier);
+  tb.first = q->n_hrchy - tb.n_tier;
+  tb.n2 = q->n * q->n;
+  tb.K = K;
+  const size_t R = static_cast<size_t>(tb.n_tier) * K;
+  tb.X = static_cast<float*>(A.alloc(sizeof(float) * R * din));
+  tb.A1 = static_cast<float*>(A.alloc(sizeof(float) * R * h));
+  tb.A2 = static_cast<float*>(A.alloc(sizeof(float) * R * h));
+  tb.Y = static_cast<float*>(A.alloc(sizeof(float) * R * dout));
+  tb.scale = static_cast<float*>(A.alloc(sizeof(float) * tb.n_tier));
+  tb.P = static_cast<float2*>(A.alloc(sizeof(float2) * R * tb.n2));
+}
+
+TermModel term_model(const heomgb_qme* q) {
+  TermModel tm;
+  tm.n = q->n;
+  tm.K = q->K;
+  tm.U = q->U;
+  tm.nidx = q->dm.nidx;
+  tm.ngd = q->dm.ngd;
+  tm.gdiag = q->dm.gdiag;
+  tm.s = q->dm.s;
+  tm.a = q->dm.a;
+  tm.V = q->dm.V;
+  tm.bath_ptr = q->dm.bath_ptr;
+  return tm;
+}
+
 void run_diff(heomgb_qme* q, double2* drho, const double2* rho, const double* alpha, const double* beta) {
   Stage st = base_stage();
   st.kind = EPI_DIFF;
@@ -514,15 +624,26 @@ void run_diff(heomgb_qme* q, double2* drho, const double2* rho, const double* al
   st.alpha = make_double2(alpha ? alpha[0] : 1.0, alpha ? alpha[1] : 0.0);
   st.beta = make_double2(beta ? beta[0] : 0.0, beta ? beta[1] : 0.0);
   st.beta_zero = (st.beta.x == 0.0 && st.beta.y == 0.0) ? 1 : 0;
-  const int block = rhs_block_size(q->dm, q->path);
-  const int grid = rhs_grid_size(q->dm, q->path, block, q->n_sm);
-  ck(launch_rhs(q->dm, st, q->path, q->precision == HEOMGB_MIXED, true, grid, block, q->stream()), "calc_diff");
+  const bool diag = q->path == PATH_DIAG;
+  if (q->term) {
+    TermInput in;
+    in.y_fixed = rho;
+    ck(term_enqueue(q->term, q->diff_tb, term_model(q), in, false, q->stream()), "terminator");
+  }
+  const int block = diag ? q->diff_plan.block : rhs_block_size(q->dm, q->path);
+  const int grid = diag ? q->diff_plan.grid : rhs_grid_size(q->dm, q->path, block, q->n_sm);
+  ck(launch_rhs(q->dm, diag ? &q->diff_plan.ds : nullptr, st, q->path, q->precision == HEOMGB_MIXED, true, grid,
+                block, q->stream()),
+     "calc_diff");
 }
 
 // ------------------------------------------------------------------ solvers
+void autotune(heomgb_qme_solver* qs);
+
 void alloc_solver(heomgb_qme_solver* qs) {
   heomgb_qme* q = qs->q;
-  const long long N = q->main_size();
+  long long N = 0;
+  for (heomgb_qme* m : qs->qmes) N += m->main_size();
   qs->N = N;
   qs->mixed = q->precision == HEOMGB_MIXED;
   qs->separate = qs->mixed;
@@ -546,9 +667,75 @@ void alloc_solver(heomgb_qme_solver* qs) {
   ck(cudaMallocHost(reinterpret_cast<void**>(&qs->ctl_host), sizeof(DpCtl)), "cudaMallocHost");
   ck(cudaEventCreate(&qs->ev0), "event create");
   ck(cudaEventCreate(&qs->ev1), "event create");
-  qs->block = rhs_block_size(q->dm, q->path);
-  qs->grid = rhs_grid_size(q->dm, q->path, qs->block, q->n_sm);
+  qs->term = q->term;
+  if (qs->term) {
+    if (qs->qmes.size() != 1) throw unsupported_error("the learned terminator is not available in batches");
+    alloc_term(qs->arena, q, qs->tb);
+  }
+  if (q->path == PATH_DIAG) {
+    autotune(qs);
+    qs->block = qs->plan.block;
+    qs->grid = qs->plan.grid;
+  } else {
+    qs->block = rhs_block_size(q->dm, q->path);
+    qs->grid = rhs_grid_size(q->dm, q->path, qs->block, q->n_sm);
+  }
   qs->partials = static_cast<double*>(A.alloc(sizeof(double) * std::max(qs->grid, 1)));
+}
+
+// Tile shape search for the diagonal-coupling kernel: CTA size x elements per
+// thread (which sets ADOs per tile), timed on right-hand-side launches over
+// the solver's own buffers; the fastest shape is kept for the captured graphs.
+void autotune(heomgb_qme_solver* qs) {
+  heomgb_qme* q = qs->q;
+  std::vector<DiagInst> insts;
+  long long off = 0;
+  for (heomgb_qme* m : qs->qmes) {
+    DiagInst I = m->dinst;
+    I.term_p = qs->term ? qs->tb.P : nullptr;
+    I.term_first = qs->term ? qs->tb.first : 0;
+    I.elem_off = off;
+    off += m->main_size();
+    insts.push_back(I);
+  }
+  double2* out = qs->kind == HEOMGB_RK4 || qs->kind == HEOMGB_LSRK4 ? qs->acc : qs->S[1];
+  ck(cudaMemsetAsync(qs->S[0], 0, sizeof(double2) * qs->N, qs->stream), "memset");
+  Stage st = base_stage();
+  st.kind = EPI_DIFF;
+  st.y_fixed = qs->S[0];
+  st.out = out;
+  st.alpha = make_double2(1.0, 0.0);
+  st.beta_zero = 1;
+  cudaEvent_t e0, e1;
+  ck(cudaEventCreate(&e0), "event");
+  ck(cudaEventCreate(&e1), "event");
+  float best = 1e30f;
+  int best_b = 128, best_e = 4;
+  const int blocks[3] = {64, 128, 256}, epts[4] = {1, 2, 4, 8};
+  for (int b : blocks)
+    for (int e : epts) {
+      try {
+        build_plan(qs->plan, insts, b, e, qs->mixed, q->n_sm, qs->stream);
+      } catch (const unsupported_error&) {
+        continue;
+      }
+      ck(launch_rhs(q->dm, &qs->plan.ds, st, PATH_DIAG, qs->mixed, true, qs->plan.grid, b, qs->stream), "tune");
+      ck(cudaEventRecord(e0, qs->stream), "event");
+      for (int r = 0; r < 3; ++r)
+        ck(launch_rhs(q->dm, &qs->plan.ds, st, PATH_DIAG, qs->mixed, true, qs->plan.grid, b, qs->stream), "tune");
+      ck(cudaEventRecord(e1, qs->stream), "event");
+      ck(cudaEventSynchronize(e1), "event sync");
+      float ms = 0.f;
+      ck(cudaEventElapsedTime(&ms, e0, e1), "event time");
+      if (ms < best) {
+        best = ms;
+        best_b = b;
+        best_e = e;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  build_plan(qs->plan, insts, best_b, best_e, qs->mixed, q->n_sm, qs->stream);
 }
 
 Stage solver_stage(heomgb_qme_solver* qs) {
@@ -566,7 +753,19 @@ Stage solver_stage(heomgb_qme_solver* qs) {
 }
 
 void launch_stage(heomgb_qme_solver* qs, const Stage& st) {
-  ck(launch_rhs(qs->q->dm, st, qs->q->path, qs->mixed, false, qs->grid, qs->block, qs->stream), "stage launch");
+  if (qs->term) {
+    TermInput in;
+    in.y_fixed = st.y_fixed;
+    in.yb[0] = st.Yb[0];
+    in.yb[1] = st.Yb[1];
+    in.y_sel = st.y_sel;
+    in.ctl = st.ctl;
+    ck(term_enqueue(qs->term, qs->tb, term_model(qs->q), in, qs->mixed, qs->stream), "terminator");
+  }
+  const bool diag = qs->q->path == PATH_DIAG;
+  ck(launch_rhs(qs->q->dm, diag ? &qs->plan.ds : nullptr, st, qs->q->path, qs->mixed, false, qs->grid, qs->block,
+                qs->stream),
+     "stage launch");
 }
 
 // One step (RK4/LSRK4) or one attempt (DP5) as a sequence of fused launches.
@@ -623,12 +822,13 @@ cudaGraphExec_t capture_units(heomgb_qme_solver* qs, int units, int* nodes) {
   int launched = 0;
   const long long before = g_launches;
   try {
-    for (int i = 0; i < units; ++i) launched += enqueue_unit(qs);
+    for (int i = 0; i < units; ++i) enqueue_unit(qs);
   } catch (...) {
     cudaStreamEndCapture(qs->stream, &g);
     if (g) cudaGraphDestroy(g);
     throw;
   }
+  launched = static_cast<int>(g_launches - before);  // kernels per replay, terminator included
   g_launches = before;  // captured launches are counted when the graph replays
   ck(cudaStreamEndCapture(qs->stream, &g), "end capture");
   cudaGraphExec_t ex = nullptr;
@@ -750,7 +950,7 @@ int solve_adaptive(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwa
 void solve_impl(heomgb_qme_solver* qs, void* rho, bool host, const double* t_list, int n_t, heomgb_callback cb,
                 void* user, const heomgb_kwargs* kw) {
   if (!qs) throw arg_error("null qme_solver");
-  need_ready(qs->q);
+  for (heomgb_qme* m : qs->qmes) need_ready(m);
   if (!rho) throw arg_error("null rho");
   if (n_t < 1 || !t_list) throw arg_error("t_list must hold at least one time");
   ck(cudaSetDevice(qs->q->device), "cudaSetDevice");
@@ -782,6 +982,10 @@ void solve_impl(heomgb_qme_solver* qs, void* rho, bool host, const double* t_lis
 }
 
 }  // namespace
+
+namespace heomgb {
+void set_error_message(const std::string& msg) { g_err = msg; }
+}  // namespace heomgb
 
 // ======================================================================= C ABI
 extern "C" {
@@ -816,6 +1020,7 @@ heomgb_status heomgb_qme_destroy(heomgb_qme* q) {
   if (q->own_stream) cudaStreamSynchronize(q->own_stream);
   if (q->user_stream_set) cudaStreamSynchronize(q->user_stream);
   q->arena.release();
+  q->term_arena.release();
   q->scratch.release();
   if (q->own_stream) cudaStreamDestroy(q->own_stream);
   delete q;
@@ -900,6 +1105,33 @@ heomgb_status heomgb_qme_set_param(heomgb_qme* q) {
   return guard([&] {
     require(q != nullptr, "null qme");
     build_model(q);
+  });
+}
+
+heomgb_status heomgb_qme_set_terminator(heomgb_qme* q, heomgb_mlp* mlp) {
+  return guard([&] {
+    need_ready(q);
+    if (q->live_solvers > 0) throw state_error("set_terminator: destroy the qme_solvers of this model first");
+    if (mlp) {
+      if (q->path != PATH_DIAG) throw unsupported_error("the learned terminator needs diagonal couplings V (heom_hilb)");
+      int din = 0, h = 0, dout = 0;
+      mlp_dims(mlp, &din, &h, &dout);
+      const int n2 = q->n * q->n;
+      if (din != 4 * n2 + q->K || dout != 2 * n2)
+        throw arg_error("terminator MLP must map 4*n_level^2 + n_dim inputs to 2*n_level^2 outputs");
+    }
+    ck(cudaSetDevice(q->device), "cudaSetDevice");
+    q->term_arena.release();
+    q->diff_tb = TermBuffers{};
+    q->term = mlp;
+    DiagInst di = q->dinst;
+    if (mlp) {
+      alloc_term(q->term_arena, q, q->diff_tb);
+      di.term_p = q->diff_tb.P;
+      di.term_first = q->diff_tb.first;
+    }
+    build_plan(q->diff_plan, {di}, q->diff_plan.block, q->diff_plan.ept, q->precision == HEOMGB_MIXED, q->n_sm,
+               q->stream());
   });
 }
 
@@ -996,6 +1228,7 @@ heomgb_status heomgb_qme_solver_create(heomgb_qme* q, heomgb_solver* s, heomgb_q
     ck(cudaSetDevice(q->device), "cudaSetDevice");
     auto qs = std::make_unique<heomgb_qme_solver>();
     qs->q = q;
+    qs->qmes = {q};
     qs->kind = s->kind;
     qs->stream = q->stream();
     alloc_solver(qs.get());
@@ -1005,13 +1238,58 @@ heomgb_status heomgb_qme_solver_create(heomgb_qme* q, heomgb_solver* s, heomgb_q
   });
 }
 
+heomgb_status heomgb_batch_solver_create(heomgb_qme* const* qmes, int count, heomgb_solver* s,
+                                         heomgb_qme_solver** out) {
+  return guard([&] {
+    require(qmes && s && out && count >= 1, "null argument or empty batch");
+    require(s->kind == HEOMGB_RK4 || s->kind == HEOMGB_LSRK4,
+            "batches step all instances with one dt: rk4 or lsrk4 only");
+    heomgb_qme* q0 = qmes[0];
+    for (int i = 0; i < count; ++i) {
+      need_ready(qmes[i]);
+      if (qmes[i]->path != PATH_DIAG)
+        throw unsupported_error("batches need heom_hilb models with diagonal couplings V");
+      if (qmes[i]->precision != q0->precision) throw arg_error("batch models must share one precision");
+      if (qmes[i]->device != q0->device) throw arg_error("batch models must live on one device");
+    }
+    ck(cudaSetDevice(q0->device), "cudaSetDevice");
+    auto qs = std::make_unique<heomgb_qme_solver>();
+    qs->q = q0;
+    qs->qmes.assign(qmes, qmes + count);
+    qs->kind = s->kind;
+    qs->stream = q0->stream();
+    alloc_solver(qs.get());
+    ck(cudaStreamSynchronize(qs->stream), "solver init sync");
+    for (heomgb_qme* m : qs->qmes) m->live_solvers += 1;
+    *out = qs.release();
+  });
+}
+
 heomgb_status heomgb_qme_solver_destroy(heomgb_qme_solver* qs) {
   if (!qs) return HEOMGB_OK;
   cudaSetDevice(qs->q->device);
   cudaStreamSynchronize(qs->stream);
-  qs->q->live_solvers -= 1;
+  for (heomgb_qme* m : qs->qmes) m->live_solvers -= 1;
   delete qs;
   return HEOMGB_OK;
+}
+
+heomgb_status heomgb_qme_solver_main_size(const heomgb_qme_solver* qs, long long* size) {
+  return guard([&] {
+    require(qs && size, "null argument");
+    *size = qs->N;
+  });
+}
+
+heomgb_status heomgb_qme_solver_tuning(const heomgb_qme_solver* qs, int* block, int* elems_per_thread,
+                                       int* n_tiles) {
+  return guard([&] {
+    require(qs != nullptr, "null qme_solver");
+    const bool diag = qs->q->path == PATH_DIAG;
+    if (block) *block = qs->block;
+    if (elems_per_thread) *elems_per_thread = diag ? qs->plan.ept : 0;
+    if (n_tiles) *n_tiles = diag ? qs->plan.ds.n_tiles : 0;
+  });
 }
 
 heomgb_status heomgb_qme_solver_solve(heomgb_qme_solver* qs, double* rho, const double* t_list, int n_t,

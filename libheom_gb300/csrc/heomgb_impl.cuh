@@ -6,6 +6,8 @@
 #include <cstddef>
 #include <cstdint>
 
+struct heomgb_mlp;
+
 namespace heomgb {
 
 // Which epilogue a right-hand-side launch runs after computing D for its elements.
@@ -35,7 +37,6 @@ struct DpCtl {
 struct RhsModel {
   int n, n2, K, U, n_hrchy;
   int h_real;                       // H has zero imaginary part
-  int tile;                         // ADOs per CTA tile (diagonal-coupling kernel)
   const int* p1;                    // (n_hrchy+1)*K, sentinel n_hrchy
   const int* m1;                    // (n_hrchy+1)*K
   const int* nidx;                  // n_hrchy*K
@@ -65,6 +66,7 @@ struct RhsModel {
   const double2* s;                 // K
   const double2* a;                 // K
   const double2* sdelta;            // U
+  const double2* gdiag;             // K: gamma_kk of every linear mode
   const float2* sigma_f;
   const float2* s_f;
   const float2* a_f;
@@ -108,14 +110,57 @@ struct Stage {
 
 enum Path : int { PATH_DIAG = 0, PATH_GENERAL = 1, PATH_LIOU = 2 };
 
+// One instance of the diagonal-coupling kernel: a model's sizes, where its
+// elements start in the (possibly concatenated) state vector, and its tables.
+// A single model is a set of one instance; a batch concatenates many.
+struct DiagInst {
+  int n, n2, K, nh;
+  int h_real;
+  int tile;                 // ADOs per CTA tile
+  long long elem_off;       // first element of this instance in the state vector
+  const int* p1;
+  const int* m1;
+  const int* nidx;
+  const double2* ngd;
+  const float2* ngd_f;
+  const double2* H;
+  const float2* H_f;
+  const int* plus_ptr;
+  const int* plus_mode;
+  const int* minus_ptr;
+  const int* minus_mode;
+  const double2* c_plus;
+  const double2* c_minus;
+  const float2* c_plus_f;
+  const float2* c_minus_f;
+  const double2* c_sd;
+  const float2* c_sd_f;
+  // learned terminator: predicted rho_{n+1_k} of the tier-N ADOs, row
+  // (l - term_first)*K + k, used where ptr_p1 is the sentinel; null = truncation
+  const float2* term_p;
+  int term_first;
+  int pad_;
+};
+struct DiagTile {
+  int inst, l0, nt, pad;
+};
+struct DiagSet {
+  const DiagInst* inst;     // device array
+  const DiagTile* tiles;    // device array
+  int n_tiles;
+  long long total;          // elements over all instances
+  size_t smem;              // dynamic shared memory of the largest tile
+};
+
 // Launchers (kernels.cu).  `mixed` selects FP32 bulk arithmetic; `in_double`
-// says the RHS input is a double2 array even in mixed mode.
-cudaError_t launch_rhs(const RhsModel& m, const Stage& st, int path, bool mixed, bool in_double, int grid,
-                       int block, cudaStream_t s);
+// says the RHS input is a double2 array even in mixed mode.  `ds` describes
+// the diagonal-coupling work (PATH_DIAG only).
+cudaError_t launch_rhs(const RhsModel& m, const DiagSet* ds, const Stage& st, int path, bool mixed, bool in_double,
+                       int grid, int block, cudaStream_t s);
 int rhs_block_size(const RhsModel& m, int path);
-int rhs_tile(const RhsModel& m, int block);
 int rhs_grid_size(const RhsModel& m, int path, int block, int n_sm);
 size_t rhs_smem_bytes(const RhsModel& m, int path, bool mixed);
+size_t diag_tile_smem(int n2, int K, int tile, bool mixed);
 
 cudaError_t launch_hrchy_build(int K, int depth, int n_hrchy, const long long* binom, int binom_dim, int* nidx,
                                int* p1, int* m1, cudaStream_t s);
@@ -130,6 +175,39 @@ cudaError_t launch_errnrm1(const double2* e, const double2* x1, const double2* x
                            cudaStream_t s);
 int errnrm1_grid(long long n);
 cudaError_t probe_fma_peaks(int n_sm, double* fp64_tflops, double* fp32_tflops, cudaStream_t s);
+
+// Buffers of one terminator inference over the tier-N ADOs [first, first+n_tier).
+struct TermBuffers {
+  int first = 0, n_tier = 0, n2 = 0, K = 0;
+  float* X = nullptr;      // rows x (2 n2 + K)
+  float* A1 = nullptr;     // rows x hidden
+  float* A2 = nullptr;
+  float* Y = nullptr;      // rows x 2 n2
+  float* scale = nullptr;  // n_tier
+  float2* P = nullptr;     // rows x n2 predictions
+};
+// Where the terminator reads its input: as a stage kernel picks its own
+// (0: y_fixed, 1: yb[cur], 2: yb[1-cur], with cur from ctl).
+struct TermInput {
+  const void* y_fixed = nullptr;
+  const void* yb[2] = {nullptr, nullptr};
+  int y_sel = 0;
+  const DpCtl* ctl = nullptr;
+};
+// Model constants the terminator's input features use (device pointers).
+struct TermModel {
+  int n = 0, K = 0, U = 0;
+  const int* nidx = nullptr;      // n_hrchy*K
+  const double2* ngd = nullptr;   // n_hrchy
+  const double2* gdiag = nullptr; // K: gamma_kk
+  const double2* s = nullptr;     // K
+  const double2* a = nullptr;     // K
+  const double2* V = nullptr;     // U*n2
+  const int* bath_ptr = nullptr;  // U+1
+};
+cudaError_t term_enqueue(heomgb_mlp* M, const TermBuffers& tb, const TermModel& tm, const TermInput& in,
+                         bool y_float, cudaStream_t s);
+void mlp_dims(const heomgb_mlp* M, int* din, int* h, int* dout);
 
 extern long long g_launches;  // kernels launched (incremented by the launchers / graph replays)
 

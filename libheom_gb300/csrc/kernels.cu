@@ -65,6 +65,23 @@ template <typename TC> __device__ __forceinline__ double2 ld_bulk(const void* ba
     return to_d(static_cast<const float2*>(base)[g]);
   }
 }
+// Streaming (evict-first) variants for the epilogue's own vectors: they are
+// touched once per stage, so they should not push the right-hand-side input,
+// which every neighbour gather reads, out of L2.
+template <typename TC> __device__ __forceinline__ void st_bulk_cs(void* base, size_t g, double2 v) {
+  if constexpr (std::is_same<TC, double>::value) {
+    __stcs(static_cast<double2*>(base) + g, v);
+  } else {
+    __stcs(static_cast<float2*>(base) + g, make_float2(static_cast<float>(v.x), static_cast<float>(v.y)));
+  }
+}
+template <typename TC> __device__ __forceinline__ double2 ld_bulk_cs(const void* base, size_t g) {
+  if constexpr (std::is_same<TC, double>::value) {
+    return __ldcs(static_cast<const double2*>(base) + g);
+  } else {
+    return to_d(__ldcs(static_cast<const float2*>(base) + g));
+  }
+}
 // value a bulk vector will hold after a store (rounding in mixed mode)
 template <typename TC> __device__ __forceinline__ double2 as_bulk(double2 v) {
   if constexpr (std::is_same<TC, double>::value) {
@@ -119,23 +136,123 @@ __device__ void dp_control(DpCtl* c, double sumsq, long long n) {
 
 // ------------------------------------------------------------------ fused stage epilogue
 // D is the operator value of heom_hilb.h:96-353 at element g; every solver
-// stage uses k = -dt*D (calc_diff_impl with alpha = dt, beta = 0).  Returns
-// the element's squared scaled error for EPI_DP7, else 0.
+// stage uses k = -dt*D (calc_diff_impl with alpha = dt, beta = 0).
+//
+// The epilogue is split in two: epi_pre reads everything the stage
+// combination needs that does not depend on D (issued before the
+// right-hand side so its loads overlap it), epi_post adds the k term and
+// stores.  epi_post returns the element's squared scaled error for EPI_DP7,
+// else 0.
 //
 // FP64 form (TC = double): the reference's operation order (rk4.h:40-65,
 // lsrk4.h:32-47, rkdp.h:111-153).  Mixed form (TC = float): stage inputs of
 // the next right-hand side are formed in FP32 from the bulk copy of the
 // state; the state, the RK4 accumulator, the LSRK4 buffer, the candidate
 // state rho + sum_j B_j k_j and the error vector e = sum_j E_j k_j are FP64.
+struct EpiPre {
+  double2 a;   // FP64 partial result (accumulator, base state, partial sum)
+  double2 b;   // FP64 base state (RK4 in FP64 form, LSRK4)
+  float2 f;    // FP32 partial result (mixed-form stage inputs)
+  double m;    // squared error scale (EPI_DP7)
+};
+
 template <typename TC>
-__device__ __forceinline__ double epilogue(const Stage& st, size_t g, cx_t<TC> Dc, double dt, int cur) {
+__device__ __forceinline__ EpiPre epi_pre(const Stage& st, size_t g, int cur) {
+  constexpr bool MIX = std::is_same<TC, float>::value;
+  EpiPre p;
+  p.a = make_double2(0.0, 0.0);
+  p.b = make_double2(0.0, 0.0);
+  p.f = make_float2(0.f, 0.f);
+  p.m = 0.0;
+  switch (st.kind) {
+    case EPI_DIFF:
+      if (!st.beta_zero) p.a = cmul(st.beta, st.out[g]);
+      break;
+    case EPI_RK4_1:
+    case EPI_RK4_2:
+    case EPI_RK4_3:
+      p.a = st.kind == EPI_RK4_1 ? __ldcs(st.S[0] + g) : __ldcs(st.acc + g);
+      if constexpr (MIX)
+        p.f = static_cast<const float2*>(st.Yb[0])[g];
+      else
+        p.b = __ldcs(st.S[0] + g);
+      break;
+    case EPI_RK4_4:
+      p.a = __ldcs(st.acc + g);
+      break;
+    case EPI_LS:
+      if (!st.ls_first) p.a = __ldcs(st.acc + g);
+      p.b = __ldcs(st.S[st.ls_in] + g);
+      break;
+    case EPI_DP: {
+      const int s_ = st.dp_stage;
+      if constexpr (MIX) {
+        if (s_ < 5) {
+          float2 y = static_cast<const float2*>(st.Yb[cur])[g];
+          for (int j = 0; j < s_; ++j) {
+            const float c = static_cast<float>(c_dpA[s_ + 1][j]);
+            const float2 kj = __ldcs(static_cast<const float2*>(st.K[j]) + g);
+            y.x = fmaf(c, kj.x, y.x);
+            y.y = fmaf(c, kj.y, y.y);
+          }
+          p.f = y;
+        } else {  // candidate state rho + sum_j B_j k_j in FP64
+          double2 y = __ldcs(st.S[cur] + g);
+          for (int j = 0; j < 5; ++j) {
+            const double c = c_dpA[6][j];
+            const float2 kj = __ldcs(static_cast<const float2*>(st.K[j]) + g);
+            y.x += c * static_cast<double>(kj.x);
+            y.y += c * static_cast<double>(kj.y);
+          }
+          p.a = y;
+        }
+      } else {
+        double2 y = __ldcs(st.S[cur] + g);
+        for (int j = 0; j < s_; ++j) {
+          const double c = c_dpA[s_ + 1][j];
+          const double2 kj = ld_bulk_cs<TC>(st.K[j], g);
+          y.x += c * kj.x;
+          y.y += c * kj.y;
+        }
+        p.a = y;
+      }
+      break;
+    }
+    case EPI_DP7: {
+      const double2 k0 = ld_bulk_cs<TC>(st.K[0], g);
+      double2 e = make_double2(c_dpE[0] * k0.x, c_dpE[0] * k0.y);
+      for (int j = 1; j < 6; ++j) {
+        const double2 kj = ld_bulk_cs<TC>(st.K[j], g);
+        e.x += c_dpE[j] * kj.x;
+        e.y += c_dpE[j] * kj.y;
+      }
+      p.a = e;
+      if constexpr (MIX) {  // scale from the bulk copies of both states
+        const float2 x1 = static_cast<const float2*>(st.Yb[1 - cur])[g];
+        const float2 x2 = static_cast<const float2*>(st.Yb[cur])[g];
+        p.m = static_cast<double>(fmaxf(x1.x * x1.x + x1.y * x1.y, x2.x * x2.x + x2.y * x2.y));
+      } else {
+        const double2 x1 = __ldcs(st.S[1 - cur] + g);
+        const double2 x2 = __ldcs(st.S[cur] + g);
+        p.m = fmax(x1.x * x1.x + x1.y * x1.y, x2.x * x2.x + x2.y * x2.y);
+      }
+      break;
+    }
+    default:
+      break;
+  }
+  return p;
+}
+
+template <typename TC>
+__device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> Dc, double dt, int cur,
+                                           const EpiPre& p) {
   constexpr bool MIX = std::is_same<TC, float>::value;
   const double2 D = to_d(Dc);
   switch (st.kind) {
     case EPI_DIFF: {
-      double2 o = st.beta_zero ? make_double2(0.0, 0.0) : cmul(st.beta, st.out[g]);
       const double2 ad = cmul(st.alpha, D);
-      st.out[g] = make_double2(o.x - ad.x, o.y - ad.y);
+      st.out[g] = make_double2(p.a.x - ad.x, p.a.y - ad.y);
       return 0.0;
     }
     case EPI_RK4_1:
@@ -143,51 +260,43 @@ __device__ __forceinline__ double epilogue(const Stage& st, size_t g, cx_t<TC> D
     case EPI_RK4_3: {  // rho_n = rho + c*k ; acc = rho + k/6 or acc += k/3 (2/6 on k2+k3)
       const double c = st.kind == EPI_RK4_3 ? 1.0 : 0.5;
       const double w = st.kind == EPI_RK4_1 ? (1.0 / 6.0) : (2.0 / 6.0);
-      double2 a = st.kind == EPI_RK4_1 ? st.S[0][g] : st.acc[g];
+      double2 a = p.a;
       if constexpr (MIX) {
         const float fdt = static_cast<float>(dt);
         const float2 k = make_float2(-fdt * Dc.x, -fdt * Dc.y);
-        const float2 s = static_cast<const float2*>(st.Yb[0])[g];
-        static_cast<float2*>(st.Ynext)[g] = make_float2(s.x + static_cast<float>(c) * k.x,
-                                                        s.y + static_cast<float>(c) * k.y);
+        static_cast<float2*>(st.Ynext)[g] = make_float2(p.f.x + static_cast<float>(c) * k.x,
+                                                        p.f.y + static_cast<float>(c) * k.y);
         a.x += static_cast<double>(static_cast<float>(w) * k.x);
         a.y += static_cast<double>(static_cast<float>(w) * k.y);
       } else {
         const double2 k = make_double2(-dt * D.x, -dt * D.y);
-        const double2 s = st.S[0][g];
-        st_bulk<TC>(st.Ynext, g, make_double2(s.x + c * k.x, s.y + c * k.y));
+        st_bulk<TC>(st.Ynext, g, make_double2(p.b.x + c * k.x, p.b.y + c * k.y));
         a.x += w * k.x;
         a.y += w * k.y;
       }
-      st.acc[g] = a;
+      __stcs(st.acc + g, a);
       return 0.0;
     }
     case EPI_RK4_4: {  // rho = acc + k4/6
-      const double2 a = st.acc[g];
       double2 v;
       if constexpr (MIX) {
         const float fdt = static_cast<float>(dt);
-        v = make_double2(a.x + static_cast<double>((1.0f / 6.0f) * (-fdt * Dc.x)),
-                         a.y + static_cast<double>((1.0f / 6.0f) * (-fdt * Dc.y)));
+        v = make_double2(p.a.x + static_cast<double>((1.0f / 6.0f) * (-fdt * Dc.x)),
+                         p.a.y + static_cast<double>((1.0f / 6.0f) * (-fdt * Dc.y)));
       } else {
         const double2 k = make_double2(-dt * D.x, -dt * D.y);
-        v = make_double2(a.x + (1.0 / 6.0) * k.x, a.y + (1.0 / 6.0) * k.y);
+        v = make_double2(p.a.x + (1.0 / 6.0) * k.x, p.a.y + (1.0 / 6.0) * k.y);
       }
-      st.S[0][g] = v;
+      __stcs(st.S[0] + g, v);
       if (st.bulk_separate) st_bulk<TC>(st.Yb[0], g, v);
       return 0.0;
     }
     case EPI_LS: {  // buff = -buff + k (beta=-1) or k (beta=0); rho += B*buff
       const double2 k = make_double2(-dt * D.x, -dt * D.y);
-      double2 b = k;
-      if (!st.ls_first) {
-        const double2 o = st.acc[g];
-        b = make_double2(-o.x + k.x, -o.y + k.y);
-      }
-      st.acc[g] = b;
-      const double2 s = st.S[st.ls_in][g];
-      const double2 v = make_double2(s.x + st.coef * b.x, s.y + st.coef * b.y);
-      st.S[1 - st.ls_in][g] = v;
+      const double2 b = st.ls_first ? k : make_double2(-p.a.x + k.x, -p.a.y + k.y);
+      __stcs(st.acc + g, b);
+      const double2 v = make_double2(p.b.x + st.coef * b.x, p.b.y + st.coef * b.y);
+      __stcs(st.S[1 - st.ls_in] + g, v);
       if (st.bulk_separate) st_bulk<TC>(st.Yb[1 - st.ls_in], g, v);
       return 0.0;
     }
@@ -196,49 +305,28 @@ __device__ __forceinline__ double epilogue(const Stage& st, size_t g, cx_t<TC> D
       if constexpr (MIX) {
         const float fdt = static_cast<float>(dt);
         const float2 k = make_float2(-fdt * Dc.x, -fdt * Dc.y);
-        static_cast<float2*>(st.K[s_])[g] = k;
+        __stcs(static_cast<float2*>(st.K[s_]) + g, k);
         if (s_ < 5) {
-          float2 y = static_cast<const float2*>(st.Yb[cur])[g];
-          for (int j = 0; j < s_; ++j) {
-            const float c = static_cast<float>(c_dpA[s_ + 1][j]);
-            const float2 kj = static_cast<const float2*>(st.K[j])[g];
-            y.x = fmaf(c, kj.x, y.x);
-            y.y = fmaf(c, kj.y, y.y);
-          }
           const float c = static_cast<float>(c_dpA[s_ + 1][s_]);
-          y.x = fmaf(c, k.x, y.x);
-          y.y = fmaf(c, k.y, y.y);
-          static_cast<float2*>(st.Ynext)[g] = y;
-        } else {  // candidate state rho + sum_j B_j k_j in FP64
-          double2 y = st.S[cur][g];
-          for (int j = 0; j < 5; ++j) {
-            const double c = c_dpA[6][j];
-            const float2 kj = static_cast<const float2*>(st.K[j])[g];
-            y.x += c * static_cast<double>(kj.x);
-            y.y += c * static_cast<double>(kj.y);
-          }
+          static_cast<float2*>(st.Ynext)[g] = make_float2(fmaf(c, k.x, p.f.x), fmaf(c, k.y, p.f.y));
+        } else {
+          double2 y = p.a;
           y.x += c_dpA[6][5] * static_cast<double>(k.x);
           y.y += c_dpA[6][5] * static_cast<double>(k.y);
-          st.S[1 - cur][g] = y;
+          __stcs(st.S[1 - cur] + g, y);
           static_cast<float2*>(st.Yb[1 - cur])[g] = make_float2(static_cast<float>(y.x), static_cast<float>(y.y));
         }
       } else {
         const double2 k = make_double2(-dt * D.x, -dt * D.y);
-        st_bulk<TC>(st.K[s_], g, k);
-        double2 y = st.S[cur][g];
-        for (int j = 0; j < s_; ++j) {
-          const double c = c_dpA[s_ + 1][j];
-          const double2 kj = ld_bulk<TC>(st.K[j], g);
-          y.x += c * kj.x;
-          y.y += c * kj.y;
-        }
+        st_bulk_cs<TC>(st.K[s_], g, k);
+        double2 y = p.a;
         const double c = c_dpA[s_ + 1][s_];
         y.x += c * k.x;
         y.y += c * k.y;
         if (s_ < 5)
           st_bulk<TC>(st.Ynext, g, y);
         else
-          st.S[1 - cur][g] = y;
+          __stcs(st.S[1 - cur] + g, y);
       }
       return 0.0;
     }
@@ -250,33 +338,29 @@ __device__ __forceinline__ double epilogue(const Stage& st, size_t g, cx_t<TC> D
       } else {
         k7 = make_double2(-dt * D.x, -dt * D.y);
       }
-      const double2 k0 = ld_bulk<TC>(st.K[0], g);
-      double2 e = make_double2(c_dpE[0] * k0.x, c_dpE[0] * k0.y);
-      for (int j = 1; j < 6; ++j) {
-        const double2 kj = ld_bulk<TC>(st.K[j], g);
-        e.x += c_dpE[j] * kj.x;
-        e.y += c_dpE[j] * kj.y;
-      }
+      double2 e = p.a;
       e.x += c_dpE[6] * k7.x;
       e.y += c_dpE[6] * k7.y;
       const double e2 = e.x * e.x + e.y * e.y;
-      if constexpr (MIX) {  // scale from the bulk copies of both states
-        const float2 x1 = static_cast<const float2*>(st.Yb[1 - cur])[g];
-        const float2 x2 = static_cast<const float2*>(st.Yb[cur])[g];
-        const float m = sqrtf(fmaxf(x1.x * x1.x + x1.y * x1.y, x2.x * x2.x + x2.y * x2.y));
-        const float s = static_cast<float>(st.ctl->atol) + static_cast<float>(st.ctl->rtol) * m;
+      if constexpr (MIX) {
+        const float s = static_cast<float>(st.ctl->atol) +
+                        static_cast<float>(st.ctl->rtol) * sqrtf(static_cast<float>(p.m));
         return e2 * static_cast<double>(1.0f / (s * s));
       } else {
-        const double2 x1 = st.S[1 - cur][g];
-        const double2 x2 = st.S[cur][g];
-        const double m = sqrt(fmax(x1.x * x1.x + x1.y * x1.y, x2.x * x2.x + x2.y * x2.y));
-        const double s = st.ctl->atol + st.ctl->rtol * m;
+        const double s = st.ctl->atol + st.ctl->rtol * sqrt(p.m);
         return e2 / (s * s);
       }
     }
     default:
       return 0.0;
   }
+}
+
+// Both halves at once, for kernels that do not overlap them.
+template <typename TC>
+__device__ __forceinline__ double epilogue(const Stage& st, size_t g, cx_t<TC> Dc, double dt, int cur) {
+  const EpiPre p = epi_pre<TC>(st, g, cur);
+  return epi_post<TC>(st, g, Dc, dt, cur, p);
 }
 
 // Block-level sum of `v`; result valid in thread 0.
@@ -345,52 +429,164 @@ __device__ __forceinline__ bool stage_prologue(const Stage& st, double& dt, int&
 // [V,X]_ab = (v_a - v_b) X_ab and {V,X}_ab = (v_a + v_b) X_ab, so element e
 // only needs the neighbour ADOs of the modes whose bath couples e.
 //
-// A CTA owns a tile of `tile` consecutive ADOs (contiguous in HBM).  The
-// tile's RHS input, H and the tile's hierarchy rows (neighbour indices and
-// occupation numbers) are staged in shared memory with coalesced loads; the
-// commutator then reads shared memory only, and every bath term costs one
-// global load of the neighbour's element.
+// Work is a list of tiles; a tile is `nt` consecutive ADOs of one instance
+// (contiguous in HBM).  A CTA stages the tile's RHS input, the instance's H
+// and the tile's hierarchy rows (neighbour indices, occupation numbers) in
+// shared memory with coalesced loads; the commutator then reads shared memory
+// only, and every bath term costs one global load of the neighbour's element.
+// A single model is one instance; a batch of uneven instances (different
+// n_state and depth) is many, all in the same launch.
 template <typename TC, typename TB, bool HREAL>
-__global__ void __launch_bounds__(256) k_rhs_diag(const RhsModel m, const Stage st) {
+__device__ __forceinline__ double diag_tile(const DiagInst* __restrict__ I, const DiagTile td, const Stage& st,
+                                            const TB* __restrict__ y, double dt, int cur, unsigned char* smem_raw) {
   using C = cx_t<TC>;
-  const int tile = m.tile;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  double dt;
-  int cur;
-  if (!stage_prologue(st, dt, cur)) return;
-  const TB* __restrict__ y = stage_input<TB>(st, cur);
-  const int n = m.n, n2 = m.n2, K = m.K, nh = m.n_hrchy, void_idx = m.n_hrchy;
+  const int n = I->n, n2 = I->n2, K = I->K, void_idx = I->nh, tile = I->tile;
+  const long long base = I->elem_off;
   C* Hs = reinterpret_cast<C*>(smem_raw);        // n2
   C* yt = Hs + n2;                                // tile*n2
   int* p1s = reinterpret_cast<int*>(yt + static_cast<size_t>(tile) * n2);  // tile*K
-  int* m1s = p1s + tile * K;                      // tile*K
-  int* nks = m1s + tile * K;                      // tile*K
-  const C* __restrict__ Hg = pick<TC>(m.H, m.H_f);
-  const C* __restrict__ ngd = pick<TC>(m.ngd, m.ngd_f);
-  const C* __restrict__ cpl = pick<TC>(m.c_plus, m.c_plus_f);
-  const C* __restrict__ cmi = pick<TC>(m.c_minus, m.c_minus_f);
-  const C* __restrict__ csd = pick<TC>(m.c_sd, m.c_sd_f);
+  int* m1s = p1s + tile * K;
+  int* nks = m1s + tile * K;
+  const C* __restrict__ Hg = pick<TC>(I->H, I->H_f);
+  const C* __restrict__ ngd = pick<TC>(I->ngd, I->ngd_f);
+  const C* __restrict__ cpl = pick<TC>(I->c_plus, I->c_plus_f);
+  const C* __restrict__ cmi = pick<TC>(I->c_minus, I->c_minus_f);
+  const C* __restrict__ csd = pick<TC>(I->c_sd, I->c_sd_f);
+  const float2* __restrict__ term_p = I->term_p;
+  const int term_first = I->term_first;
+  const int* __restrict__ plus_ptr = I->plus_ptr;
+  const int* __restrict__ plus_mode = I->plus_mode;
+  const int* __restrict__ minus_ptr = I->minus_ptr;
+  const int* __restrict__ minus_mode = I->minus_mode;
+  const TB* __restrict__ yi = y + base;
+  const int l0 = td.l0, nt = td.nt, ne = nt * n2;
   for (int i = threadIdx.x; i < n2; i += blockDim.x) Hs[i] = Hg[i];
-  const int n_tiles = (nh + tile - 1) / tile;
+  const TB* __restrict__ ysrc = yi + static_cast<size_t>(l0) * n2;
+  for (int i = threadIdx.x; i < ne; i += blockDim.x) yt[i] = ldc<TC>(ysrc + i);
+  for (int i = threadIdx.x; i < nt * K; i += blockDim.x) {
+    const size_t gi = static_cast<size_t>(l0) * K + i;
+    p1s[i] = __ldg(I->p1 + gi);
+    m1s[i] = __ldg(I->m1 + gi);
+    nks[i] = __ldg(I->nidx + gi);
+  }
+  __syncthreads();
   double local = 0.0;
-  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-    const int l0 = t * tile;
-    const int nt = min(tile, nh - l0);
-    const int ne = nt * n2;
-    const TB* __restrict__ ysrc = y + static_cast<size_t>(l0) * n2;
-    for (int i = threadIdx.x; i < ne; i += blockDim.x) yt[i] = ldc<TC>(ysrc + i);
-    for (int i = threadIdx.x; i < nt * K; i += blockDim.x) {
-      const size_t gi = static_cast<size_t>(l0) * K + i;
-      p1s[i] = __ldg(m.p1 + gi);
-      m1s[i] = __ldg(m.m1 + gi);
-      nks[i] = __ldg(m.nidx + gi);
+  // Bath terms, damping and the stage epilogue of element e of tile ADO lt.
+  // The neighbour loads of up to four +1 and four -1 terms are issued
+  // together so their L2 latencies overlap.
+  auto finish = [&](int lt, int e, int i, C D, const EpiPre& pre) {
+    const C* yl = yt + lt * n2;
+    // (sum_k n_k gamma_k + sum_u s_delta_u (v_a - v_b)^2) rho
+    const C g0 = ngd[l0 + lt], g1 = csd[e];
+    cfma(D, cx<TC>(g0.x + g1.x, g0.y + g1.y), yl[e]);
+    const int* p1row = p1s + lt * K;
+    const int* m1row = m1s + lt * K;
+    const int* nrow = nks + lt * K;
+    const int pb = __ldg(plus_ptr + e), pe = __ldg(plus_ptr + e + 1);
+    const int mb = __ldg(minus_ptr + e), me = __ldg(minus_ptr + e + 1);
+    for (int pp = pb, mp = mb; pp < pe || mp < me; pp += 4, mp += 4) {
+      C v[8], cf[8];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int p = pp + j;
+        v[j] = cx<TC>(0, 0);
+        cf[j] = cx<TC>(0, 0);
+        if (p < pe) {
+          const int k = __ldg(plus_mode + p);
+          const int lp = p1row[k];
+          if (lp != void_idx) {
+            v[j] = ldc<TC>(yi + static_cast<size_t>(lp) * n2 + e);
+            cf[j] = cpl[p];
+          } else if (term_p) {  // truncated tier: the terminator's prediction
+            const float2 t = term_p[(static_cast<size_t>(l0 + lt - term_first) * K + k) * n2 + e];
+            v[j] = cx<TC>(static_cast<TC>(t.x), static_cast<TC>(t.y));
+            cf[j] = cpl[p];
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int p = mp + j;
+        v[4 + j] = cx<TC>(0, 0);
+        cf[4 + j] = cx<TC>(0, 0);
+        if (p < me) {
+          const int k = __ldg(minus_mode + p);
+          const int lm = m1row[k];
+          if (lm != void_idx) {
+            const TC nk = static_cast<TC>(nrow[k]);
+            const C cm = cmi[p];
+            v[4 + j] = ldc<TC>(yi + static_cast<size_t>(lm) * n2 + e);
+            cf[4 + j] = cx<TC>(nk * cm.x, nk * cm.y);
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) cfma(D, cf[j], v[j]);
     }
-    __syncthreads();
+    local += epi_post<TC>(st, static_cast<size_t>(base + static_cast<long long>(l0) * n2 + i), D, dt, cur, pre);
+  };
+  if ((n & 3) == 0 && n >= 8) {
+    // 1 x 4 register micro-tile: a thread owns 4 consecutive elements of a
+    // row, so every H / rho value read from shared memory feeds 4 products.
+    const int ng = ne >> 2;
+    for (int q = threadIdx.x; q < ng; q += blockDim.x) {
+      const int i0 = q << 2;
+      const int lt = i0 / n2;
+      const int e0 = i0 - lt * n2;
+      const int a = e0 / n, b0 = e0 - a * n;
+      const C* yl = yt + lt * n2;
+      C acc[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[j] = cx<TC>(0, 0);
+      if (HREAL) {
+#pragma unroll 2
+        for (int c = 0; c < n; ++c) {
+          const TC hac = Hs[a * n + c].x;
+          const C yac = yl[a * n + c];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const C ycb = yl[c * n + b0 + j];
+            const TC hcb = Hs[c * n + b0 + j].x;
+            acc[j].x = fma(hac, ycb.x, acc[j].x);
+            acc[j].x = fma(-hcb, yac.x, acc[j].x);
+            acc[j].y = fma(hac, ycb.y, acc[j].y);
+            acc[j].y = fma(-hcb, yac.y, acc[j].y);
+          }
+        }
+      } else {
+        C neg[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) neg[j] = cx<TC>(0, 0);
+#pragma unroll 2
+        for (int c = 0; c < n; ++c) {
+          const C hac = Hs[a * n + c];
+          const C yac = yl[a * n + c];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            cfma(acc[j], hac, yl[c * n + b0 + j]);
+            cfma(neg[j], yac, Hs[c * n + b0 + j]);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          acc[j].x -= neg[j].x;
+          acc[j].y -= neg[j].y;
+        }
+      }
+#pragma unroll 1
+      for (int j = 0; j < 4; ++j) {
+        const EpiPre pre =
+            epi_pre<TC>(st, static_cast<size_t>(base + static_cast<long long>(l0) * n2 + i0 + j), cur);
+        finish(lt, e0 + j, i0 + j, cx<TC>(-acc[j].y, acc[j].x), pre);
+      }
+    }
+  } else {
     for (int i = threadIdx.x; i < ne; i += blockDim.x) {
       const int lt = i / n2;
       const int e = i - lt * n2;
       const int a = e / n, b = e - a * n;
       const C* yl = yt + lt * n2;
+      const EpiPre pre = epi_pre<TC>(st, static_cast<size_t>(base + static_cast<long long>(l0) * n2 + i), cur);
       // i[H, rho]
       C acc = cx<TC>(0, 0);
       if (HREAL) {
@@ -413,34 +609,30 @@ __global__ void __launch_bounds__(256) k_rhs_diag(const RhsModel m, const Stage 
         acc.x -= neg.x;
         acc.y -= neg.y;
       }
-      C D = cx<TC>(-acc.y, acc.x);
-      // (sum_k n_k gamma_k + sum_u s_delta_u (v_a - v_b)^2) rho
-      const C g0 = ngd[l0 + lt], g1 = csd[e];
-      cfma(D, cx<TC>(g0.x + g1.x, g0.y + g1.y), yl[e]);
-      // bath couplings of this element's modes
-      const int* p1row = p1s + lt * K;
-      const int* m1row = m1s + lt * K;
-      const int* nrow = nks + lt * K;
-      const int pb = __ldg(m.plus_ptr + e), pe = __ldg(m.plus_ptr + e + 1);
-      for (int p = pb; p < pe; ++p) {
-        const int lp = p1row[__ldg(m.plus_mode + p)];
-        if (lp != void_idx) cfma(D, cpl[p], ldc<TC>(y + static_cast<size_t>(lp) * n2 + e));
-      }
-      const int mb = __ldg(m.minus_ptr + e), me = __ldg(m.minus_ptr + e + 1);
-      for (int p = mb; p < me; ++p) {
-        const int k = __ldg(m.minus_mode + p);
-        const int lm = m1row[k];
-        if (lm != void_idx) {
-          const TC nk = static_cast<TC>(nrow[k]);
-          const C cm = cmi[p];
-          cfma(D, cx<TC>(nk * cm.x, nk * cm.y), ldc<TC>(y + static_cast<size_t>(lm) * n2 + e));
-        }
-      }
-      local += epilogue<TC>(st, static_cast<size_t>(l0) * n2 + i, D, dt, cur);
+      finish(lt, e, i, cx<TC>(-acc.y, acc.x), pre);
     }
-    __syncthreads();
   }
-  if (st.kind == EPI_DP7) dp7_finish(st, local, static_cast<long long>(nh) * n2);
+  __syncthreads();
+  return local;
+}
+
+template <typename TC, typename TB>
+__global__ void __launch_bounds__(256) k_rhs_diag(const DiagSet ds, const Stage st) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double dt;
+  int cur;
+  if (!stage_prologue(st, dt, cur)) return;
+  const TB* __restrict__ y = stage_input<TB>(st, cur);
+  double local = 0.0;
+  for (int t = blockIdx.x; t < ds.n_tiles; t += gridDim.x) {
+    const DiagTile td = ds.tiles[t];
+    const DiagInst* I = ds.inst + td.inst;
+    if (I->h_real)
+      local += diag_tile<TC, TB, true>(I, td, st, y, dt, cur, smem_raw);
+    else
+      local += diag_tile<TC, TB, false>(I, td, st, y, dt, cur, smem_raw);
+  }
+  if (st.kind == EPI_DP7) dp7_finish(st, local, ds.total);
 }
 
 // ------------------------------------------------------------------ RHS, general V
@@ -641,45 +833,37 @@ int rhs_block_size(const RhsModel& m, int path) {
   return 128;
 }
 
-// ADOs per tile of the diagonal-coupling kernel: about four elements per thread.
-int rhs_tile(const RhsModel& m, int block) { return std::max(1, (4 * block) / std::max(1, m.n2)); }
-
 int rhs_grid_size(const RhsModel& m, int path, int block, int n_sm) {
-  if (path != PATH_DIAG) {
-    const int per_sm = 4;
-    return static_cast<int>(std::min<long long>(m.n_hrchy, static_cast<long long>(n_sm) * per_sm * 4));
-  }
-  const int tile = m.tile > 0 ? m.tile : rhs_tile(m, block);
-  const long long tiles = (static_cast<long long>(m.n_hrchy) + tile - 1) / tile;
-  const long long cap = static_cast<long long>(n_sm) * (2048 / block);
-  return static_cast<int>(std::max<long long>(1, std::min(tiles, cap)));
+  (void)path;
+  (void)block;
+  const int per_sm = 4;
+  return static_cast<int>(std::min<long long>(m.n_hrchy, static_cast<long long>(n_sm) * per_sm * 4));
 }
 
 size_t rhs_smem_bytes(const RhsModel& m, int path, bool mixed) {
   const size_t cb = mixed ? sizeof(float2) : sizeof(double2);
   if (path == PATH_GENERAL) return 5 * cb * m.n2;
   if (path == PATH_LIOU) return 4 * cb * m.n2;
-  const size_t tile = m.tile > 0 ? m.tile : 1;
-  return cb * m.n2 * (1 + tile) + 3 * sizeof(int) * tile * m.K;
+  return 0;
+}
+
+size_t diag_tile_smem(int n2, int K, int tile, bool mixed) {
+  const size_t cb = mixed ? sizeof(float2) : sizeof(double2);
+  return cb * static_cast<size_t>(n2) * (1 + tile) + 3 * sizeof(int) * static_cast<size_t>(tile) * K;
 }
 
 template <typename TC, typename TB>
-static cudaError_t launch_typed(const RhsModel& m, const Stage& st, int path, int grid, int block, cudaStream_t s) {
+static cudaError_t launch_typed(const RhsModel& m, const DiagSet* ds, const Stage& st, int path, int grid, int block,
+                                cudaStream_t s) {
   const size_t smem = rhs_smem_bytes(m, path, std::is_same<TC, float>::value);
   if (path == PATH_DIAG) {
-    if (smem > 48 * 1024) {
-      cudaError_t e = m.h_real ? cudaFuncSetAttribute(k_rhs_diag<TC, TB, true>,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                      static_cast<int>(smem))
-                               : cudaFuncSetAttribute(k_rhs_diag<TC, TB, false>,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                      static_cast<int>(smem));
+    const size_t dsm = ds->smem;
+    if (dsm > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(k_rhs_diag<TC, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(dsm));
       if (e != cudaSuccess) return e;
     }
-    if (m.h_real)
-      k_rhs_diag<TC, TB, true><<<grid, block, smem, s>>>(m, st);
-    else
-      k_rhs_diag<TC, TB, false><<<grid, block, smem, s>>>(m, st);
+    k_rhs_diag<TC, TB><<<grid, block, dsm, s>>>(*ds, st);
   } else if (path == PATH_GENERAL) {
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(k_rhs_general<TC, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -699,11 +883,12 @@ static cudaError_t launch_typed(const RhsModel& m, const Stage& st, int path, in
   return cudaGetLastError();
 }
 
-cudaError_t launch_rhs(const RhsModel& m, const Stage& st, int path, bool mixed, bool in_double, int grid,
-                       int block, cudaStream_t s) {
-  if (!mixed) return launch_typed<double, double2>(m, st, path, grid, block, s);
-  if (in_double) return launch_typed<float, double2>(m, st, path, grid, block, s);
-  return launch_typed<float, float2>(m, st, path, grid, block, s);
+cudaError_t launch_rhs(const RhsModel& m, const DiagSet* ds, const Stage& st, int path, bool mixed, bool in_double,
+                       int grid, int block, cudaStream_t s) {
+  if (path == PATH_DIAG && !ds) return cudaErrorInvalidValue;
+  if (!mixed) return launch_typed<double, double2>(m, ds, st, path, grid, block, s);
+  if (in_double) return launch_typed<float, double2>(m, ds, st, path, grid, block, s);
+  return launch_typed<float, float2>(m, ds, st, path, grid, block, s);
 }
 
 // ------------------------------------------------------------------ hierarchy on the device

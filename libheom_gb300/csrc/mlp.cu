@@ -1,0 +1,545 @@
+// Learned terminator: a small MLP that predicts the truncated tier N+1 of the
+// hierarchy from tier-N ADOs, trained and evaluated with the kernels below.
+//
+// Network: x (d_in) -> Linear(h) -> GELU -> Linear(h) -> GELU -> Linear(d_out).
+// Weights are kept as FP32 masters (Adam) and BF16 copies (forward /
+// backward-data / inference); every product accumulates in FP32.
+//
+// Terminator use: for a tier-N ADO rho_n and mode k, the input is
+// [Re rho_n / s, Im rho_n / s, onehot(k), Re A / s, Im A / s] with
+// s = max_e |rho_n[e]| (the hierarchy is linear, so the map is learned on the
+// unit-scale problem) and A the adiabatic estimate of rho_{n+1_k}; the
+// output, times s, is the predicted rho_{n+1_k}.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "heomgb.h"
+#include "heomgb_impl.cuh"
+
+namespace heomgb {
+void set_error_message(const std::string& msg);
+}
+
+using namespace heomgb;
+
+namespace {
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+
+// Y[b, o] = act(sum_i X[b, i] * W[o, i] + bias[o]); PRE keeps the
+// pre-activation for the backward pass.  16x16 output tiles, K staged in 32s.
+template <bool GELU_ACT>
+__global__ void k_linear_fwd(const float* __restrict__ X, const __nv_bfloat16* __restrict__ W,
+                             const float* __restrict__ bias, float* __restrict__ Y, float* __restrict__ PRE, int B,
+                             int din, int dout) {
+  __shared__ float xs[16][33];
+  __shared__ float ws[16][33];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int b = blockIdx.y * 16 + ty, o = blockIdx.x * 16 + tx;
+  float acc = 0.f;
+  for (int k0 = 0; k0 < din; k0 += 32) {
+    for (int t = threadIdx.x; t < 16 * 32; t += 256) {
+      const int r = t / 32, c = t % 32;
+      const int gb = blockIdx.y * 16 + r, go = blockIdx.x * 16 + r, gk = k0 + c;
+      xs[r][c] = (gb < B && gk < din) ? X[static_cast<size_t>(gb) * din + gk] : 0.f;
+      ws[r][c] = (go < dout && gk < din) ? __bfloat162float(W[static_cast<size_t>(go) * din + gk]) : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int c = 0; c < 32; ++c) acc = fmaf(xs[ty][c], ws[tx][c], acc);
+    __syncthreads();
+  }
+  if (b < B && o < dout) {
+    const float z = acc + bias[o];
+    if (PRE) PRE[static_cast<size_t>(b) * dout + o] = z;
+    Y[static_cast<size_t>(b) * dout + o] = GELU_ACT ? gelu(z) : z;
+  }
+}
+
+// dX[b, i] = sum_o dZ[b, o] * W[o, i]
+__global__ void k_linear_bwd_data(const float* __restrict__ dZ, const __nv_bfloat16* __restrict__ W,
+                                  float* __restrict__ dX, int B, int din, int dout) {
+  __shared__ float zs[16][33];
+  __shared__ float ws[32][17];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int b = blockIdx.y * 16 + ty, i = blockIdx.x * 16 + tx;
+  float acc = 0.f;
+  for (int o0 = 0; o0 < dout; o0 += 32) {
+    for (int t = threadIdx.x; t < 16 * 32; t += 256) {
+      const int r = t / 32, c = t % 32;
+      const int gb = blockIdx.y * 16 + r, go = o0 + c;
+      zs[r][c] = (gb < B && go < dout) ? dZ[static_cast<size_t>(gb) * dout + go] : 0.f;
+      const int wo = o0 + t / 16, wi = blockIdx.x * 16 + t % 16;
+      ws[t / 16][t % 16] = (wo < dout && wi < din) ? __bfloat162float(W[static_cast<size_t>(wo) * din + wi]) : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int c = 0; c < 32; ++c) acc = fmaf(zs[ty][c], ws[c][tx], acc);
+    __syncthreads();
+  }
+  if (b < B && i < din) dX[static_cast<size_t>(b) * din + i] = acc;
+}
+
+// dW[o, i] = sum_b dZ[b, o] * X[b, i]; db[o] = sum_b dZ[b, o]
+__global__ void k_linear_bwd_weight(const float* __restrict__ dZ, const float* __restrict__ X, float* __restrict__ dW,
+                                    float* __restrict__ db, int B, int din, int dout) {
+  __shared__ float zs[32][17];
+  __shared__ float xs[32][17];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int o = blockIdx.y * 16 + ty, i = blockIdx.x * 16 + tx;
+  float acc = 0.f, accb = 0.f;
+  for (int b0 = 0; b0 < B; b0 += 32) {
+    for (int t = threadIdx.x; t < 32 * 16; t += 256) {
+      const int r = t / 16, c = t % 16;
+      const int gb = b0 + r;
+      const int go = blockIdx.y * 16 + c, gi = blockIdx.x * 16 + c;
+      zs[r][c] = (gb < B && go < dout) ? dZ[static_cast<size_t>(gb) * dout + go] : 0.f;
+      xs[r][c] = (gb < B && gi < din) ? X[static_cast<size_t>(gb) * din + gi] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int r = 0; r < 32; ++r) {
+      acc = fmaf(zs[r][ty], xs[r][tx], acc);
+      accb += zs[r][ty];
+    }
+    __syncthreads();
+  }
+  if (o < dout && i < din) dW[static_cast<size_t>(o) * din + i] = acc;
+  if (db && blockIdx.x == 0 && tx == 0 && o < dout) db[o] = accb;
+}
+
+__global__ void k_gelu_bwd(float* __restrict__ dY, const float* __restrict__ PRE, long long n) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    dY[i] *= gelu_grad(PRE[i]);
+}
+
+// Mean-squared error and its gradient d/dY of mean((Y-T)^2); per-CTA partial
+// losses are summed on the host.
+__global__ void k_mse(const float* __restrict__ Y, const float* __restrict__ T, float* __restrict__ dY,
+                      float* __restrict__ part, long long n) {
+  __shared__ float red[256];
+  float s = 0.f;
+  const float scale = 2.0f / static_cast<float>(n);
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const float d = Y[i] - T[i];
+    s += d * d;
+    dY[i] = scale * d;
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// Adam on the FP32 masters, then refresh the BF16 copies.
+__global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                       __nv_bfloat16* __restrict__ wb, long long n, float lr, float b1, float b2, float eps, float c1,
+                       float c2) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    wb[i] = __float2bfloat16(wi);
+  }
+}
+
+__global__ void k_to_bf16(const float* __restrict__ w, __nv_bfloat16* __restrict__ wb, long long n) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    wb[i] = __float2bfloat16(w[i]);
+}
+
+void ckm(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int grid_for(long long n) { return static_cast<int>(std::max<long long>(1, std::min<long long>((n + 255) / 256, 1024))); }
+
+}  // namespace
+
+struct heomgb_mlp {
+  int din = 0, h = 0, dout = 0;
+  long long n_params = 0;
+  // offsets into the packed parameter vector: W1, b1, W2, b2, W3, b3
+  long long off[6] = {0, 0, 0, 0, 0, 0};
+  float* w = nullptr;           // FP32 masters
+  __nv_bfloat16* wb = nullptr;  // BF16 copies
+  float* g = nullptr;           // gradients
+  float* m = nullptr;           // Adam moments
+  float* v = nullptr;
+  long long step = 0;
+  int cap = 0;                  // batch capacity of the activation buffers
+  float *a1 = nullptr, *p1 = nullptr, *a2 = nullptr, *p2 = nullptr, *y = nullptr, *d = nullptr, *d2 = nullptr;
+  float* part = nullptr;
+  cudaStream_t s = nullptr;
+  void free_acts() {
+    for (float* p : {a1, p1, a2, p2, y, d, d2, part}) cudaFree(p);
+    a1 = p1 = a2 = p2 = y = d = d2 = part = nullptr;
+    cap = 0;
+  }
+  void ensure(int B) {
+    if (B <= cap) return;
+    free_acts();
+    const size_t hb = sizeof(float) * static_cast<size_t>(B) * h;
+    ckm(cudaMalloc(&a1, hb), "mlp alloc");
+    ckm(cudaMalloc(&p1, hb), "mlp alloc");
+    ckm(cudaMalloc(&a2, hb), "mlp alloc");
+    ckm(cudaMalloc(&p2, hb), "mlp alloc");
+    ckm(cudaMalloc(&y, sizeof(float) * static_cast<size_t>(B) * dout), "mlp alloc");
+    ckm(cudaMalloc(&d, hb + sizeof(float) * static_cast<size_t>(B) * (dout + din)), "mlp alloc");
+    ckm(cudaMalloc(&d2, hb), "mlp alloc");
+    ckm(cudaMalloc(&part, sizeof(float) * 1024), "mlp alloc");
+    cap = B;
+  }
+  ~heomgb_mlp() {
+    free_acts();
+    for (void* p : {static_cast<void*>(w), static_cast<void*>(wb), static_cast<void*>(g), static_cast<void*>(m),
+                    static_cast<void*>(v)})
+      cudaFree(p);
+    if (s) cudaStreamDestroy(s);
+  }
+};
+
+namespace {
+
+template <class F>
+heomgb_status mguard(F&& f) {
+  try {
+    f();
+    return HEOMGB_OK;
+  } catch (const std::invalid_argument& e) {
+    set_error_message(e.what());
+    return HEOMGB_ERR_INVALID_ARGUMENT;
+  } catch (const std::exception& e) {
+    set_error_message(e.what());
+    return HEOMGB_ERR_CUDA;
+  }
+}
+
+void linear_fwd(heomgb_mlp* M, const float* X, int layer, float* Y, float* PRE, int B, bool act) {
+  const int din = layer == 0 ? M->din : M->h, dout = layer == 2 ? M->dout : M->h;
+  const dim3 grid((dout + 15) / 16, (B + 15) / 16);
+  const __nv_bfloat16* W = M->wb + M->off[2 * layer];
+  const float* bias = M->w + M->off[2 * layer + 1];
+  if (act)
+    k_linear_fwd<true><<<grid, 256, 0, M->s>>>(X, W, bias, Y, PRE, B, din, dout);
+  else
+    k_linear_fwd<false><<<grid, 256, 0, M->s>>>(X, W, bias, Y, PRE, B, din, dout);
+  ++g_launches;
+  ckm(cudaGetLastError(), "linear fwd");
+}
+
+void forward(heomgb_mlp* M, const float* X, float* out, int B) {
+  M->ensure(B);
+  linear_fwd(M, X, 0, M->a1, M->p1, B, true);
+  linear_fwd(M, M->a1, 1, M->a2, M->p2, B, true);
+  linear_fwd(M, M->a2, 2, out, nullptr, B, false);
+}
+
+// Forward + backward: fills M->g with d(mean sq. error)/d(params); returns the loss.
+float backward(heomgb_mlp* M, const float* X, const float* T, int B) {
+  M->ensure(B);
+  forward(M, X, M->y, B);
+  const long long ny = static_cast<long long>(B) * M->dout;
+  const int gm = grid_for(ny);
+  float* dy = M->d;                                   // B*dout
+  k_mse<<<gm, 256, 0, M->s>>>(M->y, T, dy, M->part, ny);
+  ++g_launches;
+  // layer 3
+  {
+    const dim3 gw((M->h + 15) / 16, (M->dout + 15) / 16);
+    k_linear_bwd_weight<<<gw, 256, 0, M->s>>>(dy, M->a2, M->g + M->off[4], M->g + M->off[5], B, M->h, M->dout);
+    const dim3 gd((M->h + 15) / 16, (B + 15) / 16);
+    k_linear_bwd_data<<<gd, 256, 0, M->s>>>(dy, M->wb + M->off[4], M->d2, B, M->h, M->dout);
+    const long long nh = static_cast<long long>(B) * M->h;
+    k_gelu_bwd<<<grid_for(nh), 256, 0, M->s>>>(M->d2, M->p2, nh);
+    g_launches += 3;
+  }
+  // layer 2
+  float* dh1 = M->d + ny;  // B*h scratch after dy
+  {
+    const dim3 gw((M->h + 15) / 16, (M->h + 15) / 16);
+    k_linear_bwd_weight<<<gw, 256, 0, M->s>>>(M->d2, M->a1, M->g + M->off[2], M->g + M->off[3], B, M->h, M->h);
+    const dim3 gd((M->h + 15) / 16, (B + 15) / 16);
+    k_linear_bwd_data<<<gd, 256, 0, M->s>>>(M->d2, M->wb + M->off[2], dh1, B, M->h, M->h);
+    const long long nh = static_cast<long long>(B) * M->h;
+    k_gelu_bwd<<<grid_for(nh), 256, 0, M->s>>>(dh1, M->p1, nh);
+    g_launches += 3;
+  }
+  // layer 1
+  {
+    const dim3 gw((M->din + 15) / 16, (M->h + 15) / 16);
+    k_linear_bwd_weight<<<gw, 256, 0, M->s>>>(dh1, X, M->g + M->off[0], M->g + M->off[1], B, M->din, M->h);
+    ++g_launches;
+  }
+  ckm(cudaGetLastError(), "mlp backward");
+  std::vector<float> part(gm);
+  ckm(cudaMemcpyAsync(part.data(), M->part, sizeof(float) * gm, cudaMemcpyDeviceToHost, M->s), "loss copy");
+  ckm(cudaStreamSynchronize(M->s), "mlp sync");
+  double loss = 0;
+  for (float p : part) loss += p;
+  return static_cast<float>(loss / static_cast<double>(ny));
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ terminator inference
+// Inputs of the rows (tier-N ADO j, mode k), d_in = 4 n2 + K:
+//   [Re rho/s, Im rho/s (2 n2), onehot(k) (K), Re A/s, Im A/s (2 n2)]
+// with s = max_e |rho_l[e]| and A the adiabatic estimate of rho_{n+1_k}
+// (the tier-(N+1) equation with its own time derivative and the commutator
+// with H dropped; V_u diagonal):
+//   A[ab] = (n_k+1) (-i s_k (v_a - v_b) + a_k (v_a + v_b)) rho_ab / (ngamma_l + gamma_kk).
+// CTA j stages rho_l (l = first+j), reduces s, and writes the K rows.
+template <typename TB>
+__global__ void k_term_pack(const TermInput in, const TermModel tm, int first, int n_tier, float* __restrict__ X,
+                            float* __restrict__ scale) {
+  __shared__ float red[128];
+  const int j = blockIdx.x;
+  if (j >= n_tier) return;
+  const int n = tm.n, n2 = n * n, K = tm.K;
+  const int cur = in.ctl ? in.ctl->cur : 0;
+  const void* ysel = in.y_sel == 1 ? in.yb[cur] : (in.y_sel == 2 ? in.yb[1 - cur] : in.y_fixed);
+  const int l = first + j;
+  const TB* yl = static_cast<const TB*>(ysel) + static_cast<size_t>(l) * n2;
+  float mx = 0.f;
+  for (int e = threadIdx.x; e < n2; e += blockDim.x) {
+    const float re = static_cast<float>(yl[e].x), im = static_cast<float>(yl[e].y);
+    mx = fmaxf(mx, re * re + im * im);
+  }
+  red[threadIdx.x] = mx;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + o]);
+    __syncthreads();
+  }
+  const float s = sqrtf(red[0]) + 1e-30f;
+  const float inv = 1.0f / s;
+  if (threadIdx.x == 0) scale[j] = s;
+  const int din = 4 * n2 + K;
+  const double2 gl = tm.ngd[l];
+  for (int k = 0; k < K; ++k) {
+    float* row = X + (static_cast<size_t>(j) * K + k) * din;
+    int u = 0;
+    while (u + 1 < tm.U && tm.bath_ptr[u + 1] <= k) ++u;
+    const double2 sk = tm.s[k], ak = tm.a[k], gk = tm.gdiag[k];
+    const double nk1 = static_cast<double>(tm.nidx[static_cast<size_t>(l) * K + k]) + 1.0;
+    // 1 / (ngamma_l + gamma_kk)
+    const double dr = gl.x + gk.x, di = gl.y + gk.y, dd = dr * dr + di * di;
+    const double ir = dd > 0.0 ? dr / dd : 0.0, ii = dd > 0.0 ? -di / dd : 0.0;
+    for (int f = threadIdx.x; f < din; f += blockDim.x) {
+      float v;
+      if (f < 2 * n2) {
+        const int e = f < n2 ? f : f - n2;
+        v = static_cast<float>(f < n2 ? yl[e].x : yl[e].y) * inv;
+      } else if (f < 2 * n2 + K) {
+        v = (f - 2 * n2 == k) ? 1.f : 0.f;
+      } else {
+        const int g2 = f - 2 * n2 - K;
+        const int e = g2 < n2 ? g2 : g2 - n2;
+        const int a = e / n, b = e - a * n;
+        const double2 va = tm.V[static_cast<size_t>(u) * n2 + a * n + a], vb = tm.V[static_cast<size_t>(u) * n2 + b * n + b];
+        // c = -i s_k (va - vb) + a_k (va + vb)
+        const double mr = va.x - vb.x, mi = va.y - vb.y, pr = va.x + vb.x, pi = va.y + vb.y;
+        const double t1r = sk.x * mr - sk.y * mi, t1i = sk.x * mi + sk.y * mr;  // s_k (va - vb)
+        const double cr = t1i + (ak.x * pr - ak.y * pi), ci = -t1r + (ak.x * pi + ak.y * pr);
+        const double yr = static_cast<double>(yl[e].x), yi = static_cast<double>(yl[e].y);
+        const double zr = cr * yr - ci * yi, zi = cr * yi + ci * yr;     // c * rho_ab
+        const double wr = zr * ir - zi * ii, wi = zr * ii + zi * ir;     // / (ngamma + gamma_k)
+        v = static_cast<float>((g2 < n2 ? wr : wi) * nk1) * inv;
+      }
+      row[f] = v;
+    }
+  }
+}
+
+// P[(j*K+k)*n2 + e] = s_j * (Y[row][e] + i Y[row][n2+e])
+__global__ void k_term_scatter(const float* __restrict__ Y, const float* __restrict__ scale, int n_tier, int n2,
+                               int K, float2* __restrict__ P) {
+  const long long total = static_cast<long long>(n_tier) * K * n2;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long r = i / n2;
+    const int e = static_cast<int>(i - r * n2);
+    const float s = scale[r / K];
+    const float* yr = Y + r * (2 * n2);
+    P[i] = make_float2(s * yr[e], s * yr[n2 + e]);
+  }
+}
+
+namespace heomgb {
+
+cudaError_t term_enqueue(heomgb_mlp* M, const TermBuffers& tb, const TermModel& tm, const TermInput& in,
+                         bool y_float, cudaStream_t s) {
+  if (tb.n_tier <= 0) return cudaSuccess;
+  const int R = tb.n_tier * tb.K;
+  if (y_float)
+    k_term_pack<float2><<<tb.n_tier, 128, 0, s>>>(in, tm, tb.first, tb.n_tier, tb.X, tb.scale);
+  else
+    k_term_pack<double2><<<tb.n_tier, 128, 0, s>>>(in, tm, tb.first, tb.n_tier, tb.X, tb.scale);
+  const int din = M->din, h = M->h, dout = M->dout;
+  const dim3 g1((h + 15) / 16, (R + 15) / 16), g3((dout + 15) / 16, (R + 15) / 16);
+  k_linear_fwd<true><<<g1, 256, 0, s>>>(tb.X, M->wb + M->off[0], M->w + M->off[1], tb.A1, nullptr, R, din, h);
+  k_linear_fwd<true><<<g1, 256, 0, s>>>(tb.A1, M->wb + M->off[2], M->w + M->off[3], tb.A2, nullptr, R, h, h);
+  k_linear_fwd<false><<<g3, 256, 0, s>>>(tb.A2, M->wb + M->off[4], M->w + M->off[5], tb.Y, nullptr, R, h, dout);
+  const long long tot = static_cast<long long>(R) * tb.n2;
+  k_term_scatter<<<grid_for(tot), 256, 0, s>>>(tb.Y, tb.scale, tb.n_tier, tb.n2, tb.K, tb.P);
+  g_launches += 5;
+  return cudaGetLastError();
+}
+
+void mlp_dims(const heomgb_mlp* M, int* din, int* h, int* dout) {
+  *din = M->din;
+  *h = M->h;
+  *dout = M->dout;
+}
+
+}  // namespace heomgb
+
+extern "C" {
+
+heomgb_status heomgb_mlp_create(int d_in, int d_hidden, int d_out, unsigned long long seed, heomgb_mlp** out) {
+  return mguard([&] {
+    if (!out || d_in < 1 || d_hidden < 1 || d_out < 1) throw std::invalid_argument("bad MLP sizes");
+    auto M = std::make_unique<heomgb_mlp>();
+    M->din = d_in;
+    M->h = d_hidden;
+    M->dout = d_out;
+    const long long sz[6] = {static_cast<long long>(d_hidden) * d_in, d_hidden,
+                             static_cast<long long>(d_hidden) * d_hidden, d_hidden,
+                             static_cast<long long>(d_out) * d_hidden, d_out};
+    long long o = 0;
+    for (int i = 0; i < 6; ++i) {
+      M->off[i] = o;
+      o += sz[i];
+    }
+    M->n_params = o;
+    // He-uniform initialisation from a 64-bit LCG (deterministic per seed); zero biases.
+    std::vector<float> w(o, 0.f);
+    unsigned long long st = seed * 6364136223846793005ULL + 1442695040888963407ULL;
+    auto uni = [&]() {
+      st = st * 6364136223846793005ULL + 1442695040888963407ULL;
+      return static_cast<float>((st >> 11) * (1.0 / 9007199254740992.0)) * 2.f - 1.f;
+    };
+    const int fan_in[3] = {d_in, d_hidden, d_hidden};
+    for (int l = 0; l < 3; ++l) {
+      const float a = std::sqrt(6.0f / static_cast<float>(fan_in[l])) * (l == 2 ? 0.5f : 1.0f);
+      for (long long i = 0; i < sz[2 * l]; ++i) w[M->off[2 * l] + i] = a * uni();
+    }
+    ckm(cudaStreamCreateWithFlags(&M->s, cudaStreamNonBlocking), "stream");
+    const size_t fb = sizeof(float) * o;
+    ckm(cudaMalloc(&M->w, fb), "mlp alloc");
+    ckm(cudaMalloc(&M->g, fb), "mlp alloc");
+    ckm(cudaMalloc(&M->m, fb), "mlp alloc");
+    ckm(cudaMalloc(&M->v, fb), "mlp alloc");
+    ckm(cudaMalloc(&M->wb, sizeof(__nv_bfloat16) * o), "mlp alloc");
+    ckm(cudaMemcpyAsync(M->w, w.data(), fb, cudaMemcpyHostToDevice, M->s), "mlp init");
+    ckm(cudaMemsetAsync(M->g, 0, fb, M->s), "memset");
+    ckm(cudaMemsetAsync(M->m, 0, fb, M->s), "memset");
+    ckm(cudaMemsetAsync(M->v, 0, fb, M->s), "memset");
+    k_to_bf16<<<grid_for(o), 256, 0, M->s>>>(M->w, M->wb, o);
+    ++g_launches;
+    ckm(cudaStreamSynchronize(M->s), "mlp init sync");
+    *out = M.release();
+  });
+}
+
+heomgb_status heomgb_mlp_destroy(heomgb_mlp* M) {
+  if (M) {
+    cudaStreamSynchronize(M->s);
+    delete M;
+  }
+  return HEOMGB_OK;
+}
+
+heomgb_status heomgb_mlp_sizes(const heomgb_mlp* M, int* d_in, int* d_hidden, int* d_out, long long* n_params) {
+  return mguard([&] {
+    if (!M) throw std::invalid_argument("null mlp");
+    if (d_in) *d_in = M->din;
+    if (d_hidden) *d_hidden = M->h;
+    if (d_out) *d_out = M->dout;
+    if (n_params) *n_params = M->n_params;
+  });
+}
+
+heomgb_status heomgb_mlp_get_params(heomgb_mlp* M, float* params) {
+  return mguard([&] {
+    if (!M || !params) throw std::invalid_argument("null argument");
+    ckm(cudaMemcpyAsync(params, M->w, sizeof(float) * M->n_params, cudaMemcpyDeviceToHost, M->s), "copy");
+    ckm(cudaStreamSynchronize(M->s), "sync");
+  });
+}
+
+heomgb_status heomgb_mlp_set_params(heomgb_mlp* M, const float* params) {
+  return mguard([&] {
+    if (!M || !params) throw std::invalid_argument("null argument");
+    ckm(cudaMemcpyAsync(M->w, params, sizeof(float) * M->n_params, cudaMemcpyHostToDevice, M->s), "copy");
+    k_to_bf16<<<grid_for(M->n_params), 256, 0, M->s>>>(M->w, M->wb, M->n_params);
+    ++g_launches;
+    ckm(cudaStreamSynchronize(M->s), "sync");
+  });
+}
+
+heomgb_status heomgb_mlp_forward(heomgb_mlp* M, const float* x_dev, float* y_dev, int batch) {
+  return mguard([&] {
+    if (!M || !x_dev || !y_dev || batch < 1) throw std::invalid_argument("bad argument");
+    forward(M, x_dev, y_dev, batch);
+    ckm(cudaStreamSynchronize(M->s), "sync");
+  });
+}
+
+heomgb_status heomgb_mlp_gradients(heomgb_mlp* M, const float* x_dev, const float* t_dev, int batch,
+                                   float* grad_host, float* loss) {
+  return mguard([&] {
+    if (!M || !x_dev || !t_dev || batch < 1) throw std::invalid_argument("bad argument");
+    const float l = backward(M, x_dev, t_dev, batch);
+    if (loss) *loss = l;
+    if (grad_host) {
+      ckm(cudaMemcpyAsync(grad_host, M->g, sizeof(float) * M->n_params, cudaMemcpyDeviceToHost, M->s), "copy");
+      ckm(cudaStreamSynchronize(M->s), "sync");
+    }
+  });
+}
+
+heomgb_status heomgb_mlp_train_step(heomgb_mlp* M, const float* x_dev, const float* t_dev, int batch, float lr,
+                                    float* loss) {
+  return mguard([&] {
+    if (!M || !x_dev || !t_dev || batch < 1) throw std::invalid_argument("bad argument");
+    const float l = backward(M, x_dev, t_dev, batch);
+    M->step += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - std::pow(b1, static_cast<float>(M->step));
+    const float c2 = 1.f - std::pow(b2, static_cast<float>(M->step));
+    k_adam<<<grid_for(M->n_params), 256, 0, M->s>>>(M->w, M->g, M->m, M->v, M->wb, M->n_params, lr, b1, b2, 1e-8f,
+                                                    c1, c2);
+    ++g_launches;
+    ckm(cudaGetLastError(), "adam");
+    ckm(cudaStreamSynchronize(M->s), "sync");
+    if (loss) *loss = l;
+  });
+}
+
+}  // extern "C"

@@ -251,7 +251,7 @@ class qme_solver:
         self._need()
         if not (isinstance(rho, np.ndarray) and rho.dtype == np.complex128 and rho.flags.c_contiguous):
             raise TypeError("rho must be a C-contiguous complex128 array")
-        if rho.size != self.qme.main_size():
+        if rho.size != self.main_size():
             raise ValueError("rho must hold main_size() elements")
         t = np.ascontiguousarray(t_list, dtype=np.float64)
         cb = CALLBACK(lambda tt, _u: callback(tt)) if callback else CALLBACK()
@@ -267,6 +267,17 @@ class qme_solver:
         kw = _kwargs(kwargs)
         check(self._lib.heomgb_qme_solver_solve_device(self._h, ctypes.c_void_p(int(rho_ptr)), t.ctypes.data,
                                                        len(t), cb, None, ctypes.byref(kw)))
+
+    def main_size(self) -> int:
+        v = ctypes.c_longlong()
+        check(self._lib.heomgb_qme_solver_main_size(self._h, ctypes.byref(v)))
+        return v.value
+
+    def tuning(self) -> dict:
+        """Tile shape the autotuner picked (diagonal-coupling kernel)."""
+        b, e, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(self._lib.heomgb_qme_solver_tuning(self._h, ctypes.byref(b), ctypes.byref(e), ctypes.byref(t)))
+        return dict(block=b.value, elems_per_thread=e.value, n_tiles=t.value)
 
     def stats(self) -> dict:
         r, a, c = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
@@ -291,6 +302,31 @@ class qme_solver:
             self.close()
         except Exception:
             pass
+
+
+class batch_solver(qme_solver):
+    """Many uneven instances stepped together, every stage in one launch.
+
+    The state is the concatenation of the models' states in order
+    (`offsets()` gives each instance's first element)."""
+
+    def __init__(self, qmes, solver: solver_base, engine=None):
+        qmes = list(qmes)
+        if not qmes:
+            raise ValueError("empty batch")
+        for q in qmes:
+            q._need()
+        self.qme, self.qmes, self.solver = qmes[0], qmes, solver
+        self._lib = qmes[0]._lib
+        self._h = ctypes.c_void_p()
+        arr = (ctypes.c_void_p * len(qmes))(*[q._h.value for q in qmes])
+        check(self._lib.heomgb_batch_solver_create(arr, len(qmes), solver._h, ctypes.byref(self._h)))
+        for q in qmes:
+            q._solvers.add(self)
+
+    def offsets(self):
+        sizes = [q.main_size() for q in self.qmes]
+        return np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
 
 
 def from_params(p, form: str = "hilb", precision: str = "fp64", stream=None) -> heom:

@@ -215,6 +215,22 @@ size_t heomgb_errnrm1_scratch(long long n);
 heomgb_status heomgb_errnrm1_device(const void* e, const void* x1, const void* x2, double atol, double rtol,
                                     long long n, double* scratch, double* result, void* cuda_stream);
 
+/* ---- allocation-free variant ------------------------------------------------ */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (code inside a framework that owns the device heap, or a plugin whose
+ * allocations are audited) but do own device memory for the outputs: builds
+ * the hierarchy tables hs.n, hs.ptr_p1, hs.ptr_m1 (as heomgb_qme_get_hrchy
+ * returns them) into caller-owned device buffers of C(n_dim+max_depth,
+ * max_depth)*n_dim, (C+1)*n_dim and (C+1)*n_dim ints, enqueued on cuda_stream
+ * (NULL: legacy stream); *n_hrchy receives C.  Its scratch (a binomial table)
+ * lives in a fixed device array, so n_dim + max_depth + 2 may not exceed
+ * HEOMGB_NOALLOC_MAX_BINOM_DIM (HEOMGB_ERR_CAPACITY otherwise).  The first call
+ * on a device looks up that array's device address; make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race. */
+#define HEOMGB_NOALLOC_MAX_BINOM_DIM 96
+heomgb_status heomgb_hrchy_build_noalloc(int n_dim, int max_depth, int* n_dev, int* ptr_p1_dev, int* ptr_m1_dev,
+                                         int* n_hrchy, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -85,6 +85,8 @@ SIGNATURES = {
     "heomgb_mlp_train_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                              ctypes.c_float, ctypes.POINTER(ctypes.c_float)]),
     "heomgb_qme_set_terminator": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "heomgb_hrchy_build_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_void_p, c_int_p, ctypes.c_void_p]),
     "heomgb_errnrm1_scratch": (ctypes.c_size_t, [ctypes.c_longlong]),
     "heomgb_errnrm1_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
                                              ctypes.c_double, ctypes.c_longlong, ctypes.c_void_p, c_double_p,

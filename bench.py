@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--form", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 comparison run (profiling)")
+    ap.add_argument("--t-final", type=float, default=None,
+                    help="propagate to this time instead of the workload's (short profiling runs)")
     return ap.parse_args()
 
 
@@ -155,6 +157,7 @@ class Workload:
         self.batched = len(self.ps) > 1
         self.n_hrchy = sum(p.n_hrchy() for p in self.ps)
         self.N = sum(p.n_hrchy() * p.n_level ** 2 for p in self.ps)
+        self.promoted = 0
 
     def rho0(self):
         return np.concatenate([p.rho0_ground().ravel() for p in self.ps])
@@ -162,6 +165,14 @@ class Workload:
     def make(self, precision, stream):
         import libheom_gb300 as lh
         qmes = [lh.from_params(p, precision=precision, stream=stream) for p in self.ps]
+        if self.batched:
+            # models that the range guard keeps in FP64 form a second
+            # sub-batch; group them so each sub-batch is contiguous on the device
+            order = sorted(range(len(qmes)), key=lambda i: qmes[i].get_precision()["effective"] == "fp64")
+            self.ps = [self.ps[i] for i in order]
+            qmes = [qmes[i] for i in order]
+            self.promoted = sum(q.get_precision()["effective"] == "fp64" for q in qmes) if precision == "mixed" \
+                else self.promoted
         solver = lh.SOLVERS[self.wl["solver"]]()
         qs = lh.batch_solver(qmes, solver) if self.batched else lh.qme_solver(qmes[0], solver)
         return qmes, qs
@@ -170,9 +181,10 @@ class Workload:
         """Accuracy of `got` against the FP64 result `ref` (flat concatenated states).
 
         rho0: max |delta rho_0| (system density matrix) over the instances whose
-        FP64 rho_0 stays bounded (|rho_0| <= 2; some seeded batch instances are
-        unstable under the reference's algorithm itself); all_ados: the same
-        over every ADO element of those instances."""
+        FP64 rho_0 stays physical (|rho_0| <= 1 + 1e-3; some seeded batch
+        instances diverge under the reference's algorithm itself); all_ados_rel:
+        max over those instances of max |delta rho| / max |rho| taken over all
+        of an instance's ADOs."""
         off = 0
         e0, ea, stable = 0.0, 0.0, 0
         for p in self.ps:
@@ -180,12 +192,12 @@ class Workload:
             size = p.n_hrchy() * n2
             r, g = ref[off:off + size], got[off:off + size]
             off += size
-            if not np.all(np.isfinite(r)) or np.abs(r[:n2]).max() > 2.0:
+            if not np.all(np.isfinite(r)) or np.abs(r[:n2]).max() > 1.0 + 1e-3:
                 continue
             stable += 1
             e0 = max(e0, float(np.abs(g[:n2] - r[:n2]).max()))
-            ea = max(ea, float(np.abs(g - r).max()))
-        return {"rho0": e0, "all_ados": ea, "instances_checked": stable, "instances": len(self.ps)}
+            ea = max(ea, float(np.abs(g - r).max() / (np.abs(r).max() + 1e-300)))
+        return {"rho0": e0, "all_ados_rel": ea, "instances_checked": stable, "instances": len(self.ps)}
 
     def flops_per_launch(self):
         from libheom_gb300 import roofline
@@ -198,7 +210,8 @@ class Workload:
         counts = [p.n_hrchy() for p in self.ps]
         return {"instances": len(self.ps), "n_level": sorted({p.n_level for p in self.ps}),
                 "max_depth": [min(p.max_depth for p in self.ps), max(p.max_depth for p in self.ps)],
-                "n_hrchy_total": self.n_hrchy, "n_hrchy_per_instance": [min(counts), max(counts)]}
+                "n_hrchy_total": self.n_hrchy, "n_hrchy_per_instance": [min(counts), max(counts)],
+                "kept_fp64_by_range_guard": self.promoted}
 
 
 def cpu_baseline(w: Workload):
@@ -268,6 +281,8 @@ def run_ours(args):
     rho0 = torch.from_numpy(w.rho0()).to(dev)
     rho = torch.empty_like(rho0)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    if args.t_final is not None:
+        wl["t_final"] = args.t_final
     t_list = [0.0, wl["t_final"]]
     per_rhs = 7 if wl["solver"] == "rkdp" else 4
 
@@ -301,12 +316,24 @@ def run_ours(args):
         tm64 = qs64.timing()
         avg64 = 1e-3 * tm64["busy_ms"] / max(tm64["kernels"], 1)
         fl64 = w.flops_per_launch() / avg64 / 1e12
-        plain = {"value": st64["rhs"] * w.n_hrchy / (ms64 / 1e3), "ms_per_step": ms64,
+        plain = {"value": st64["ado_updates"] / (ms64 / 1e3), "ms_per_step": ms64,
                  "attempts": st64["attempts"], "avg_stage_kernel_us": 1e6 * avg64, "tuning": qs64.tuning(),
                  "roofline": {"bound": "fp64 pipe", "achieved": fl64, "peak": fma_peaks[0], "unit": "TFLOP/s",
                               "frac": fl64 / fma_peaks[0], "peak_source": "measured (heomgb_probe_fma_peaks)"}}
         qs64.close()
         del qs64, q64
+
+    def alg_bytes_of(tm, st):
+        """Algorithmic bytes of the stage kernels of one solve (per sub-batch
+        precision), counted over the stage launches that did work (right-hand
+        sides evaluated); launches of a captured graph replayed after the
+        interval ended return at once and move no data."""
+        parts = tm.get("parts") or [dict(tm, precision="mixed" if mixed else "fp64", elements=N, rhs=st["rhs"])]
+        tot = 0.0
+        for part in parts:
+            bpe, per_unit = roofline.bytes_per_element(wl["solver"], part["precision"] == "mixed")
+            tot += bpe * part["elements"] / per_unit * part["rhs"]
+        return tot
 
     for _ in range(args.warmup):
         with torch.cuda.stream(stream):
@@ -319,7 +346,7 @@ def run_ours(args):
     sampler = ClockSampler(local)
     sampler.start()
     launches0 = lh.launch_count()
-    times, rhs, busy, kernels = [], 0, 0.0, 0
+    times, rhs, upd, busy, kernels, alg_bytes = [], 0, 0, 0.0, 0, 0.0
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()  # the state would stay L2-resident otherwise: flush between steps
@@ -332,15 +359,17 @@ def run_ours(args):
         st = qs.stats()
         tm = qs.timing()
         rhs += st["rhs"]
+        upd += st["ado_updates"]
         busy += tm["busy_ms"]
         kernels += tm["kernels"]
+        alg_bytes += alg_bytes_of(tm, st)
     launches = lh.launch_count() - launches0
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     clocks = sampler.stop()
     # units of all ranks over the slowest rank's time (no collective touches the state)
-    value, total_s = job_throughput(rhs * w.n_hrchy, float(sum(times)) / 1e3)
+    value, total_s = job_throughput(upd, float(sum(times)) / 1e3)
     total_ms = 1e3 * total_s
 
     # end to end through the public API with host buffers (pinned), copies inside
@@ -352,14 +381,14 @@ def run_ours(args):
         t0 = time.perf_counter()
         qs.solve(arr, t_list, None, wl["kw"])
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    e2e_rhs = qs.stats()["rhs"]
-    e2e = {"value": e2e_rhs * w.n_hrchy * world / (statistics.median(e2e_ms) / 1e3), "unit": "ADO-updates/s",
+    e2e_upd = qs.stats()["ado_updates"]
+    e2e = {"value": e2e_upd * world / (statistics.median(e2e_ms) / 1e3), "unit": "ADO-updates/s",
            "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N}
 
     # roofline of the fused stage kernel
-    bpe, launches_per_unit = roofline.bytes_per_element(wl["solver"], mixed)
-    alg_bytes_per_launch = bpe * N / launches_per_unit
-    avg_launch_s = (busy / 1e3) / max(kernels, 1)
+    # per working launch: busy time / right-hand sides evaluated
+    alg_bytes_per_launch = alg_bytes / max(rhs, 1)
+    avg_launch_s = (busy / 1e3) / max(rhs, 1)
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes_per_launch / avg_launch_s / 1e9
     flops = w.flops_per_launch()
@@ -369,8 +398,9 @@ def run_ours(args):
             "alg_bytes_per_launch": alg_bytes_per_launch, "avg_launch_us": avg_launch_s * 1e6,
             "alg_flops_per_launch": flops, "achieved_tflops": flops / avg_launch_s / 1e12,
             "fma_peaks_tflops": {"fp64": fma_peaks[0], "fp32": fma_peaks[1]},
-            "note": "avg launch time = CUDA-event time of graph replays / kernels replayed (includes "
-                    "intra-graph gaps); the 7-site state is L2-resident within a propagation"}
+            "note": "avg launch time = CUDA-event time of the graph replays / stages evaluated (one stage "
+                    "over the whole state; intra-graph gaps and the no-op launches replayed after an interval "
+                    "ends are included in the time, not in the count)"}
     line = {"metric": "ADO-updates/s", "value": value, "unit": "ADO-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

@@ -92,6 +92,17 @@ heomgb_status heomgb_qme_set_noise(heomgb_qme* q, int u, const double* V, int le
                                    const double* phi_0, const double* sigma, const double* S, const double* A,
                                    const double* s_delta);
 heomgb_status heomgb_qme_set_precision(heomgb_qme* q, heomgb_precision p);
+/* Precision after set_param (no reference counterpart: the reference has one
+ * compile-time precision).  A MIXED request runs with FP64 arithmetic
+ * (effective = FP64) when the bath expansion makes FP32 arithmetic unsafe.
+ * With growth_log10 = max_k N log10((|s_k| + |a_k|) / |Re gamma_kk|) (how far
+ * deep ADOs outgrow rho_0 under the integer normalisation) and cancel_log10 =
+ * max_u log10(sum_k |s_k| / |sum_k s_k|) (how strongly one bath's coefficients
+ * cancel, e.g. a Matsubara frequency near the Drude pole), that is when
+ * cancel_log10 > 0.8, or growth_log10 > 7.5, or both growth_log10 > 2 and
+ * cancel_log10 > 0.2. */
+heomgb_status heomgb_qme_get_precision(const heomgb_qme* q, int* requested, int* effective, double* growth_log10,
+                                       double* cancel_log10);
 /* Run the model's CUDA work on this stream (a cudaStream_t); NULL restores the
  * library's own stream.  Must precede heomgb_qme_solver_create to affect it. */
 heomgb_status heomgb_qme_set_stream(heomgb_qme* q, void* cuda_stream);
@@ -142,9 +153,13 @@ heomgb_status heomgb_batch_solver_create(heomgb_qme* const* qmes, int count, heo
 /* Elements of the state a solve of qs expects (main_size(), summed over a batch). */
 heomgb_status heomgb_qme_solver_main_size(const heomgb_qme_solver* qs, long long* size);
 /* Tile shape the autotuner picked for the diagonal-coupling kernel: CTA size,
- * elements per thread and number of tiles (0 for the other kernels). */
+ * elements per thread, number of tiles and the kernel variant's minimum
+ * resident CTAs (1, or 3 for the mixed form's register-capped variant); 0 for
+ * the other kernels.  The environment variable
+ * HEOMGB_TILE=<64|128|256>x<1..8>[x<1|3>] (e.g. "128x2") pins the shape
+ * instead of searching, for reproducible profiles. */
 heomgb_status heomgb_qme_solver_tuning(const heomgb_qme_solver* qs, int* block, int* elems_per_thread,
-                                       int* n_tiles);
+                                       int* n_tiles, int* min_blocks);
 
 /* qme_solver::solve(rho, t_list, n_t, callback, kwargs) -- qme_solver.h:44-52,
  * solver_base.h:64-79.  rho: host array of main_size() complex, updated in
@@ -180,9 +195,12 @@ heomgb_status heomgb_probe_fma_peaks(double* fp64_tflops, double* fp32_tflops);
  * As a terminator of a model with n_level n and n_dim K it maps
  * [Re rho_n / s, Im rho_n / s, onehot(k), Re A / s, Im A / s] (4n^2 + K) of a
  * tier-N ADO, with A the adiabatic estimate of rho_{n+1_k} (its own time
- * derivative and the commutator with H dropped) and
- * s = max_e |rho_n[e]|, to rho_{n+1_k} / s (2n^2), i.e. it stands in for the
- * ADOs that plain truncation drops (ptr_p1 == ptr_void). */
+ * derivative and the commutator with H dropped) and s = max_e |rho_n[e]|, to
+ * an elementwise gain (2n^2 outputs: Re C_e, z_e) with
+ *   C_e = Re C_e - i sign(v_a - v_b) softplus(z_e),
+ *   rho_{n+1_k}[e] ~ C_e rho_n[e] / sigma_k,
+ * i.e. it stands in for the ADOs that plain truncation drops
+ * (ptr_p1 == ptr_void) through a closure term that can only damp. */
 typedef struct heomgb_mlp heomgb_mlp;
 heomgb_status heomgb_mlp_create(int d_in, int d_hidden, int d_out, unsigned long long seed, heomgb_mlp** out);
 heomgb_status heomgb_mlp_destroy(heomgb_mlp* mlp);
@@ -191,7 +209,13 @@ heomgb_status heomgb_mlp_get_params(heomgb_mlp* mlp, float* params);       /* ho
 heomgb_status heomgb_mlp_set_params(heomgb_mlp* mlp, const float* params); /* host, n_params floats */
 /* y = mlp(x) for `batch` rows; x_dev / y_dev are device float arrays. */
 heomgb_status heomgb_mlp_forward(heomgb_mlp* mlp, const float* x_dev, float* y_dev, int batch);
-/* Gradient of mean((mlp(x) - t)^2) with respect to the packed parameters
+/* Loss used by gradients / train_step.  kind 0 (default): mean((mlp(x) - t)^2),
+ * t has d_out floats per row.  kind 1: the terminator's closure loss, with
+ * d_out = 2 n2 and t rows [Re t, Im t, Re r, Im r, sg] (5 n2 floats;
+ * t = rho_{n+1_k}/s, r = rho_n/(s sigma_k), sg = sign(v_a - v_b)): the mean over
+ * rows of sum_e |sg_e| |C_e r_e - t_e|^2 / (sum_e |sg_e| (|t_e|^2 + 1e-2 |r_e|^2) + 1e-6). */
+heomgb_status heomgb_mlp_set_loss(heomgb_mlp* mlp, int kind, int n2);
+/* Gradient of the loss with respect to the packed parameters
  * (grad_host: n_params floats, may be NULL) and the loss; no update. */
 heomgb_status heomgb_mlp_gradients(heomgb_mlp* mlp, const float* x_dev, const float* t_dev, int batch,
                                    float* grad_host, float* loss);

@@ -48,6 +48,7 @@ SIGNATURES = {
                                             ctypes.c_void_p, ctypes.c_void_p]),
     "heomgb_qme_set_precision": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "heomgb_qme_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "heomgb_qme_get_precision": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_double_p, c_double_p]),
     "heomgb_qme_set_param": (ctypes.c_int, [ctypes.c_void_p]),
     "heomgb_qme_get_n_hrchy": (ctypes.c_int, [ctypes.c_void_p, c_int_p]),
     "heomgb_qme_get_n_dim": (ctypes.c_int, [ctypes.c_void_p, c_int_p]),
@@ -64,7 +65,7 @@ SIGNATURES = {
     "heomgb_batch_solver_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                   ctypes.POINTER(ctypes.c_void_p)]),
     "heomgb_qme_solver_main_size": (ctypes.c_int, [ctypes.c_void_p, c_ll_p]),
-    "heomgb_qme_solver_tuning": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p]),
+    "heomgb_qme_solver_tuning": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p]),
     "heomgb_qme_solver_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                                CALLBACK, ctypes.c_void_p, ctypes.POINTER(Kwargs)]),
     "heomgb_qme_solver_solve_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -79,6 +80,7 @@ SIGNATURES = {
     "heomgb_mlp_sizes": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p, c_ll_p]),
     "heomgb_mlp_get_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "heomgb_mlp_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "heomgb_mlp_set_loss": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "heomgb_mlp_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "heomgb_mlp_gradients": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                             ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),

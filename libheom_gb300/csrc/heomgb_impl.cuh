@@ -150,6 +150,7 @@ struct DiagSet {
   int n_tiles;
   long long total;          // elements over all instances
   size_t smem;              // dynamic shared memory of the largest tile
+  int min_blocks;           // 1, or 3: the mixed kernel compiled for 3 resident 256-thread CTAs (<= 80 registers)
 };
 
 // Launchers (kernels.cu).  `mixed` selects FP32 bulk arithmetic; `in_double`
@@ -202,6 +203,7 @@ struct TermModel {
   const double2* gdiag = nullptr; // K: gamma_kk
   const double2* s = nullptr;     // K
   const double2* a = nullptr;     // K
+  const double2* sigma = nullptr; // K
   const double2* V = nullptr;     // U*n2
   const int* bath_ptr = nullptr;  // U+1
 };

@@ -6,6 +6,7 @@
 // n x n matrix is contiguous, row-major, at offset l*n^2; element e = a*n+b.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 #include <type_traits>
 
@@ -147,8 +148,11 @@ __device__ void dp_control(DpCtl* c, double sumsq, long long n) {
 // FP64 form (TC = double): the reference's operation order (rk4.h:40-65,
 // lsrk4.h:32-47, rkdp.h:111-153).  Mixed form (TC = float): stage inputs of
 // the next right-hand side are formed in FP32 from the bulk copy of the
-// state; the state, the RK4 accumulator, the LSRK4 buffer, the candidate
-// state rho + sum_j B_j k_j and the error vector e = sum_j E_j k_j are FP64.
+// state; the state, the RK4 accumulator, the LSRK4 buffer and the
+// Dormand-Prince candidate state rho + sum_j B_j k_j are accumulated in FP64
+// (the k_j themselves are FP32).  The error vector e = sum_j E_j k_j only
+// steers the step size: it is combined from the FP32 k_j in FP32, while the
+// error norm's sum over elements and the step controller are FP64.
 struct EpiPre {
   double2 a;   // FP64 partial result (accumulator, base state, partial sum)
   double2 b;   // FP64 base state (RK4 in FP64 form, LSRK4)
@@ -196,13 +200,13 @@ __device__ __forceinline__ EpiPre epi_pre(const Stage& st, size_t g, int cur) {
             y.y = fmaf(c, kj.y, y.y);
           }
           p.f = y;
-        } else {  // candidate state rho + sum_j B_j k_j in FP64
+        } else {  // candidate state rho + sum_j B_j k_j, accumulated in FP64
           double2 y = __ldcs(st.S[cur] + g);
           for (int j = 0; j < 5; ++j) {
             const double c = c_dpA[6][j];
             const float2 kj = __ldcs(static_cast<const float2*>(st.K[j]) + g);
-            y.x += c * static_cast<double>(kj.x);
-            y.y += c * static_cast<double>(kj.y);
+            y.x = fma(c, static_cast<double>(kj.x), y.x);
+            y.y = fma(c, static_cast<double>(kj.y), y.y);
           }
           p.a = y;
         }
@@ -219,14 +223,25 @@ __device__ __forceinline__ EpiPre epi_pre(const Stage& st, size_t g, int cur) {
       break;
     }
     case EPI_DP7: {
-      const double2 k0 = ld_bulk_cs<TC>(st.K[0], g);
-      double2 e = make_double2(c_dpE[0] * k0.x, c_dpE[0] * k0.y);
-      for (int j = 1; j < 6; ++j) {
-        const double2 kj = ld_bulk_cs<TC>(st.K[j], g);
-        e.x += c_dpE[j] * kj.x;
-        e.y += c_dpE[j] * kj.y;
+      if constexpr (MIX) {  // FP32 stage vectors: combine them in FP32
+        float2 e = make_float2(0.f, 0.f);
+        for (int j = 0; j < 6; ++j) {
+          const float c = static_cast<float>(c_dpE[j]);
+          const float2 kj = __ldcs(static_cast<const float2*>(st.K[j]) + g);
+          e.x = fmaf(c, kj.x, e.x);
+          e.y = fmaf(c, kj.y, e.y);
+        }
+        p.f = e;
+      } else {
+        const double2 k0 = ld_bulk_cs<TC>(st.K[0], g);
+        double2 e = make_double2(c_dpE[0] * k0.x, c_dpE[0] * k0.y);
+        for (int j = 1; j < 6; ++j) {
+          const double2 kj = ld_bulk_cs<TC>(st.K[j], g);
+          e.x += c_dpE[j] * kj.x;
+          e.y += c_dpE[j] * kj.y;
+        }
+        p.a = e;
       }
-      p.a = e;
       if constexpr (MIX) {  // scale from the bulk copies of both states
         const float2 x1 = static_cast<const float2*>(st.Yb[1 - cur])[g];
         const float2 x2 = static_cast<const float2*>(st.Yb[cur])[g];
@@ -311,8 +326,8 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
           static_cast<float2*>(st.Ynext)[g] = make_float2(fmaf(c, k.x, p.f.x), fmaf(c, k.y, p.f.y));
         } else {
           double2 y = p.a;
-          y.x += c_dpA[6][5] * static_cast<double>(k.x);
-          y.y += c_dpA[6][5] * static_cast<double>(k.y);
+          y.x = fma(c_dpA[6][5], static_cast<double>(k.x), y.x);
+          y.y = fma(c_dpA[6][5], static_cast<double>(k.y), y.y);
           __stcs(st.S[1 - cur] + g, y);
           static_cast<float2*>(st.Yb[1 - cur])[g] = make_float2(static_cast<float>(y.x), static_cast<float>(y.y));
         }
@@ -331,22 +346,19 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
       return 0.0;
     }
     case EPI_DP7: {  // e = sum_j E_j k_j ; scaled squared error (linalg_engine_cuda.cu:102-146)
-      double2 k7;
-      if constexpr (MIX) {
+      if constexpr (MIX) {  // per-element term in FP32; the sum over elements is FP64
         const float fdt = static_cast<float>(dt);
-        k7 = make_double2(static_cast<double>(-fdt * Dc.x), static_cast<double>(-fdt * Dc.y));
-      } else {
-        k7 = make_double2(-dt * D.x, -dt * D.y);
-      }
-      double2 e = p.a;
-      e.x += c_dpE[6] * k7.x;
-      e.y += c_dpE[6] * k7.y;
-      const double e2 = e.x * e.x + e.y * e.y;
-      if constexpr (MIX) {
+        const float c = static_cast<float>(c_dpE[6]);
+        const float ex = fmaf(c, -fdt * Dc.x, p.f.x), ey = fmaf(c, -fdt * Dc.y, p.f.y);
         const float s = static_cast<float>(st.ctl->atol) +
                         static_cast<float>(st.ctl->rtol) * sqrtf(static_cast<float>(p.m));
-        return e2 * static_cast<double>(1.0f / (s * s));
+        return static_cast<double>((ex * ex + ey * ey) / (s * s));
       } else {
+        const double2 k7 = make_double2(-dt * D.x, -dt * D.y);
+        double2 e = p.a;
+        e.x += c_dpE[6] * k7.x;
+        e.y += c_dpE[6] * k7.y;
+        const double e2 = e.x * e.x + e.y * e.y;
         const double s = st.ctl->atol + st.ctl->rtol * sqrt(p.m);
         return e2 / (s * s);
       }
@@ -442,9 +454,11 @@ __device__ __forceinline__ double diag_tile(const DiagInst* __restrict__ I, cons
   using C = cx_t<TC>;
   const int n = I->n, n2 = I->n2, K = I->K, void_idx = I->nh, tile = I->tile;
   const long long base = I->elem_off;
+  const bool mt4 = (n & 3) == 0 && n >= 8;
   C* Hs = reinterpret_cast<C*>(smem_raw);        // n2
   C* yt = Hs + n2;                                // tile*n2
-  int* p1s = reinterpret_cast<int*>(yt + static_cast<size_t>(tile) * n2);  // tile*K
+  C* Ds = yt + static_cast<size_t>(tile) * n2;    // tile*n2 commutators (micro-tiled path only)
+  int* p1s = reinterpret_cast<int*>(Ds + (mt4 ? static_cast<size_t>(tile) * n2 : 0));  // tile*K
   int* m1s = p1s + tile * K;
   int* nks = m1s + tile * K;
   const C* __restrict__ Hg = pick<TC>(I->H, I->H_f);
@@ -525,9 +539,12 @@ __device__ __forceinline__ double diag_tile(const DiagInst* __restrict__ I, cons
     }
     local += epi_post<TC>(st, static_cast<size_t>(base + static_cast<long long>(l0) * n2 + i), D, dt, cur, pre);
   };
-  if ((n & 3) == 0 && n >= 8) {
+  if (mt4) {
     // 1 x 4 register micro-tile: a thread owns 4 consecutive elements of a
     // row, so every H / rho value read from shared memory feeds 4 products.
+    // The commutators go to shared memory; the bath terms and the epilogue
+    // then run one element per thread, so a warp's neighbour and state
+    // accesses cover consecutive elements (coalesced).
     const int ng = ne >> 2;
     for (int q = threadIdx.x; q < ng; q += blockDim.x) {
       const int i0 = q << 2;
@@ -573,12 +590,14 @@ __device__ __forceinline__ double diag_tile(const DiagInst* __restrict__ I, cons
           acc[j].y -= neg[j].y;
         }
       }
-#pragma unroll 1
-      for (int j = 0; j < 4; ++j) {
-        const EpiPre pre =
-            epi_pre<TC>(st, static_cast<size_t>(base + static_cast<long long>(l0) * n2 + i0 + j), cur);
-        finish(lt, e0 + j, i0 + j, cx<TC>(-acc[j].y, acc[j].x), pre);
-      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) Ds[i0 + j] = cx<TC>(-acc[j].y, acc[j].x);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < ne; i += blockDim.x) {
+      const int lt = i / n2;
+      const EpiPre pre = epi_pre<TC>(st, static_cast<size_t>(base + static_cast<long long>(l0) * n2 + i), cur);
+      finish(lt, i - lt * n2, i, Ds[i], pre);
     }
   } else {
     for (int i = threadIdx.x; i < ne; i += blockDim.x) {
@@ -616,8 +635,8 @@ __device__ __forceinline__ double diag_tile(const DiagInst* __restrict__ I, cons
   return local;
 }
 
-template <typename TC, typename TB>
-__global__ void __launch_bounds__(256) k_rhs_diag(const DiagSet ds, const Stage st) {
+template <typename TC, typename TB, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_rhs_diag(const DiagSet ds, const Stage st) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double dt;
   int cur;
@@ -849,7 +868,9 @@ size_t rhs_smem_bytes(const RhsModel& m, int path, bool mixed) {
 
 size_t diag_tile_smem(int n2, int K, int tile, bool mixed) {
   const size_t cb = mixed ? sizeof(float2) : sizeof(double2);
-  return cb * static_cast<size_t>(n2) * (1 + tile) + 3 * sizeof(int) * static_cast<size_t>(tile) * K;
+  const int n = static_cast<int>(std::lround(std::sqrt(static_cast<double>(n2))));
+  const bool mt4 = (n & 3) == 0 && n >= 8;  // diag_tile's micro-tiled path stages its commutators
+  return cb * static_cast<size_t>(n2) * (1 + tile * (mt4 ? 2 : 1)) + 3 * sizeof(int) * static_cast<size_t>(tile) * K;
 }
 
 template <typename TC, typename TB>
@@ -858,12 +879,17 @@ static cudaError_t launch_typed(const RhsModel& m, const DiagSet* ds, const Stag
   const size_t smem = rhs_smem_bytes(m, path, std::is_same<TC, float>::value);
   if (path == PATH_DIAG) {
     const size_t dsm = ds->smem;
+    // the register-capped variant exists for the FP32 arithmetic only (the
+    // FP64 kernel would spill at 80 registers)
+    auto kern = k_rhs_diag<TC, TB, 1>;
+    if constexpr (std::is_same<TC, float>::value) {
+      if (ds->min_blocks == 3) kern = k_rhs_diag<TC, TB, 3>;
+    }
     if (dsm > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(k_rhs_diag<TC, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(dsm));
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dsm));
       if (e != cudaSuccess) return e;
     }
-    k_rhs_diag<TC, TB><<<grid, block, dsm, s>>>(*ds, st);
+    kern<<<grid, block, dsm, s>>>(*ds, st);
   } else if (path == PATH_GENERAL) {
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(k_rhs_general<TC, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize,

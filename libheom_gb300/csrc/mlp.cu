@@ -9,7 +9,8 @@
 // [Re rho_n / s, Im rho_n / s, onehot(k), Re A / s, Im A / s] with
 // s = max_e |rho_n[e]| (the hierarchy is linear, so the map is learned on the
 // unit-scale problem) and A the adiabatic estimate of rho_{n+1_k}; the
-// output, times s, is the predicted rho_{n+1_k}.
+// output is an elementwise complex gain C with rho_{n+1_k} ~ C rho_n / sigma_k,
+// constrained so that the closure term damps (k_term_scatter).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -149,6 +150,54 @@ __global__ void k_mse(const float* __restrict__ Y, const float* __restrict__ T, 
   if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
+// Closure ("gain") loss of the terminator head.  Per row the network gives
+// (Re C_e, z_e) for the n2 elements; C_e = Re C_e - i sg_e softplus(z_e) with
+// sg_e = sign(v_a - v_b) of the mode's bath (0 where the +1 term vanishes).
+// Target row: [Re t, Im t, Re r, Im r, sg] (5 n2 floats), t = rho_{n+1_k}/s,
+// r = rho_n/(s sigma_k).  Loss = mean over rows of
+//   sum_e m_e |C_e r_e - t_e|^2 / (sum_e m_e (|t_e|^2 + 1e-2 |r_e|^2) + 1e-6),
+// m_e = |sg_e|: each row's error relative to its own size.
+__device__ __forceinline__ float softplus_f(float z) { return fmaxf(z, 0.f) + log1pf(expf(-fabsf(z))); }
+__device__ __forceinline__ float sigmoid_f(float z) { return 1.f / (1.f + expf(-z)); }
+
+__global__ void k_gain_loss(const float* __restrict__ Y, const float* __restrict__ T, float* __restrict__ dY,
+                            float* __restrict__ part, int B, int n2) {
+  __shared__ float red[256];
+  float acc = 0.f;
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x) {
+    const float* y = Y + static_cast<size_t>(b) * 2 * n2;
+    const float* t = T + static_cast<size_t>(b) * 5 * n2;
+    float* dy = dY + static_cast<size_t>(b) * 2 * n2;
+    float den = 1e-6f;
+    for (int e = 0; e < n2; ++e) {
+      const float m = fabsf(t[4 * n2 + e]);
+      den += m * (t[e] * t[e] + t[n2 + e] * t[n2 + e] + 1e-2f * (t[2 * n2 + e] * t[2 * n2 + e] +
+                                                                 t[3 * n2 + e] * t[3 * n2 + e]));
+    }
+    const float w = 2.f / (static_cast<float>(B) * den);
+    float num = 0.f;
+    for (int e = 0; e < n2; ++e) {
+      const float sg = t[4 * n2 + e], m = fabsf(sg);
+      const float cr = y[e], ci = -sg * softplus_f(y[n2 + e]);
+      const float rr = t[2 * n2 + e], ri = t[3 * n2 + e];
+      const float dr = cr * rr - ci * ri - t[e], di = cr * ri + ci * rr - t[n2 + e];
+      num += m * (dr * dr + di * di);
+      // conj(d) r = (dr rr + di ri) + i (dr ri - di rr)
+      const float re = dr * rr + di * ri, im = dr * ri - di * rr;
+      dy[e] = w * m * re;
+      dy[n2 + e] = w * m * sg * sigmoid_f(y[n2 + e]) * im;
+    }
+    acc += num / den;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
 // Adam on the FP32 masters, then refresh the BF16 copies.
 __global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
                        __nv_bfloat16* __restrict__ wb, long long n, float lr, float b1, float b2, float eps, float c1,
@@ -191,6 +240,8 @@ struct heomgb_mlp {
   float* m = nullptr;           // Adam moments
   float* v = nullptr;
   long long step = 0;
+  int loss_kind = 0;            // 0: mean squared error; 1: terminator closure loss (k_gain_loss)
+  int loss_n2 = 0;              // elements per ADO for loss_kind 1 (d_out = 2 loss_n2)
   int cap = 0;                  // batch capacity of the activation buffers
   float *a1 = nullptr, *p1 = nullptr, *a2 = nullptr, *p2 = nullptr, *y = nullptr, *d = nullptr, *d2 = nullptr;
   float* part = nullptr;
@@ -266,7 +317,11 @@ float backward(heomgb_mlp* M, const float* X, const float* T, int B) {
   const long long ny = static_cast<long long>(B) * M->dout;
   const int gm = grid_for(ny);
   float* dy = M->d;                                   // B*dout
-  k_mse<<<gm, 256, 0, M->s>>>(M->y, T, dy, M->part, ny);
+  const int gl = M->loss_kind == 1 ? grid_for(B) : gm;
+  if (M->loss_kind == 1)
+    k_gain_loss<<<gl, 256, 0, M->s>>>(M->y, T, dy, M->part, B, M->loss_n2);
+  else
+    k_mse<<<gm, 256, 0, M->s>>>(M->y, T, dy, M->part, ny);
   ++g_launches;
   // layer 3
   {
@@ -296,12 +351,12 @@ float backward(heomgb_mlp* M, const float* X, const float* T, int B) {
     ++g_launches;
   }
   ckm(cudaGetLastError(), "mlp backward");
-  std::vector<float> part(gm);
-  ckm(cudaMemcpyAsync(part.data(), M->part, sizeof(float) * gm, cudaMemcpyDeviceToHost, M->s), "loss copy");
+  std::vector<float> part(gl);
+  ckm(cudaMemcpyAsync(part.data(), M->part, sizeof(float) * gl, cudaMemcpyDeviceToHost, M->s), "loss copy");
   ckm(cudaStreamSynchronize(M->s), "mlp sync");
   double loss = 0;
   for (float p : part) loss += p;
-  return static_cast<float>(loss / static_cast<double>(ny));
+  return static_cast<float>(loss / static_cast<double>(M->loss_kind == 1 ? B : ny));
 }
 
 }  // namespace
@@ -376,17 +431,42 @@ __global__ void k_term_pack(const TermInput in, const TermModel tm, int first, i
   }
 }
 
-// P[(j*K+k)*n2 + e] = s_j * (Y[row][e] + i Y[row][n2+e])
-__global__ void k_term_scatter(const float* __restrict__ Y, const float* __restrict__ scale, int n_tier, int n2,
-                               int K, float2* __restrict__ P) {
+// Gain head: row (j, k) gives C_e = Y[e] - i sg_e softplus(Y[n2+e]) with
+// sg_e = sign(Re(v_a - v_b)) for the bath of mode k, and the prediction
+//   P[(j*K+k)*n2 + e] = C_e rho_l[e] / sigma_k   (rho_l[e] = s_j X[row][e] + i s_j X[row][n2+e]).
+// Its +1 term in the right-hand side, i (v_a - v_b) sigma_k P_e, is then
+// i (v_a - v_b) C_e rho_l[e]: a rate whose real part is -|v_a - v_b| softplus <= 0,
+// so the closure only damps (or shifts the frequency of) the tier-N ADOs.
+__global__ void k_term_scatter(const float* __restrict__ Y, const float* __restrict__ X,
+                               const float* __restrict__ scale, const TermModel tm, int n_tier, int din,
+                               float2* __restrict__ P) {
+  const int n = tm.n, n2 = n * n, K = tm.K;
   const long long total = static_cast<long long>(n_tier) * K * n2;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
        i += static_cast<long long>(gridDim.x) * blockDim.x) {
     const long long r = i / n2;
     const int e = static_cast<int>(i - r * n2);
+    const int k = static_cast<int>(r % K);
+    int u = 0;
+    while (u + 1 < tm.U && tm.bath_ptr[u + 1] <= k) ++u;
+    const int a = e / n, b = e - a * n;
+    const double dv = tm.V[static_cast<size_t>(u) * n2 + a * n + a].x - tm.V[static_cast<size_t>(u) * n2 + b * n + b].x;
+    if (dv == 0.0) {
+      P[i] = make_float2(0.f, 0.f);
+      continue;
+    }
+    const float sg = dv > 0.0 ? 1.f : -1.f;
     const float s = scale[r / K];
     const float* yr = Y + r * (2 * n2);
-    P[i] = make_float2(s * yr[e], s * yr[n2 + e]);
+    const float* xr = X + r * din;
+    const float cr = yr[e], ci = -sg * softplus_f(yr[n2 + e]);
+    const float rr = s * xr[e], ri = s * xr[n2 + e];
+    // (C rho) / sigma_k
+    const float pr = cr * rr - ci * ri, pi = cr * ri + ci * rr;
+    const double2 sk = tm.sigma[k];
+    const double dd = sk.x * sk.x + sk.y * sk.y;
+    const float ir = static_cast<float>(sk.x / dd), ii = static_cast<float>(-sk.y / dd);
+    P[i] = make_float2(pr * ir - pi * ii, pr * ii + pi * ir);
   }
 }
 
@@ -406,7 +486,7 @@ cudaError_t term_enqueue(heomgb_mlp* M, const TermBuffers& tb, const TermModel& 
   k_linear_fwd<true><<<g1, 256, 0, s>>>(tb.A1, M->wb + M->off[2], M->w + M->off[3], tb.A2, nullptr, R, h, h);
   k_linear_fwd<false><<<g3, 256, 0, s>>>(tb.A2, M->wb + M->off[4], M->w + M->off[5], tb.Y, nullptr, R, h, dout);
   const long long tot = static_cast<long long>(R) * tb.n2;
-  k_term_scatter<<<grid_for(tot), 256, 0, s>>>(tb.Y, tb.scale, tb.n_tier, tb.n2, tb.K, tb.P);
+  k_term_scatter<<<grid_for(tot), 256, 0, s>>>(tb.Y, tb.X, tb.scale, tm, tb.n_tier, din, tb.P);
   g_launches += 5;
   return cudaGetLastError();
 }
@@ -500,6 +580,16 @@ heomgb_status heomgb_mlp_set_params(heomgb_mlp* M, const float* params) {
     k_to_bf16<<<grid_for(M->n_params), 256, 0, M->s>>>(M->w, M->wb, M->n_params);
     ++g_launches;
     ckm(cudaStreamSynchronize(M->s), "sync");
+  });
+}
+
+heomgb_status heomgb_mlp_set_loss(heomgb_mlp* M, int kind, int n2) {
+  return mguard([&] {
+    if (!M) throw std::invalid_argument("null mlp");
+    if (kind != 0 && kind != 1) throw std::invalid_argument("unknown loss kind");
+    if (kind == 1 && (n2 < 1 || M->dout != 2 * n2)) throw std::invalid_argument("closure loss needs d_out = 2 n2");
+    M->loss_kind = kind;
+    M->loss_n2 = kind == 1 ? n2 : 0;
   });
 }
 

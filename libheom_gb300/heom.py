@@ -111,6 +111,18 @@ class heom:
         if not self._h:
             raise RuntimeError("set_param has not been called")
 
+    def get_precision(self) -> dict:
+        """Requested / effective precision and the range-guard inputs
+        (heomgb_qme_get_precision): a MIXED model runs in FP64 when
+        cancel_log10 > 0.8, growth_log10 > 7.5, or both growth_log10 > 2 and
+        cancel_log10 > 0.2."""
+        self._need()
+        r, e, g, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        check(self._lib.heomgb_qme_get_precision(self._h, ctypes.byref(r), ctypes.byref(e), ctypes.byref(g),
+                                                 ctypes.byref(c)))
+        names = {0: "fp64", 1: "mixed"}
+        return dict(requested=names[r.value], effective=names[e.value], growth_log10=g.value, cancel_log10=c.value)
+
     def get_n_hrchy(self) -> int:
         self._need()
         v = ctypes.c_int()
@@ -275,16 +287,18 @@ class qme_solver:
 
     def tuning(self) -> dict:
         """Tile shape the autotuner picked (diagonal-coupling kernel)."""
-        b, e, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        check(self._lib.heomgb_qme_solver_tuning(self._h, ctypes.byref(b), ctypes.byref(e), ctypes.byref(t)))
-        return dict(block=b.value, elems_per_thread=e.value, n_tiles=t.value)
+        b, e, t, m = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(self._lib.heomgb_qme_solver_tuning(self._h, ctypes.byref(b), ctypes.byref(e), ctypes.byref(t),
+                                                 ctypes.byref(m)))
+        return dict(block=b.value, elems_per_thread=e.value, n_tiles=t.value, min_blocks=m.value)
 
     def stats(self) -> dict:
         r, a, c = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
         d = ctypes.c_double()
         check(self._lib.heomgb_qme_solver_stats(self._h, ctypes.byref(r), ctypes.byref(a), ctypes.byref(c),
                                                 ctypes.byref(d)))
-        return dict(rhs=r.value, attempts=a.value, accepted=c.value, dt_save=d.value)
+        nh = sum(q.get_n_hrchy() for q in getattr(self, "qmes", [self.qme]))
+        return dict(rhs=r.value, attempts=a.value, accepted=c.value, dt_save=d.value, ado_updates=r.value * nh)
 
     def timing(self) -> dict:
         """Device time of the last solve inside stage-kernel graph replays."""
@@ -304,18 +318,10 @@ class qme_solver:
             pass
 
 
-class batch_solver(qme_solver):
-    """Many uneven instances stepped together, every stage in one launch.
+class _batch_part(qme_solver):
+    """One C-level batch solver over models that share an effective precision."""
 
-    The state is the concatenation of the models' states in order
-    (`offsets()` gives each instance's first element)."""
-
-    def __init__(self, qmes, solver: solver_base, engine=None):
-        qmes = list(qmes)
-        if not qmes:
-            raise ValueError("empty batch")
-        for q in qmes:
-            q._need()
+    def __init__(self, qmes, solver):
         self.qme, self.qmes, self.solver = qmes[0], qmes, solver
         self._lib = qmes[0]._lib
         self._h = ctypes.c_void_p()
@@ -324,9 +330,120 @@ class batch_solver(qme_solver):
         for q in qmes:
             q._solvers.add(self)
 
+
+class batch_solver:
+    """Many uneven instances stepped together, every stage in one launch.
+
+    The state is the concatenation of the models' states in order
+    (`offsets()` gives each instance's first element).  Models whose effective
+    precision differs (a MIXED request kept in FP64 by the range
+    guard, heomgb_qme_get_precision) run in a second sub-batch; each output
+    interval then steps both sub-batches."""
+
+    def __init__(self, qmes, solver: solver_base, engine=None):
+        qmes = list(qmes)
+        if not qmes:
+            raise ValueError("empty batch")
+        for q in qmes:
+            q._need()
+        self.qmes, self.solver = qmes, solver
+        sizes = [q.main_size() for q in qmes]
+        self._off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        groups = {}
+        for i, q in enumerate(qmes):
+            groups.setdefault(q.get_precision()["effective"], []).append(i)
+        self._parts = []
+        for _, idx in sorted(groups.items()):
+            part = _batch_part([qmes[i] for i in idx], solver)
+            ranges = [(int(self._off[i]), int(self._off[i + 1])) for i in idx]
+            contiguous = all(ranges[j][1] == ranges[j + 1][0] for j in range(len(ranges) - 1))
+            self._parts.append((part, idx, ranges, contiguous))
+
     def offsets(self):
-        sizes = [q.main_size() for q in self.qmes]
-        return np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        return self._off.copy()
+
+    def main_size(self) -> int:
+        return int(self._off[-1])
+
+    def parts(self):
+        """[(instance indices, effective precision)] of the sub-batches."""
+        return [(idx, p.qme.get_precision()["effective"]) for p, idx, _, _ in self._parts]
+
+    def _gather(self, rho, ranges):
+        return np.concatenate([rho[a:b] for a, b in ranges]) if len(ranges) > 1 else rho[ranges[0][0]:ranges[0][1]].copy()
+
+    def _scatter(self, rho, ranges, sub):
+        o = 0
+        for a, b in ranges:
+            rho[a:b] = sub[o:o + b - a]
+            o += b - a
+
+    def solve(self, rho: np.ndarray, t_list, callback=None, kwargs=None) -> None:
+        if not (isinstance(rho, np.ndarray) and rho.dtype == np.complex128 and rho.flags.c_contiguous):
+            raise TypeError("rho must be a C-contiguous complex128 array")
+        if rho.size != self.main_size():
+            raise ValueError("rho must hold main_size() elements")
+        flat = rho.reshape(-1)
+        if len(self._parts) == 1:
+            self._parts[0][0].solve(flat, t_list, callback, kwargs)
+            return
+        t = [float(x) for x in t_list]
+        for i in range(len(t) - 1):
+            if callback:
+                callback(t[i])
+            for part, _, ranges, _ in self._parts:
+                sub = self._gather(flat, ranges)
+                part.solve(sub, [t[i], t[i + 1]], None, kwargs)
+                self._scatter(flat, ranges, sub)
+        if callback and t:
+            callback(t[-1])
+
+    def solve_device(self, rho_ptr: int, t_list, callback=None, kwargs=None) -> None:
+        """rho_ptr: device pointer to the concatenated state (complex128)."""
+        if len(self._parts) == 1:
+            self._parts[0][0].solve_device(rho_ptr, t_list, callback, kwargs)
+            return
+        if not all(c for _, _, _, c in self._parts):
+            raise ValueError("sub-batches must be contiguous in the state for device solves; order the models "
+                             "by effective precision")
+        t = [float(x) for x in t_list]
+        for i in range(len(t) - 1):
+            if callback:
+                callback(t[i])
+            for part, _, ranges, _ in self._parts:
+                part.solve_device(int(rho_ptr) + 16 * ranges[0][0], [t[i], t[i + 1]], None, kwargs)
+        if callback and t:
+            callback(t[-1])
+
+    def stats(self) -> dict:
+        out = dict(rhs=0, attempts=0, accepted=0, ado_updates=0, dt_save=-1.0)
+        for part, idx, _, _ in self._parts:
+            st = part.stats()
+            nh = sum(self.qmes[i].get_n_hrchy() for i in idx)
+            out["rhs"] = max(out["rhs"], st["rhs"])
+            out["attempts"] = max(out["attempts"], st["attempts"])
+            out["accepted"] = max(out["accepted"], st["accepted"])
+            out["ado_updates"] += st["rhs"] * nh
+        return out
+
+    def timing(self) -> dict:
+        """Busy time and stage kernels of the last solve, in total and per sub-batch."""
+        ms, k, parts = 0.0, 0, []
+        for part, idx, ranges, _ in self._parts:
+            t = part.timing()
+            ms += t["busy_ms"]
+            k += t["kernels"]
+            parts.append(dict(t, precision=part.qme.get_precision()["effective"], instances=len(idx),
+                              elements=sum(b - a for a, b in ranges), rhs=part.stats()["rhs"]))
+        return dict(busy_ms=ms, kernels=k, parts=parts)
+
+    def tuning(self) -> dict:
+        return {"parts": [p.tuning() for p, _, _, _ in self._parts]} if len(self._parts) > 1 else \
+            self._parts[0][0].tuning()
+
+    def close(self) -> None:
+        for part, _, _, _ in self._parts:
+            part.close()
 
 
 def from_params(p, form: str = "hilb", precision: str = "fp64", stream=None) -> heom:

@@ -13,6 +13,24 @@ without it one network cannot serve a range of (lambda, beta): measured on
 spin-boson data, the best linear closure of the bare inputs explains under a
 third of the variance.
 
+Output: an elementwise gain C with rho_{n+1_k} ~ C rho_n / sigma_k, whose
+imaginary part is constrained (C = y - i sign(v_a - v_b) softplus(z)) so that
+the closure term only damps the tier-N ADOs.  Unconstrained regressions of
+rho_{n+1_k} (and the adiabatic estimate itself) made the truncated hierarchy
+blow up at low temperature, where the Matsubara coefficients are negative.
+The loss is relative per row, so weak-coupling rows, where plain truncation
+is already accurate, weigh as much as strong-coupling ones.
+
+Applicability and fallback.  A damping-only closure cannot stand in for the
+anti-damping that large negative Matsubara coefficients bring at low
+temperature, so the closure is used (and trained) only where a bath's
+expansion is dominated by its positive terms: cancel_log10 =
+max_u log10(sum_k |s_k| / |sum_k s_k|) <= 0.2, the quantity the mixed form's
+range guard reports (heomgb_qme_get_precision).  Elsewhere the model keeps
+plain truncation.  `propagate` also checks rho_0 at every output time (finite,
+populations in [-0.05, 1.05]) and reruns with plain truncation if the closure
+failed.
+
 Training data: trajectories of the plain method at a deeper hierarchy; since
 the breadth-first ADO order is tier-ascending, the first C(K+N, N) ADOs of a
 deep state are exactly the ADOs of the depth-N model, in the same order.
@@ -51,6 +69,10 @@ class MLP:
         if arr.size != self.n_params:
             raise ValueError("wrong parameter count")
         check(self._lib.heomgb_mlp_set_params(self._h, arr.ctypes.data))
+
+    def set_loss(self, kind: int, n2: int = 0) -> None:
+        """0: mean squared error; 1: the terminator's closure loss (heomgb_mlp_set_loss)."""
+        check(self._lib.heomgb_mlp_set_loss(self._h, kind, n2))
 
     def forward(self, x_dev, y_dev, batch: int) -> None:
         check(self._lib.heomgb_mlp_forward(self._h, ctypes.c_void_p(x_dev), ctypes.c_void_p(y_dev), batch))
@@ -95,7 +117,7 @@ def attach(qme, mlp) -> None:
 
 
 def _mode_constants(p: HeomParams):
-    bath_of, s_k, a_k, g_k = [], [], [], []
+    bath_of, s_k, a_k, g_k, sig = [], [], [], [], []
     for u in range(p.n_noise):
         sv = p.S[u] @ p.phi_0[u]
         av = p.A[u] @ p.phi_0[u]
@@ -104,7 +126,16 @@ def _mode_constants(p: HeomParams):
             s_k.append(sv[k])
             a_k.append(av[k])
             g_k.append(p.gamma[u][k, k])
-    return np.array(bath_of), np.array(s_k), np.array(a_k), np.array(g_k)
+            sig.append(p.sigma[u][k])
+    return np.array(bath_of), np.array(s_k), np.array(a_k), np.array(g_k), np.array(sig)
+
+
+def gain_signs(p: HeomParams):
+    """(K, n2) sign(Re(v_a - v_b)) of every mode's bath (0 where the +1 term vanishes)."""
+    bath_of = _mode_constants(p)[0]
+    V = np.stack([np.diag(p.V[u]).real for u in range(p.n_noise)])
+    dv = (V[:, :, None] - V[:, None, :]).reshape(p.n_noise, -1)
+    return np.sign(dv[bath_of])
 
 
 def features(p: HeomParams, n_tab, rho_shallow, first):
@@ -112,7 +143,7 @@ def features(p: HeomParams, n_tab, rho_shallow, first):
     n = p.n_level
     n2 = n * n
     K = p.n_modes
-    bath_of, s_k, a_k, g_k = _mode_constants(p)
+    bath_of, s_k, a_k, g_k, _ = _mode_constants(p)
     R = rho_shallow[first:]                                    # (T, n, n)
     T = R.shape[0]
     s = np.sqrt((np.abs(R.astype(np.complex64)) ** 2).reshape(T, -1).max(axis=1)) + 1e-30
@@ -140,11 +171,21 @@ def sample_spin_boson(rng, depth):
     return spin_boson(eps=eps, lam=lam, beta=beta, depth=depth), (lam, beta, eps)
 
 
+CANCEL_MAX = 0.2
+
+
+def admits(qme) -> bool:
+    """True where the closure applies (see the module docstring)."""
+    return qme.get_precision()["cancel_log10"] <= CANCEL_MAX
+
+
 def deep_trajectories(params, t_samples, dt=0.005, precision="fp64"):
     """Plain-method states of a batch of (deep) instances at t_samples; returns
-    a list per instance of arrays (n_t, n_hrchy, n, n) and the stable mask."""
+    a list per instance of arrays (n_t, n_hrchy, n, n) and the mask of the
+    instances that stay bounded and that the closure applies to."""
     from .heom import batch_solver, from_params, rk4
     qmes = [from_params(p, precision=precision) for p in params]
+    gate = [admits(q) for q in qmes]
     bs = batch_solver(qmes, rk4())
     rho = np.concatenate([p.rho0_ground().ravel() for p in params])
     off = bs.offsets()
@@ -154,7 +195,7 @@ def deep_trajectories(params, t_samples, dt=0.005, precision="fp64"):
     out, stable = [], []
     for i, p in enumerate(params):
         a = frames[:, off[i]:off[i + 1]].reshape(len(t_samples), p.n_hrchy(), p.n_level, p.n_level)
-        ok = bool(np.all(np.isfinite(a)) and np.abs(a[:, 0]).max() <= 2.0)
+        ok = bool(gate[i] and np.all(np.isfinite(a)) and np.abs(a[:, 0]).max() <= 2.0)
         out.append(a)
         stable.append(ok)
     bs.close()
@@ -164,7 +205,8 @@ def deep_trajectories(params, t_samples, dt=0.005, precision="fp64"):
 
 
 def make_dataset(params_deep, shallow_depth, t_samples, dt=0.005):
-    """(X, T) rows for training from plain deep trajectories."""
+    """(X, T) rows for the closure loss from plain deep trajectories: T rows are
+    [Re t, Im t, Re r, Im r, sg] with t = rho_{n+1_k}/s, r = rho_n/(s sigma_k)."""
     from .heom import from_params
     p0 = params_deep[0]
     q = from_params(HeomParams(**{**p0.__dict__, "max_depth": shallow_depth}))
@@ -183,18 +225,23 @@ def make_dataset(params_deep, shallow_depth, t_samples, dt=0.005):
     for p, tr, ok in zip(params_deep, traj, stable):
         if not ok:
             continue
+        sig = _mode_constants(p)[4]
+        sg = gain_signs(p)                                    # (K, n2)
         for frame in tr:
             X, s = features(p, n_sh, frame[:nh_sh], first)
+            T = s.shape[0]
             child = p1_deep[first:nh_sh]                      # (T, K)
-            tgt = frame[child] / s[:, None, None, None]       # (T, K, n, n)
-            tgt = tgt.reshape(-1, n2)
+            tgt = (frame[child] / s[:, None, None, None]).reshape(-1, n2)
+            r = (frame[first:nh_sh].reshape(T, 1, n2) / s[:, None, None] / sig[None, :, None]).reshape(-1, n2)
+            sgr = np.broadcast_to(sg[None], (T,) + sg.shape).reshape(-1, n2)
             Xs.append(X)
-            Ts.append(np.concatenate([tgt.real, tgt.imag], axis=1).astype(np.float32))
+            Ts.append(np.concatenate([tgt.real, tgt.imag, r.real, r.imag, sgr], axis=1).astype(np.float32))
     return np.concatenate(Xs), np.concatenate(Ts), int(stable.sum())
 
 
-def train(mlp: MLP, X, T, epochs=10, batch=4096, lr=1e-3, seed=0, log=None):
-    """Adam on mean squared error with this library's kernels; returns epoch losses."""
+def train(mlp: MLP, X, T, epochs=10, batch=4096, lr=1e-3, seed=0, log=None, cosine=False):
+    """Adam with this library's kernels on the MLP's loss (set_loss); returns
+    epoch losses.  cosine: decay the step size to zero over the epochs."""
     import torch
     dev = torch.device("cuda")
     Xd = torch.from_numpy(np.ascontiguousarray(X)).to(dev)
@@ -203,6 +250,7 @@ def train(mlp: MLP, X, T, epochs=10, batch=4096, lr=1e-3, seed=0, log=None):
     n = X.shape[0]
     losses = []
     for ep in range(epochs):
+        lr_ep = 0.5 * lr * (1.0 + math.cos(math.pi * ep / epochs)) if cosine else lr
         perm = torch.randperm(n, generator=g).to(dev)
         tot, cnt = 0.0, 0
         for i in range(0, n - batch + 1, batch):
@@ -210,7 +258,7 @@ def train(mlp: MLP, X, T, epochs=10, batch=4096, lr=1e-3, seed=0, log=None):
             xb = Xd.index_select(0, idx).contiguous()
             tb = Td.index_select(0, idx).contiguous()
             torch.cuda.synchronize()
-            loss = mlp.train_step(xb.data_ptr(), tb.data_ptr(), batch, lr)
+            loss = mlp.train_step(xb.data_ptr(), tb.data_ptr(), batch, lr_ep)
             tot += loss
             cnt += 1
         losses.append(tot / max(cnt, 1))
@@ -219,9 +267,41 @@ def train(mlp: MLP, X, T, epochs=10, batch=4096, lr=1e-3, seed=0, log=None):
     return losses
 
 
+def physical(rho0, tol=0.05) -> bool:
+    """rho_0 finite with populations in [-tol, 1 + tol]."""
+    if not np.all(np.isfinite(rho0)):
+        return False
+    pops = np.real(np.diagonal(rho0))
+    return bool(pops.min() >= -tol and pops.max() <= 1.0 + tol)
+
+
+def propagate(p: HeomParams, mlp, t_list, dt=0.005, observe=None):
+    """Propagate p (truncated at its depth) with the learned closure `mlp` and
+    RK4; if rho_0 leaves the physical range at an output time, rerun with plain
+    truncation.  Returns (list of rho_0 at t_list, True if the closure was kept)."""
+    from .heom import from_params, qme_solver, rk4
+    for use in ((True, False) if mlp is not None else (False,)):
+        q = from_params(p)
+        if use and not admits(q):
+            q.close()
+            continue
+        if use:
+            attach(q, mlp)
+        s = qme_solver(q, rk4())
+        r = p.rho0_ground()
+        out = []
+        s.solve(r, t_list, lambda t: out.append(r[0].copy()), {"dt": dt})
+        s.close()
+        q.close()
+        if not use or all(physical(x) for x in out):
+            return out, use
+    raise AssertionError("unreachable")
+
+
 def population_errors(params_shallow, params_deep, mlp, t_list, dt=0.005):
-    """Max |rho_00(t) - rho_00^deep(t)| of plain truncation and of the learned
-    terminator, per instance (both at the shallow depth)."""
+    """Per instance: [max |rho_00(t) - rho_00^deep(t)| of plain truncation, the
+    same with the learned closure (plain-truncation fallback included), 1 if
+    the closure was kept], all at the shallow depth."""
     from .heom import from_params, qme_solver, rk4
     out = []
     for ps, pd in zip(params_shallow, params_deep):
@@ -230,19 +310,12 @@ def population_errors(params_shallow, params_deep, mlp, t_list, dt=0.005):
         sd = qme_solver(qd, rk4())
         r = pd.rho0_ground()
         sd.solve(r, t_list, lambda t: ref.append(r[0, 0, 0].real), {"dt": dt})
-        res = []
-        for use in (False, True):
-            q = from_params(ps)
-            if use:
-                attach(q, mlp)
-            s = qme_solver(q, rk4())
-            r = ps.rho0_ground()
-            pops = []
-            s.solve(r, t_list, lambda t: pops.append(r[0, 0, 0].real), {"dt": dt})
-            res.append(float(np.max(np.abs(np.array(pops) - np.array(ref)))))
-            s.close()
-            q.close()
-        out.append(res)
         sd.close()
         qd.close()
+        ref = np.array(ref)
+        plain, _ = propagate(ps, None, t_list, dt)
+        term, kept = propagate(ps, mlp, t_list, dt)
+        e_plain = float(np.max(np.abs(np.array([x[0, 0].real for x in plain]) - ref)))
+        e_term = float(np.max(np.abs(np.array([x[0, 0].real for x in term]) - ref)))
+        out.append([e_plain, e_term, 1.0 if kept else 0.0])
     return np.array(out)

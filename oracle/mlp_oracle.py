@@ -9,6 +9,9 @@ backward and inference kernels of the terminator (libheom_gb300/csrc/mlp.cu).
 * Terminator features of a tier-N ADO rho_n and mode k:
   [Re rho/s, Im rho/s, onehot(k), Re A/s, Im A/s], s = max |rho_n|,
   A = (n_k+1) (-i s_k (v_a - v_b) + a_k (v_a + v_b)) rho_ab / (ngamma_n + gamma_kk).
+* Gain head and closure loss: outputs (y | z) of a row give
+  C = y - i sign(v_a - v_b) softplus(z) and the prediction C rho_n / sigma_k;
+  the loss is each row's squared error relative to its own size.
 """
 from __future__ import annotations
 
@@ -54,11 +57,45 @@ def forward(params, x, din, h, dout):
     return a2 @ W3.T + b3, (z1, a1, z2, a2)
 
 
-def gradients(params, x, t, din, h, dout):
-    """Gradient of mean((y - t)^2) with respect to the packed parameters."""
+def softplus(z):
+    return np.maximum(z, 0.0) + np.log1p(np.exp(-np.abs(z)))
+
+
+def gain_head(y, sg):
+    """C_e = y_e - i sg_e softplus(z_e) from the outputs (y | z) of a row."""
+    n2 = sg.shape[-1]
+    return y[..., :n2] - 1j * sg * softplus(y[..., n2:])
+
+
+def gain_loss(y, t):
+    """Closure loss of rows y (B, 2 n2) against t (B, 5 n2) and its gradient d/dy."""
+    n2 = y.shape[1] // 2
+    tt = t[:, :n2] + 1j * t[:, n2:2 * n2]
+    r = t[:, 2 * n2:3 * n2] + 1j * t[:, 3 * n2:4 * n2]
+    sg = t[:, 4 * n2:]
+    m = np.abs(sg)
+    C = gain_head(y, sg)
+    d = C * r - tt
+    den = (m * (np.abs(tt) ** 2 + 1e-2 * np.abs(r) ** 2)).sum(1) + 1e-6
+    B = y.shape[0]
+    loss = float(np.mean((m * np.abs(d) ** 2).sum(1) / den))
+    w = (2.0 / (B * den))[:, None]
+    cr = np.conj(d) * r
+    z = y[:, n2:]
+    dy = np.concatenate([w * m * cr.real, w * m * sg * (1.0 / (1.0 + np.exp(-z))) * cr.imag], axis=1)
+    return loss, dy
+
+
+def gradients(params, x, t, din, h, dout, loss_kind=0):
+    """Gradient of the loss (0: mean((y - t)^2); 1: gain_loss) with respect to
+    the packed parameters."""
     W1, b1, W2, b2, W3, b3 = unpack(params, din, h, dout)
     y, (z1, a1, z2, a2) = forward(params, x, din, h, dout)
-    dy = 2.0 * (y - t) / y.size
+    if loss_kind == 1:
+        loss, dy = gain_loss(y, t)
+    else:
+        dy = 2.0 * (y - t) / y.size
+        loss = float(np.mean((y - t) ** 2))
     gW3 = dy.T @ a2
     gb3 = dy.sum(0)
     d2 = (dy @ W3) * gelu_grad(z2)
@@ -67,7 +104,6 @@ def gradients(params, x, t, din, h, dout):
     d1 = (d2 @ W2) * gelu_grad(z1)
     gW1 = d1.T @ x
     gb1 = d1.sum(0)
-    loss = float(np.mean((y - t) ** 2))
     return np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gW3.ravel(), gb3]), loss
 
 

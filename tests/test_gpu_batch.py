@@ -62,3 +62,31 @@ def test_batch_rejects_adaptive_solver():
     qmes = [lh.from_params(p) for p in ps]
     with pytest.raises(lh.HeomError):
         lh.batch_solver(qmes, lh.rkdp())
+
+
+def test_range_guard_splits_mixed_batch():
+    """A MIXED request whose bath expansion defeats FP32 stage inputs (deep
+    ADOs that outgrow rho_0 and coefficients that cancel) keeps FP64
+    arithmetic; the batch then runs as two sub-batches whose concatenated
+    result matches per-instance solves."""
+    ps = sample_instances(12, 6)
+    qmes = [lh.from_params(p, precision="mixed") for p in ps]
+    info = [q.get_precision() for q in qmes]
+    assert all(i["requested"] == "mixed" for i in info)
+    kept = [k for k, i in enumerate(info) if i["effective"] == "fp64"]
+    assert kept and len(kept) < len(ps)
+    for k, i in enumerate(info):
+        g, c = i["growth_log10"], i["cancel_log10"]
+        assert (k in kept) == (c > 0.8 or g > 7.5 or (g > 2.0 and c > 0.2))
+    bs = lh.batch_solver(qmes, lh.rk4())
+    assert sorted(len(idx) for idx, _ in bs.parts()) == sorted([len(kept), len(ps) - len(kept)])
+    rho = np.concatenate([p.rho0_ground().ravel() for p in ps])
+    bs.solve(rho, [0.0, 0.05, 0.1], None, {"dt": 0.005})
+    off = bs.offsets()
+    mixed_k = next(k for k, i in enumerate(info) if i["effective"] == "mixed")
+    # FP64 arithmetic is reproduced to rounding; the FP32 sub-batch to FP32 level
+    for k, tol in ((kept[0], 1e-12), (mixed_k, 1e-6)):
+        q1 = lh.from_params(ps[k], precision="mixed")
+        r1 = ps[k].rho0_ground().ravel().copy()
+        lh.qme_solver(q1, lh.rk4()).solve(r1, [0.0, 0.05, 0.1], None, {"dt": 0.005})
+        assert np.abs(rho[off[k]:off[k + 1]] - r1).max() <= tol * max(1.0, np.abs(r1).max())

@@ -92,6 +92,20 @@ heomgb_status heomgb_qme_set_noise(heomgb_qme* q, int u, const double* V, int le
                                    const double* phi_0, const double* sigma, const double* S, const double* A,
                                    const double* s_delta);
 heomgb_status heomgb_qme_set_precision(heomgb_qme* q, heomgb_precision p);
+/* Normalisation of the auxiliary density operators, the reference's
+ * compile-time LIBHEOM_SQRT_NORMALIZATION switch made a model option: INTEGER
+ * (the reference's default) or SQRT, where the +1 terms scale by sqrt(n_k+1)
+ * and the -1 terms by sqrt(n_k) instead of 1 and n_k (heom_hilb.h:140-196,
+ * heom_liou.h:188-230, heom_ado.h:93-97,131-139).  Set before set_param. */
+typedef enum heomgb_normalization { HEOMGB_NORM_INTEGER = 0, HEOMGB_NORM_SQRT = 1 } heomgb_normalization;
+heomgb_status heomgb_qme_set_normalization(heomgb_qme* q, heomgb_normalization norm);
+/* Storage order of every ADO in the state vectors the caller passes (rho,
+ * drho, the solve state and the callback's view of it): the reference's
+ * `order` template argument (row_major / col_major, type.h; lil_matrix.h.j2:
+ * 156-163).  Parameter matrices are always given row-major (logical entries).
+ * The device keeps row-major ADOs and transposes at the boundary. */
+typedef enum heomgb_order { HEOMGB_ROW_MAJOR = 0, HEOMGB_COL_MAJOR = 1 } heomgb_order;
+heomgb_status heomgb_qme_set_order(heomgb_qme* q, heomgb_order order);
 /* Precision after set_param (no reference counterpart: the reference has one
  * compile-time precision).  A MIXED request runs with FP64 arithmetic
  * (effective = FP64) when the bath expansion makes FP32 arithmetic unsafe.

@@ -79,6 +79,10 @@ class qme_base {
   std::unique_ptr<lil_matrix[]> A;
   std::unique_ptr<complex128[]> s_delta;
   heomgb_precision precision = HEOMGB_FP64;
+  // the reference's LIBHEOM_SQRT_NORMALIZATION build switch, as a member
+  heomgb_normalization normalization = HEOMGB_NORM_INTEGER;
+  // the reference's `order` template argument, as a member
+  heomgb_order order = HEOMGB_ROW_MAJOR;
 
   virtual ~qme_base() { release(); }
 
@@ -137,6 +141,8 @@ class qme_base {
                                  reinterpret_cast<const double*>(Ad.data()), reinterpret_cast<const double*>(&sd)));
     }
     check(heomgb_qme_set_precision(h_, precision));
+    check(heomgb_qme_set_normalization(h_, normalization));
+    check(heomgb_qme_set_order(h_, order));
     check(heomgb_qme_set_param(h_));
   }
 };

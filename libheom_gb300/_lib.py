@@ -47,6 +47,8 @@ SIGNATURES = {
                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_void_p]),
     "heomgb_qme_set_precision": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "heomgb_qme_set_normalization": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "heomgb_qme_set_order": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "heomgb_qme_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "heomgb_qme_get_precision": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_double_p, c_double_p]),
     "heomgb_qme_set_param": (ctypes.c_int, [ctypes.c_void_p]),

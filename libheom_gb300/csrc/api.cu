@@ -264,6 +264,10 @@ struct heomgb_qme {
   int U = -1;
   std::vector<Bath> baths;
   int precision = HEOMGB_FP64;       // requested
+  int sqrt_norm = 0;                 // HEOMGB_NORM_SQRT
+  int col_major = 0;                 // HEOMGB_COL_MAJOR: ADOs stored column-major at the boundary
+  double2* tx = nullptr;             // col_major transposes of calc_diff (in scratch)
+  double2* ty = nullptr;
   int precision_eff = HEOMGB_FP64;   // in use: a MIXED request falls back to FP64 under the range guard
   double range_growth = 0.0;         // range guard inputs (see build_model)
   double range_cancel = 0.0;
@@ -302,8 +306,10 @@ struct heomgb_qme_solver {
   cudaStream_t stream = nullptr;
   bool mixed = false;
   bool separate = false;
+  bool col_major = false;              // models store their ADOs column-major
   long long N = 0;
   DeviceArena arena;
+  double2* otmp = nullptr;             // boundary transposes of col_major models
   double2* S[2] = {nullptr, nullptr};
   void* Yb[2] = {nullptr, nullptr};
   void* Ytmp[2] = {nullptr, nullptr};
@@ -461,6 +467,7 @@ void build_model(heomgb_qme* q) {
   bool h_real = true;
   for (const cd& v : q->H) h_real = h_real && v.imag() == 0.0;
   m.h_real = h_real ? 1 : 0;
+  m.sqrt_norm = q->sqrt_norm;
   m.H = q->arena.upload(to_d2(q->H), s);
   m.H_f = q->arena.upload(to_f2(q->H), s);
   std::vector<cd> Vall;
@@ -536,6 +543,7 @@ void build_model(heomgb_qme* q) {
     di.K = K;
     di.nh = nh;
     di.h_real = m.h_real;
+    di.sqrt_norm = m.sqrt_norm;
     di.elem_off = 0;
     di.p1 = m.p1;
     di.m1 = m.m1;
@@ -658,7 +666,29 @@ TermModel term_model(const heomgb_qme* q) {
   return tm;
 }
 
+void run_diff_rm(heomgb_qme* q, double2* drho, const double2* rho, const double* alpha, const double* beta);
+
+// calc_diff in the model's storage order: a col_major model sees its ADOs
+// transposed into row-major scratch and the result transposed back.
 void run_diff(heomgb_qme* q, double2* drho, const double2* rho, const double* alpha, const double* beta) {
+  if (!q->col_major) {
+    run_diff_rm(q, drho, rho, alpha, beta);
+    return;
+  }
+  cudaStream_t s = q->stream();
+  if (!q->tx) {
+    const size_t bytes = sizeof(double2) * q->main_size();
+    q->tx = static_cast<double2*>(q->scratch.alloc(bytes));
+    q->ty = static_cast<double2*>(q->scratch.alloc(bytes));
+  }
+  const bool beta_zero = !beta || (beta[0] == 0.0 && beta[1] == 0.0);
+  ck(launch_transpose_ados(rho, q->tx, q->n, q->n_hrchy, s), "transpose in");
+  if (!beta_zero) ck(launch_transpose_ados(drho, q->ty, q->n, q->n_hrchy, s), "transpose in");
+  run_diff_rm(q, q->ty, q->tx, alpha, beta);
+  ck(launch_transpose_ados(q->ty, drho, q->n, q->n_hrchy, s), "transpose out");
+}
+
+void run_diff_rm(heomgb_qme* q, double2* drho, const double2* rho, const double* alpha, const double* beta) {
   Stage st = base_stage();
   st.kind = EPI_DIFF;
   st.y_sel = 0;
@@ -690,6 +720,7 @@ void alloc_solver(heomgb_qme_solver* qs) {
   for (heomgb_qme* m : qs->qmes) N += m->main_size();
   qs->N = N;
   qs->mixed = q->precision_eff == HEOMGB_MIXED;
+  qs->col_major = q->col_major != 0;
   qs->separate = qs->mixed;
   const size_t bd = sizeof(double2) * N;
   const size_t bb = (qs->mixed ? sizeof(float2) : sizeof(double2)) * N;
@@ -704,6 +735,7 @@ void alloc_solver(heomgb_qme_solver* qs) {
     qs->Ytmp[1] = A.alloc(bb);
   }
   if (qs->kind == HEOMGB_RK4 || qs->kind == HEOMGB_LSRK4) qs->acc = static_cast<double2*>(A.alloc(bd));
+  if (qs->col_major) qs->otmp = static_cast<double2*>(A.alloc(bd));
   if (qs->kind == HEOMGB_RKDP)
     for (int i = 0; i < 6; ++i) qs->K[i] = A.alloc(bb);
   qs->ctl = static_cast<DpCtl*>(A.alloc(sizeof(DpCtl)));
@@ -1033,6 +1065,15 @@ int solve_adaptive(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwa
   return qs->ctl_host->cur;
 }
 
+// Per-instance ADO transposes of a concatenated (batch) state.
+void transpose_instances(heomgb_qme_solver* qs, const double2* in, double2* out) {
+  long long off = 0;
+  for (heomgb_qme* m : qs->qmes) {
+    ck(launch_transpose_ados(in + off, out + off, m->n, m->n_hrchy, qs->stream), "transpose");
+    off += m->main_size();
+  }
+}
+
 void solve_impl(heomgb_qme_solver* qs, void* rho, bool host, const double* t_list, int n_t, heomgb_callback cb,
                 void* user, const heomgb_kwargs* kw) {
   if (!qs) throw arg_error("null qme_solver");
@@ -1053,14 +1094,24 @@ void solve_impl(heomgb_qme_solver* qs, void* rho, bool host, const double* t_lis
       if (!host) ck(cudaStreamSynchronize(qs->stream), "sync before callback");
       cb(t_list[i], user);
     }
-    ck(cudaMemcpyAsync(qs->S[0], rho, bytes, in_kind, qs->stream), "state in");
+    if (qs->col_major) {  // the caller's ADOs are column-major: transpose at the boundary
+      ck(cudaMemcpyAsync(qs->otmp, rho, bytes, in_kind, qs->stream), "state in");
+      transpose_instances(qs, qs->otmp, qs->S[0]);
+    } else {
+      ck(cudaMemcpyAsync(qs->S[0], rho, bytes, in_kind, qs->stream), "state in");
+    }
     state_to_bulk(qs, 0);
     int cur = 0;
     if (qs->kind == HEOMGB_RKDP)
       cur = solve_adaptive(qs, t_list[i], t_list[i + 1], kw, 0);
     else
       solve_fixed(qs, t_list[i], t_list[i + 1], kw);
-    ck(cudaMemcpyAsync(rho, qs->S[cur], bytes, out_kind, qs->stream), "state out");
+    if (qs->col_major) {
+      transpose_instances(qs, qs->S[cur], qs->otmp);
+      ck(cudaMemcpyAsync(rho, qs->otmp, bytes, out_kind, qs->stream), "state out");
+    } else {
+      ck(cudaMemcpyAsync(rho, qs->S[cur], bytes, out_kind, qs->stream), "state out");
+    }
     ck(cudaStreamSynchronize(qs->stream), "interval sync");
     busy_collect(qs);
   }
@@ -1179,6 +1230,24 @@ heomgb_status heomgb_qme_set_precision(heomgb_qme* q, heomgb_precision p) {
   });
 }
 
+heomgb_status heomgb_qme_set_order(heomgb_qme* q, heomgb_order order) {
+  return guard([&] {
+    require(q != nullptr, "null qme");
+    require(order == HEOMGB_ROW_MAJOR || order == HEOMGB_COL_MAJOR, "unknown order");
+    if (q->live_solvers > 0) throw state_error("set_order: destroy the qme_solvers of this model first");
+    q->col_major = order == HEOMGB_COL_MAJOR ? 1 : 0;
+  });
+}
+
+heomgb_status heomgb_qme_set_normalization(heomgb_qme* q, heomgb_normalization norm) {
+  return guard([&] {
+    require(q != nullptr, "null qme");
+    require(norm == HEOMGB_NORM_INTEGER || norm == HEOMGB_NORM_SQRT, "unknown normalisation");
+    if (q->live_solvers > 0) throw state_error("set_normalization: destroy the qme_solvers of this model first");
+    q->sqrt_norm = norm == HEOMGB_NORM_SQRT ? 1 : 0;
+  });
+}
+
 heomgb_status heomgb_qme_get_precision(const heomgb_qme* q, int* requested, int* effective, double* growth_log10,
                                        double* cancel_log10) {
   return guard([&] {
@@ -1211,6 +1280,7 @@ heomgb_status heomgb_qme_set_terminator(heomgb_qme* q, heomgb_mlp* mlp) {
     if (q->live_solvers > 0) throw state_error("set_terminator: destroy the qme_solvers of this model first");
     if (mlp) {
       if (q->path != PATH_DIAG) throw unsupported_error("the learned terminator needs diagonal couplings V (heom_hilb)");
+      if (q->sqrt_norm) throw unsupported_error("the learned terminator is trained for the integer normalisation");
       int din = 0, h = 0, dout = 0;
       mlp_dims(mlp, &din, &h, &dout);
       const int n2 = q->n * q->n;
@@ -1349,6 +1419,7 @@ heomgb_status heomgb_batch_solver_create(heomgb_qme* const* qmes, int count, heo
         throw unsupported_error("batches need heom_hilb models with diagonal couplings V");
       if (qmes[i]->precision_eff != q0->precision_eff)
         throw arg_error("batch models must share one effective precision (heomgb_qme_get_precision)");
+      if (qmes[i]->col_major != q0->col_major) throw arg_error("batch models must share one storage order");
       if (qmes[i]->device != q0->device) throw arg_error("batch models must live on one device");
     }
     ck(cudaSetDevice(q0->device), "cudaSetDevice");

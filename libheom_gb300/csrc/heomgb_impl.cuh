@@ -37,6 +37,7 @@ struct DpCtl {
 struct RhsModel {
   int n, n2, K, U, n_hrchy;
   int h_real;                       // H has zero imaginary part
+  int sqrt_norm;                    // see DiagInst::sqrt_norm
   const int* p1;                    // (n_hrchy+1)*K, sentinel n_hrchy
   const int* m1;                    // (n_hrchy+1)*K
   const int* nidx;                  // n_hrchy*K
@@ -139,7 +140,7 @@ struct DiagInst {
   // (l - term_first)*K + k, used where ptr_p1 is the sentinel; null = truncation
   const float2* term_p;
   int term_first;
-  int pad_;
+  int sqrt_norm;            // 1: +1 terms scale by sqrt(n_k+1), -1 terms by sqrt(n_k) (else 1 and n_k)
 };
 struct DiagTile {
   int inst, l0, nt, pad;
@@ -168,6 +169,7 @@ cudaError_t launch_hrchy_build(int K, int depth, int n_hrchy, const long long* b
 cudaError_t launch_ngd(int K, int n_hrchy, const int* nidx, const double2* gdiag, double2* ngd, float2* ngd_f,
                        cudaStream_t s);
 cudaError_t launch_to_bulk(const double2* src, float2* dst, long long n, cudaStream_t s);
+cudaError_t launch_transpose_ados(const double2* in, double2* out, int n, long long count, cudaStream_t s);
 cudaError_t launch_ctl_init(DpCtl* c, double t, double dt, double t_bound, double atol, double rtol, int cur,
                             cudaStream_t s);
 cudaError_t launch_ctl_set_fixed(DpCtl* c, double dt, cudaStream_t s);

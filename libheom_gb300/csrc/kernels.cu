@@ -468,6 +468,7 @@ __device__ __forceinline__ double diag_tile(const DiagInst* __restrict__ I, cons
   const C* __restrict__ csd = pick<TC>(I->c_sd, I->c_sd_f);
   const float2* __restrict__ term_p = I->term_p;
   const int term_first = I->term_first;
+  const bool sqn = I->sqrt_norm != 0;
   const int* __restrict__ plus_ptr = I->plus_ptr;
   const int* __restrict__ plus_mode = I->plus_mode;
   const int* __restrict__ minus_ptr = I->minus_ptr;
@@ -511,6 +512,10 @@ __device__ __forceinline__ double diag_tile(const DiagInst* __restrict__ I, cons
           if (lp != void_idx) {
             v[j] = ldc<TC>(yi + static_cast<size_t>(lp) * n2 + e);
             cf[j] = cpl[p];
+            if (sqn) {
+              const TC f = sqrt(static_cast<TC>(nrow[k] + 1));
+              cf[j] = cx<TC>(f * cf[j].x, f * cf[j].y);
+            }
           } else if (term_p) {  // truncated tier: the terminator's prediction
             const float2 t = term_p[(static_cast<size_t>(l0 + lt - term_first) * K + k) * n2 + e];
             v[j] = cx<TC>(static_cast<TC>(t.x), static_cast<TC>(t.y));
@@ -527,7 +532,7 @@ __device__ __forceinline__ double diag_tile(const DiagInst* __restrict__ I, cons
           const int k = __ldg(minus_mode + p);
           const int lm = m1row[k];
           if (lm != void_idx) {
-            const TC nk = static_cast<TC>(nrow[k]);
+            const TC nk = sqn ? sqrt(static_cast<TC>(nrow[k])) : static_cast<TC>(nrow[k]);
             const C cm = cmi[p];
             v[4 + j] = ldc<TC>(yi + static_cast<size_t>(lm) * n2 + e);
             cf[4 + j] = cx<TC>(nk * cm.x, nk * cm.y);
@@ -726,12 +731,20 @@ __global__ void __launch_bounds__(256) k_rhs_general(const RhsModel m, const Sta
         C ph = cx<TC>(0, 0), ps = cx<TC>(0, 0);
         for (int k = k0; k < k1; ++k) {
           const int lp = __ldg(m.p1 + static_cast<size_t>(l) * K + k);
-          if (lp != void_idx) cfma(ph, sig[k], ldc<TC>(y + static_cast<size_t>(lp) * n2 + e));
+          if (lp != void_idx) {
+            C c = sig[k];
+            if (m.sqrt_norm) {
+              const TC f = sqrt(static_cast<TC>(__ldg(m.nidx + static_cast<size_t>(l) * K + k) + 1));
+              c = cx<TC>(f * c.x, f * c.y);
+            }
+            cfma(ph, c, ldc<TC>(y + static_cast<size_t>(lp) * n2 + e));
+          }
         }
         for (int k = k0; k < k1; ++k) {
           const int lm = __ldg(m.m1 + static_cast<size_t>(l) * K + k);
           if (lm != void_idx) {
-            const TC nk = static_cast<TC>(__ldg(m.nidx + static_cast<size_t>(l) * K + k));
+            const int nki = __ldg(m.nidx + static_cast<size_t>(l) * K + k);
+            const TC nk = m.sqrt_norm ? sqrt(static_cast<TC>(nki)) : static_cast<TC>(nki);
             const C r = ldc<TC>(y + static_cast<size_t>(lm) * n2 + e);
             cfma(ph, cx<TC>(nk * sv[k].x, nk * sv[k].y), r);
             cfma(ps, cx<TC>(-nk * av[k].x, -nk * av[k].y), r);
@@ -810,12 +823,20 @@ __global__ void __launch_bounds__(256) k_rhs_liou(const RhsModel m, const Stage 
         C ph = cx<TC>(0, 0), ps = cx<TC>(0, 0);
         for (int k = k0; k < k1; ++k) {
           const int lp = __ldg(m.p1 + static_cast<size_t>(l) * K + k);
-          if (lp != void_idx) cfma(ph, sig[k], ldc<TC>(y + static_cast<size_t>(lp) * n2 + e));
+          if (lp != void_idx) {
+            C c = sig[k];
+            if (m.sqrt_norm) {
+              const TC f = sqrt(static_cast<TC>(__ldg(m.nidx + static_cast<size_t>(l) * K + k) + 1));
+              c = cx<TC>(f * c.x, f * c.y);
+            }
+            cfma(ph, c, ldc<TC>(y + static_cast<size_t>(lp) * n2 + e));
+          }
         }
         for (int k = k0; k < k1; ++k) {
           const int lm = __ldg(m.m1 + static_cast<size_t>(l) * K + k);
           if (lm != void_idx) {
-            const TC nk = static_cast<TC>(__ldg(m.nidx + static_cast<size_t>(l) * K + k));
+            const int nki = __ldg(m.nidx + static_cast<size_t>(l) * K + k);
+            const TC nk = m.sqrt_norm ? sqrt(static_cast<TC>(nki)) : static_cast<TC>(nki);
             const C r = ldc<TC>(y + static_cast<size_t>(lm) * n2 + e);
             cfma(ph, cx<TC>(nk * sv[k].x, nk * sv[k].y), r);
             cfma(ps, cx<TC>(-nk * av[k].x, -nk * av[k].y), r);
@@ -1029,6 +1050,29 @@ __global__ void k_to_bulk(const double2* src, float2* dst, long long n) {
 cudaError_t launch_to_bulk(const double2* src, float2* dst, long long n, cudaStream_t s) {
   const int grid = static_cast<int>(std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 8)));
   k_to_bulk<<<grid, 256, 0, s>>>(src, dst, n);
+  ++g_launches;
+  return cudaGetLastError();
+}
+
+// out_l = in_l^T for `count` consecutive n x n blocks: the reference's
+// col_major storage of the ADOs <-> the row-major layout the kernels use.
+// Out of place; one thread per element, reads coalesced.
+__global__ void k_transpose_ados(const double2* __restrict__ in, double2* __restrict__ out, int n, long long count) {
+  const long long n2 = static_cast<long long>(n) * n, total = n2 * count;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long l = i / n2;
+    const int e = static_cast<int>(i - l * n2);
+    const int a = e / n, b = e - a * n;
+    out[l * n2 + static_cast<long long>(b) * n + a] = in[i];
+  }
+}
+
+cudaError_t launch_transpose_ados(const double2* in, double2* out, int n, long long count, cudaStream_t s) {
+  const long long total = static_cast<long long>(n) * n * count;
+  if (total <= 0) return cudaSuccess;
+  const int grid = static_cast<int>(std::max<long long>(1, std::min<long long>((total + 255) / 256, 152 * 8)));
+  k_transpose_ados<<<grid, 256, 0, s>>>(in, out, n, count);
   ++g_launches;
   return cudaGetLastError();
 }

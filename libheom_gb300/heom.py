@@ -56,6 +56,10 @@ class heom:
         self.V, self.len_gamma, self.gamma, self.phi_0, self.sigma = [], [], [], [], []
         self.S, self.A, self.s_delta = [], [], []
         self.precision = "fp64"
+        # "integer" (the reference's default) or "sqrt" (its LIBHEOM_SQRT_NORMALIZATION build)
+        self.normalization = "integer"
+        # storage of every ADO in the caller's state arrays: the reference's `order`
+        self.order = "row_major"
         self.stream = None  # optional cudaStream_t handle (int)
         self._h = ctypes.c_void_p()
         self._lib = _lib.load()
@@ -103,6 +107,8 @@ class heom:
             check(lib.heomgb_qme_set_noise(h, u, V.ctypes.data, L, g.ctypes.data, p.ctypes.data, s.ctypes.data,
                                            Sm.ctypes.data, Am.ctypes.data, sd.ctypes.data))
         check(lib.heomgb_qme_set_precision(h, _PRECISION[self.precision]))
+        check(lib.heomgb_qme_set_normalization(h, {"integer": 0, "sqrt": 1}[self.normalization]))
+        check(lib.heomgb_qme_set_order(h, {"row_major": 0, "col_major": 1}[self.order]))
         if self.stream:
             check(lib.heomgb_qme_set_stream(h, ctypes.c_void_p(int(self.stream))))
         check(lib.heomgb_qme_set_param(h))
@@ -464,6 +470,8 @@ def from_params(p, form: str = "hilb", precision: str = "fp64", stream=None) -> 
         q.A[u] = p.A[u]
         q.s_delta[u] = p.s_delta[u]
     q.precision = precision
+    q.normalization = p.normalization
+    q.order = p.order
     q.stream = stream
     q.set_param()
     return q

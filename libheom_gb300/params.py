@@ -27,6 +27,10 @@ class HeomParams:
     max_depth: int
     name: str = "heom"
     meta: dict = field(default_factory=dict)
+    # "integer" (the reference's default) or "sqrt" (LIBHEOM_SQRT_NORMALIZATION)
+    normalization: str = "integer"
+    # storage of every ADO in the state vector: the reference's `order`
+    order: str = "row_major"
 
     def __post_init__(self):
         self.H = np.ascontiguousarray(self.H, dtype=np.complex128)
@@ -44,6 +48,10 @@ class HeomParams:
         self.phi_0 = [np.ascontiguousarray(np.atleast_1d(g), dtype=np.complex128) for g in self.phi_0]
         self.sigma = [np.ascontiguousarray(np.atleast_1d(g), dtype=np.complex128) for g in self.sigma]
         self.s_delta = [complex(x) for x in self.s_delta]
+        if self.normalization not in ("integer", "sqrt"):
+            raise ValueError("normalization must be 'integer' or 'sqrt'")
+        if self.order not in ("row_major", "col_major"):
+            raise ValueError("order must be 'row_major' or 'col_major'")
         for u in range(U):
             k = self.gamma[u].shape[0]
             if self.V[u].shape != (n, n):

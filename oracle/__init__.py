@@ -21,9 +21,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_lib", "libheom_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libheomref.so")
+REF_SQRT_SO = os.path.join(HERE, "_ref", "libheomref_sqrt.so")
 REF_TREE = "/root/reference"
 
-FORMS = {"hilb": 0, "liou": 1, "ado": 2}
+FORMS = {"hilb": 0, "liou": 1, "ado": 2, "redfield_hilb": 3, "redfield_liou": 4}
 SOLVERS = {"rk4": 0, "lsrk4": 1, "rkdp": 2}
 
 
@@ -31,7 +32,8 @@ class _Case(ctypes.Structure):
     _fields_ = [("n_level", ctypes.c_int), ("n_noise", ctypes.c_int), ("max_depth", ctypes.c_int),
                 ("H", ctypes.c_void_p), ("V", ctypes.c_void_p), ("len_gamma", ctypes.c_void_p),
                 ("gamma", ctypes.c_void_p), ("phi_0", ctypes.c_void_p), ("sigma", ctypes.c_void_p),
-                ("S", ctypes.c_void_p), ("A", ctypes.c_void_p), ("s_delta", ctypes.c_void_p)]
+                ("S", ctypes.c_void_p), ("A", ctypes.c_void_p), ("s_delta", ctypes.c_void_p),
+                ("sqrt_normalization", ctypes.c_int), ("col_major", ctypes.c_int)]
 
 
 class PackedCase:
@@ -52,21 +54,26 @@ class PackedCase:
         ptr = lambda a: a.ctypes.data if a.size else None
         self.struct = _Case(p.n_level, p.n_noise, p.max_depth, ptr(self.H), ptr(self.V), ptr(self.len_gamma),
                             ptr(self.gamma), ptr(self.phi_0), ptr(self.sigma), ptr(self.S), ptr(self.A),
-                            ptr(self.s_delta))
+                            ptr(self.s_delta), 1 if getattr(p, "normalization", "integer") == "sqrt" else 0,
+                            1 if getattr(p, "order", "row_major") == "col_major" else 0)
 
 
 def build(which: str = "port") -> None:
-    target = {"port": PORT_SO, "ref": REF_SO}[which]
-    if which == "ref" and not os.path.isdir(REF_TREE):
+    target = {"port": PORT_SO, "ref": REF_SO, "ref_sqrt": REF_SQRT_SO}[which]
+    if which.startswith("ref") and not os.path.isdir(REF_TREE):
         raise FileNotFoundError("reference tree not present; the reference oracle cannot be built here")
-    subprocess.run(["make", "-s", "-C", HERE, which], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "port" if which == "port" else "ref"], check=True)
     if not os.path.exists(target):
         raise RuntimeError(f"oracle build produced no {target}")
 
 
 class Oracle:
+    """which: "port", "ref" (the reference's build) or "ref_sqrt" (its
+    LIBHEOM_SQRT_NORMALIZATION build; models must then carry
+    normalization="sqrt")."""
+
     def __init__(self, which: str = "port"):
-        path = {"port": PORT_SO, "ref": REF_SO}[which]
+        path = {"port": PORT_SO, "ref": REF_SO, "ref_sqrt": REF_SQRT_SO}[which]
         if not os.path.exists(path):
             build(which)
         self.which = which

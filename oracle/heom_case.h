@@ -25,6 +25,8 @@ typedef struct heom_case {
   const double* S;       /* sum_u len_u^2 complex                           */
   const double* A;       /* sum_u len_u^2 complex                           */
   const double* s_delta; /* U complex                                       */
+  int sqrt_normalization; /* 1: LIBHEOM_SQRT_NORMALIZATION (heom_hilb.h:140-196) */
+  int col_major;          /* 1: the `col_major` order: each ADO stored column-major */
 } heom_case;
 
 /* form: 0 = heom_hilb, 1 = heom_liou (CSR superoperators), 2 = heom_ado.

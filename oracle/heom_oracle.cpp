@@ -113,6 +113,7 @@ struct Model {
   std::vector<cx> sigma, s, a; // K
   std::vector<cx> s_delta;     // U
   std::vector<cx> ngamma;      // count
+  bool sqrt_norm = false;      // LIBHEOM_SQRT_NORMALIZATION
   Hierarchy hs;
 };
 
@@ -123,6 +124,7 @@ Model make_model(const heom_case* c) {
   m.n = c->n_level;
   m.n2 = m.n * m.n;
   m.U = c->n_noise;
+  m.sqrt_norm = c->sqrt_normalization != 0;
   if (m.n <= 0 || m.U < 0 || c->max_depth < 0) throw std::invalid_argument("bad sizes");
   m.H.resize(m.n2);
   for (int i = 0; i < m.n2; ++i) m.H[i] = C(c->H, i);
@@ -164,6 +166,14 @@ Model make_model(const heom_case* c) {
   return m;
 }
 
+// out_l = in_l^T for every n x n block (row-major <-> column-major storage).
+void transpose_ados(const cx* in, cx* out, int n, int count) {
+  const size_t n2 = static_cast<size_t>(n) * n;
+  for (int l = 0; l < count; ++l)
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) out[l * n2 + static_cast<size_t>(j) * n + i] = in[l * n2 + static_cast<size_t>(i) * n + j];
+}
+
 // ---------------------------------------------------------------- RHS
 // out_l = beta*out_l - alpha*D_l, with D_l the operator of heom_hilb.h:96-212.
 void calc_diff(const Model& m, const cx* rho, cx* out, cx alpha, cx beta) {
@@ -199,6 +209,8 @@ void calc_diff(const Model& m, const cx* rho, cx* out, cx alpha, cx beta) {
             }
         }
         // Phi = sum sigma_k rho_{n+1_k} + n_k s_k rho_{n-1_k};  Psi = -sum n_k a_k rho_{n-1_k}
+        // (heom_hilb.h:170-196; with the square-root normalisation the +1 term
+        // carries sqrt(n_k+1) and the -1 terms sqrt(n_k) instead of n_k)
         std::fill(Phi.begin(), Phi.end(), cx{0, 0});
         std::fill(Psi.begin(), Psi.end(), cx{0, 0});
         for (int k = 0; k < K; ++k) {
@@ -206,7 +218,9 @@ void calc_diff(const Model& m, const cx* rho, cx* out, cx alpha, cx beta) {
           const int p = m.hs.p1[static_cast<size_t>(l) * K + k];
           if (p != count) {
             const cx* rp = rho + static_cast<size_t>(p) * n2;
-            for (int e = 0; e < n2; ++e) Phi[e] = Phi[e] + m.sigma[k] * rp[e];
+            const double nk = m.hs.n[static_cast<size_t>(l) * K + k];
+            const cx cp = m.sqrt_norm ? std::sqrt(nk + 1.0) * m.sigma[k] : m.sigma[k];
+            for (int e = 0; e < n2; ++e) Phi[e] = Phi[e] + cp * rp[e];
           }
         }
         for (int k = 0; k < K; ++k) {
@@ -215,7 +229,8 @@ void calc_diff(const Model& m, const cx* rho, cx* out, cx alpha, cx beta) {
           if (q != count) {
             const double nk = m.hs.n[static_cast<size_t>(l) * K + k];
             const cx* rq = rho + static_cast<size_t>(q) * n2;
-            const cx cs = nk * m.s[k], ca = -1.0 * (nk * m.a[k]);
+            const double f = m.sqrt_norm ? std::sqrt(nk) : nk;
+            const cx cs = f * m.s[k], ca = -1.0 * (f * m.a[k]);
             for (int e = 0; e < n2; ++e) {
               Phi[e] = Phi[e] + cs * rq[e];
               Psi[e] = Psi[e] + ca * rq[e];
@@ -433,6 +448,16 @@ int oracle_calc_diff(const heom_case* c, int form, const double* rho, double* dr
     (void)form;
     oracle_set_threads(n_threads);
     Model m = make_model(c);
+    if (c->col_major) {
+      // the col_major order stores every ADO column-major; the operator is the same
+      const size_t N = static_cast<size_t>(m.hs.count) * m.n2;
+      std::vector<cx> x(N), y(N);
+      transpose_ados(reinterpret_cast<const cx*>(rho), x.data(), m.n, m.hs.count);
+      transpose_ados(reinterpret_cast<const cx*>(drho), y.data(), m.n, m.hs.count);
+      calc_diff(m, x.data(), y.data(), cx{alpha[0], alpha[1]}, cx{beta[0], beta[1]});
+      transpose_ados(y.data(), reinterpret_cast<cx*>(drho), m.n, m.hs.count);
+      return 0;
+    }
     calc_diff(m, reinterpret_cast<const cx*>(rho), reinterpret_cast<cx*>(drho), cx{alpha[0], alpha[1]},
               cx{beta[0], beta[1]});
     return 0;
@@ -452,17 +477,32 @@ int oracle_solve(const heom_case* c, int form, int solver, double* rho, const do
     oracle_set_threads(n_threads);
     Model m = make_model(c);
     Integrator in(m, solver);
-    cx* r = reinterpret_cast<cx*>(rho);
     const size_t N = in.N;
+    std::vector<cx> work;
+    cx* r = reinterpret_cast<cx*>(rho);
+    if (c->col_major) {  // integrate the row-major transpose; the error norm is layout-free
+      work.resize(N);
+      transpose_ados(r, work.data(), m.n, m.hs.count);
+      r = work.data();
+    }
+    auto snap = [&](int i) {
+      if (!rho_t) return;
+      cx* dst = reinterpret_cast<cx*>(rho_t) + N * i;
+      if (c->col_major)
+        transpose_ados(r, dst, m.n, m.hs.count);
+      else
+        std::memcpy(dst, r, N * sizeof(cx));
+    };
     // solver_base::solve: callback at t_i, then one interval (solver_base.h:64-79).
     for (int i = 0; i < n_t - 1; ++i) {
-      if (rho_t) std::memcpy(rho_t + 2 * N * i, r, N * sizeof(cx));
+      snap(i);
       if (solver == 2)
         in.adaptive(r, t_list[i], t_list[i + 1], dt, atol, rtol);
       else
         in.fixed(r, t_list[i], t_list[i + 1], dt);
     }
-    if (rho_t && n_t > 0) std::memcpy(rho_t + 2 * N * (n_t - 1), r, N * sizeof(cx));
+    if (n_t > 0) snap(n_t - 1);
+    if (c->col_major) transpose_ados(r, reinterpret_cast<cx*>(rho), m.n, m.hs.count);
     if (stats) {
       stats[0] = in.st.rhs;
       stats[1] = in.st.attempts;

@@ -8,6 +8,7 @@
 //   errnrm1                       linalg_engine_eigen.h.j2:360-379
 //   gemm (matrix*ptr, ptr*matrix) linalg_engine_eigen.h.j2:381-412
 //   gemv (dense and CSR)          linalg_engine_eigen.h.j2:414-433
+//   eig / utf / utb (Redfield)    linalg_engine.h:405-483
 // plus `dense_matrix` / `sparse_matrix` containers with `import` from LIL
 // (dense_matrix_eigen.h.j2:62-80, sparse_matrix_eigen.h.j2:53-75).
 // Semantics follow BLAS: a beta of exactly zero never reads the output.
@@ -88,6 +89,19 @@ class dense_matrix<dynamic, dtype, order, loops> : public matrix_base<dynamic, d
   int rows = 0, cols = 0;
   std::vector<dtype> data;
   dtype at(int r, int c) const { return order == row_major ? data[r * cols + c] : data[c * rows + r]; }
+  dtype& ref(int r, int c) { return order == row_major ? data[r * cols + c] : data[c * rows + r]; }
+  void set_shape(int r, int c) {
+    rows = r;
+    cols = c;
+    data.assign(static_cast<size_t>(r) * c, zero<dtype>());
+  }
+  // dense -> LIL (dense_matrix_eigen.h.j2:82-100): logical entries, zeros skipped
+  void dump(lil_matrix<dynamic, dtype, order, nil>& dest) {
+    dest.set_shape(rows, cols);
+    for (int r = 0; r < rows; ++r)
+      for (int c = 0; c < cols; ++c)
+        if (at(r, c) != zero<dtype>()) dest.push(r, c, at(r, c));
+  }
   void import(lil_matrix<dynamic, dtype, order, nil>& src) {
     rows = std::get<0>(src.shape);
     cols = std::get<1>(src.shape);
@@ -182,6 +196,101 @@ struct gemv_impl<dynamic, dtype, sparse_matrix, order, loops> {
       for (int p = A.ptr[r]; p < A.ptr[r + 1]; ++p) s += A.val[p] * x[A.idx[p]];
       y[r] = beta == zero<dtype>() ? alpha * s : alpha * s + beta * y[r];
     }
+  }
+};
+
+// eig (linalg_engine.h:405-423), Hermitian A: w ascending, v[i*n + k] = component
+// i of eigenvector k (unitary).  Cyclic complex Jacobi: each rotation first
+// turns a_pq real with a phase, then applies the real symmetric 2x2 rotation.
+template <typename dtype, order_t order>
+struct eig_impl<dynamic, dtype, dense_matrix, order, loops> {
+  static void func(loops*, dense_matrix<dynamic, dtype, order, loops>& A, real_t<dtype>* w, dtype* v, int n) {
+    using R = real_t<dtype>;
+    std::vector<dtype> a(static_cast<size_t>(n) * n), u(static_cast<size_t>(n) * n, zero<dtype>());
+    for (int r = 0; r < n; ++r)
+      for (int c = 0; c < n; ++c) a[r * n + c] = A.at(r, c);
+    for (int i = 0; i < n; ++i) u[i * n + i] = one<dtype>();
+    R norm = 0;
+    for (const dtype& x : a) norm += std::norm(x);
+    for (int sweep = 0; sweep < 100; ++sweep) {
+      R off = 0;
+      for (int p = 0; p < n; ++p)
+        for (int q = p + 1; q < n; ++q) off += std::norm(a[p * n + q]);
+      if (off <= 1e-32 * norm) break;
+      for (int p = 0; p < n; ++p)
+        for (int q = p + 1; q < n; ++q) {
+          const dtype g = a[p * n + q];
+          const R ag = std::abs(g);
+          if (ag == 0) continue;
+          const dtype ph = g / ag;  // e^{i phi}
+          const R app = std::real(a[p * n + p]), aqq = std::real(a[q * n + q]);
+          const R th = (aqq - app) / (2 * ag);
+          const R t = (th >= 0 ? 1 : -1) / (std::abs(th) + std::sqrt(th * th + 1));
+          const R c = 1 / std::sqrt(t * t + 1), s = t * c;
+          // G on columns p, q: G_pp = c, G_pq = s, G_qp = -s e^{-i phi}, G_qq = c e^{-i phi}
+          const dtype em = std::conj(ph);
+          for (int k = 0; k < n; ++k) {  // A <- A G, U <- U G
+            for (dtype* m : {a.data(), u.data()}) {
+              const dtype xp = m[k * n + p], xq = m[k * n + q];
+              m[k * n + p] = c * xp - s * em * xq;
+              m[k * n + q] = s * xp + c * em * xq;
+            }
+          }
+          for (int k = 0; k < n; ++k) {  // A <- G^dagger A
+            const dtype xp = a[p * n + k], xq = a[q * n + k];
+            a[p * n + k] = c * xp - s * ph * xq;
+            a[q * n + k] = s * xp + c * ph * xq;
+          }
+        }
+    }
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](int x, int y) { return std::real(a[x * n + x]) < std::real(a[y * n + y]); });
+    for (int k = 0; k < n; ++k) {
+      w[k] = std::real(a[idx[k] * n + idx[k]]);
+      for (int i = 0; i < n; ++i) v[i * n + k] = u[i * n + idx[k]];
+    }
+  }
+};
+
+// utf (linalg_engine.h:434-453): A_v = v^dagger A v, row-major n x n.
+template <typename dtype, order_t order>
+struct utf_impl<dynamic, dtype, dense_matrix, order, loops> {
+  static void func(loops*, dense_matrix<dynamic, dtype, order, loops>& A, dtype* v, dtype* A_v, int n) {
+    std::vector<dtype> t(static_cast<size_t>(n) * n, zero<dtype>());
+    for (int a = 0; a < n; ++a)
+      for (int j = 0; j < n; ++j) {
+        dtype acc = zero<dtype>();
+        for (int b = 0; b < n; ++b) acc += A.at(a, b) * v[b * n + j];
+        t[a * n + j] = acc;
+      }
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        dtype acc = zero<dtype>();
+        for (int a = 0; a < n; ++a) acc += std::conj(v[a * n + i]) * t[a * n + j];
+        A_v[i * n + j] = acc;
+      }
+  }
+};
+
+// utb (linalg_engine.h:464-483): A = v A_v v^dagger.
+template <typename dtype, order_t order>
+struct utb_impl<dynamic, dtype, dense_matrix, order, loops> {
+  static void func(loops*, dtype* A_v, dtype* v, dense_matrix<dynamic, dtype, order, loops>& A, int n) {
+    std::vector<dtype> t(static_cast<size_t>(n) * n, zero<dtype>());
+    for (int a = 0; a < n; ++a)
+      for (int j = 0; j < n; ++j) {
+        dtype acc = zero<dtype>();
+        for (int i = 0; i < n; ++i) acc += v[a * n + i] * A_v[i * n + j];
+        t[a * n + j] = acc;
+      }
+    A.set_shape(n, n);
+    for (int a = 0; a < n; ++a)
+      for (int b = 0; b < n; ++b) {
+        dtype acc = zero<dtype>();
+        for (int j = 0; j < n; ++j) acc += t[a * n + j] * std::conj(v[b * n + j]);
+        A.ref(a, b) = acc;
+      }
   }
 };
 

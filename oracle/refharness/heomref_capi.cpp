@@ -18,6 +18,8 @@
 #include "heom_liou.h"
 #include "heom_ado.h"
 #include "hrchy_space.h"
+#include "redfield_hilb.h"
+#include "redfield_liou.h"
 #include "qme_solver.h"
 #include "solver/lsrk4.h"
 #include "solver/rk4.h"
@@ -39,12 +41,15 @@ thread_local std::string g_err;
 
 cplx C(const double* p, size_t i) { return cplx(p[2 * i], p[2 * i + 1]); }
 
-void fill_lil(lil_matrix<dynamic, cplx, row_major, nil>& m, int rows, int cols, const double* src) {
+// Logical (row, col) entries through the reference's own push(), which stores
+// them as data[row][col] (row_major) or data[col][row] (col_major).
+template <order_t order>
+void fill_lil(lil_matrix<dynamic, cplx, order, nil>& m, int rows, int cols, const double* src) {
   m.set_shape(rows, cols);
   for (int r = 0; r < rows; ++r)
     for (int c = 0; c < cols; ++c) {
       const cplx v = C(src, static_cast<size_t>(r) * cols + c);
-      if (v != cplx(0.0, 0.0)) m.data[r][c] = v;
+      if (v != cplx(0.0, 0.0)) m.push(r, c, v);
     }
 }
 
@@ -78,9 +83,38 @@ void fill_params(Q& q, const heom_case* c) {
 using hilb_t = heom_hilb<dynamic, cplx, dense_matrix, row_major, loops>;
 using liou_t = heom_liou<dynamic, cplx, sparse_matrix, row_major, row_major, loops>;
 using ado_t = heom_ado<dynamic, cplx, sparse_matrix, row_major, row_major, loops>;
+// col_major: heom_hilb only (the harness's set-up algebra covers the gemv
+// heom::set_param needs in that order, not the Liouville-space kron products)
+using hilb_c_t = heom_hilb<dynamic, cplx, dense_matrix, col_major, loops>;
+using rf_hilb_t = redfield_hilb<dynamic, cplx, dense_matrix, row_major, loops>;
+using rf_liou_t = redfield_liou<dynamic, cplx, sparse_matrix, row_major, row_major, loops>;
+
+void check_normalisation(const heom_case* c) {
+#ifdef LIBHEOM_SQRT_NORMALIZATION
+  const int built_sqrt = 1;
+#else
+  const int built_sqrt = 0;
+#endif
+  // the normalisation is the reference's compile-time switch: one build per choice
+  if (c->sqrt_normalization != built_sqrt)
+    throw std::invalid_argument("this reference build has the other normalisation");
+}
+
+std::unique_ptr<qme_base<cplx, col_major, loops>> make_qme_c(int form, const heom_case* c, int threads, loops* eng,
+                                                             int* n_hrchy) {
+  check_normalisation(c);
+  if (form != 0) throw std::invalid_argument("col_major: heom_hilb only in this harness");
+  auto q = std::make_unique<hilb_c_t>(c->max_depth, 1, threads);
+  fill_params(*q, c);
+  q->set_param(eng);
+  *n_hrchy = q->get_n_hrchy();
+  return q;
+}
 
 std::unique_ptr<qme_base<cplx, row_major, loops>> make_qme(int form, const heom_case* c, int threads,
                                                              loops* eng, int* n_hrchy) {
+  check_normalisation(c);
+  if (c->col_major) throw std::invalid_argument("make_qme: row_major model expected");
   if (form == 0) {
     auto q = std::make_unique<hilb_t>(c->max_depth, 1, threads);
     fill_params(*q, c);
@@ -99,8 +133,59 @@ std::unique_ptr<qme_base<cplx, row_major, loops>> make_qme(int form, const heom_
     q->set_param(eng);
     *n_hrchy = q->get_n_hrchy();
     return q;
+  } else if (form == 3) {  // redfield_hilb (redfield_hilb.h:18-91): no hierarchy
+    auto q = std::make_unique<rf_hilb_t>();
+    fill_params(*q, c);
+    q->set_param(eng);
+    *n_hrchy = 1;
+    return q;
+  } else if (form == 4) {  // redfield_liou (redfield_liou.h:18-104)
+    auto q = std::make_unique<rf_liou_t>();
+    fill_params(*q, c);
+    q->set_param(eng);
+    *n_hrchy = 1;
+    return q;
   }
   throw std::invalid_argument("unknown form");
+}
+
+template <class Q>
+void diff_with(Q* q, loops* eng, const double* rho, double* drho, const double* alpha, const double* beta) {
+  const int size = q->main_size();
+  const int tsize = std::max(1, q->temp_size());
+  std::vector<cplx> x(size), y(size), temp(tsize);
+  std::memcpy(x.data(), rho, sizeof(cplx) * size);
+  std::memcpy(y.data(), drho, sizeof(cplx) * size);
+  q->calc_diff_impl(eng, y.data(), x.data(), cplx(alpha[0], alpha[1]), cplx(beta[0], beta[1]), temp.data());
+  std::memcpy(drho, y.data(), sizeof(cplx) * size);
+}
+
+template <order_t order>
+void solve_with(qme_base<cplx, order, loops>* q, loops* eng, int solver, double* rho, const double* t_list, int n_t,
+                double dt, double atol, double rtol, double* rho_t) {
+  const int size = q->main_size();
+  std::unique_ptr<solver_base<cplx, order, loops>> s;
+  if (solver == 0)
+    s = std::make_unique<rk4<cplx, order, loops>>();
+  else if (solver == 1)
+    s = std::make_unique<lsrk4<cplx, order, loops>>();
+  else if (solver == 2)
+    s = std::make_unique<rkdp<cplx, order, loops>>();
+  else
+    throw std::invalid_argument("unknown solver");
+  qme_solver<cplx, order, loops> qs(eng, q, s.get());
+  kwargs_t kw;
+  kw["dt"] = dt;
+  kw["atol"] = atol;
+  kw["rtol"] = rtol;
+  cplx* r = reinterpret_cast<cplx*>(rho);
+  int idx = 0;
+  qs.solve(r, t_list, n_t,
+           [&](double) {
+             if (rho_t) std::memcpy(rho_t + 2 * static_cast<size_t>(idx) * size, r, sizeof(cplx) * size);
+             ++idx;
+           },
+           kw);
 }
 
 }  // namespace
@@ -149,6 +234,11 @@ int heomref_calc_diff(const heom_case* c, int form, const double* rho, double* d
   try {
     loops eng;
     int nh = 0;
+    if (c->col_major) {
+      auto q = make_qme_c(form, c, n_threads, &eng, &nh);
+      diff_with(q.get(), &eng, rho, drho, alpha, beta);
+      return 0;
+    }
     auto q = make_qme(form, c, n_threads, &eng, &nh);
     const int size = q->main_size();
     const int tsize = std::max(1, q->temp_size());
@@ -172,30 +262,13 @@ int heomref_solve(const heom_case* c, int form, int solver, double* rho, const d
   try {
     loops eng;
     int nh = 0;
-    auto q = make_qme(form, c, n_threads, &eng, &nh);
-    const int size = q->main_size();
-    std::unique_ptr<solver_base<cplx, row_major, loops>> s;
-    if (solver == 0)
-      s = std::make_unique<rk4<cplx, row_major, loops>>();
-    else if (solver == 1)
-      s = std::make_unique<lsrk4<cplx, row_major, loops>>();
-    else if (solver == 2)
-      s = std::make_unique<rkdp<cplx, row_major, loops>>();
-    else
-      throw std::invalid_argument("unknown solver");
-    qme_solver<cplx, row_major, loops> qs(&eng, q.get(), s.get());
-    kwargs_t kw;
-    kw["dt"] = dt;
-    kw["atol"] = atol;
-    kw["rtol"] = rtol;
-    cplx* r = reinterpret_cast<cplx*>(rho);
-    int idx = 0;
-    qs.solve(r, t_list, n_t,
-             [&](double) {
-               if (rho_t) std::memcpy(rho_t + 2 * static_cast<size_t>(idx) * size, r, sizeof(cplx) * size);
-               ++idx;
-             },
-             kw);
+    if (c->col_major) {
+      auto q = make_qme_c(form, c, n_threads, &eng, &nh);
+      solve_with<col_major>(q.get(), &eng, solver, rho, t_list, n_t, dt, atol, rtol, rho_t);
+    } else {
+      auto q = make_qme(form, c, n_threads, &eng, &nh);
+      solve_with<row_major>(q.get(), &eng, solver, rho, t_list, n_t, dt, atol, rtol, rho_t);
+    }
     return 0;
   } catch (std::exception& e) {
     g_err = e.what();

@@ -8,9 +8,13 @@
 //   axpym (heom_liou.h:96-99, heom_ado.h:336-337) linalg_engine_nil.h.j2:38-56
 //   gemm  (heom_liou.h:91, Xi = -s_delta Phi^2)   linalg_engine_nil.h.j2:59-96
 //   kron_x_1 / kron_1_x_T (heom_liou.h:72-87)     linalg_engine_nil.h.j2:197-299
-// Only the row-major orders are provided (the order the oracle instantiates).
+//   dotu / gevm / lu_solve (redfield.h:32-41,66-73) linalg_engine_nil.h.j2:467-533
+// The row-major orders are provided, and the col-major gemv that heom_hilb's
+// set-up needs in that order.
 #ifndef HEOMREF_SHIM_LINALG_ENGINE_NIL_H
 #define HEOMREF_SHIM_LINALG_ENGINE_NIL_H
+
+#include <vector>
 
 #include "env.h"
 #include "linalg_engine/linalg_engine.h"
@@ -25,6 +29,17 @@ struct gemv_impl<dynamic, dtype, lil_matrix, row_major, nil> {
     for (int r = 0; r < n; ++r) y[r] *= beta;
     for (const auto& row : A.data)
       for (const auto& e : row.second) y[row.first] += alpha * e.second * x[e.first];
+  }
+};
+
+// col_major LIL stores A(r, c) as data[c][r] (lil_matrix.h.j2:156-163).
+template <typename dtype>
+struct gemv_impl<dynamic, dtype, lil_matrix, col_major, nil> {
+  static void func(nil*, dtype alpha, lil_matrix<dynamic, dtype, col_major, nil>& A,
+                   dtype* x, dtype beta, dtype* y, int n) {
+    for (int r = 0; r < n; ++r) y[r] *= beta;
+    for (const auto& col : A.data)
+      for (const auto& e : col.second) y[e.first] += alpha * e.second * x[col.first];
   }
 };
 
@@ -107,6 +122,61 @@ struct kron_1_x_T_impl<dynamic, dtype, lil_matrix, row_major, row_major, nil> {
     }
   }
 };
+
+// dotu (linalg_engine.h:207-217): sum_i x_i y_i (no conjugation).
+template <typename dtype>
+struct dotu_impl<dynamic, dtype, nil> {
+  static dtype func(nil*, dtype* x, dtype* y, int n) {
+    dtype acc = zero<dtype>();
+    for (int i = 0; i < n; ++i) acc += x[i] * y[i];
+    return acc;
+  }
+};
+
+// gevm (linalg_engine.h:374-394): y = alpha x^T A + beta y.
+template <typename dtype>
+struct gevm_impl<dynamic, dtype, lil_matrix, row_major, nil> {
+  static void func(nil*, dtype alpha, dtype* x, lil_matrix<dynamic, dtype, row_major, nil>& A, dtype beta,
+                   dtype* y, int n) {
+    std::vector<dtype> out(n, zero<dtype>());
+    for (const auto& row : A.data)
+      for (const auto& e : row.second) out[e.first] += x[row.first] * e.second;
+    for (int i = 0; i < n; ++i) y[i] = (beta == zero<dtype>() ? zero<dtype>() : beta * y[i]) + alpha * out[i];
+  }
+};
+
+// lu_solve (the reference's nil engine, linalg_engine_nil.h.j2:467-533): x
+// with A x = b by Gaussian elimination with partial pivoting (the Redfield
+// correlation's (gamma - i omega) x = phi_0).
+template <typename dtype>
+void lu_solve(const lil_matrix<dynamic, dtype, row_major, nil>& A, const std::vector<dtype>& b,
+              std::vector<dtype>& x) {
+  const int n = std::get<0>(A.shape);
+  std::vector<dtype> m(static_cast<size_t>(n) * n, zero<dtype>());
+  for (const auto& row : A.data)
+    for (const auto& e : row.second) m[row.first * n + e.first] = e.second;
+  x.assign(b.begin(), b.end());
+  for (int i = 0; i < n; ++i) {
+    int piv = i;
+    for (int r = i + 1; r < n; ++r)
+      if (std::abs(m[r * n + i]) > std::abs(m[piv * n + i])) piv = r;
+    if (piv != i) {
+      for (int c = 0; c < n; ++c) std::swap(m[i * n + c], m[piv * n + c]);
+      std::swap(x[i], x[piv]);
+    }
+    for (int r = i + 1; r < n; ++r) {
+      if (m[r * n + i] == zero<dtype>()) continue;
+      const dtype f = m[r * n + i] / m[i * n + i];
+      for (int c = i; c < n; ++c) m[r * n + c] -= f * m[i * n + c];
+      x[r] -= f * x[i];
+    }
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    dtype acc = x[i];
+    for (int c = i + 1; c < n; ++c) acc -= m[i * n + c] * x[c];
+    x[i] = acc / m[i * n + i];
+  }
+}
 
 }  // namespace libheom
 

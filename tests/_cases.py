@@ -58,7 +58,8 @@ def projector_case(seed=6, n=4, depth=3) -> HeomParams:
 
 
 def params_to_dict(p: HeomParams) -> dict:
-    d = dict(H=p.H, V=np.array(p.V), s_delta=np.array(p.s_delta, complex), max_depth=np.array(p.max_depth))
+    d = dict(H=p.H, V=np.array(p.V), s_delta=np.array(p.s_delta, complex), max_depth=np.array(p.max_depth),
+             normalization=np.array(p.normalization), order=np.array(p.order))
     for u in range(p.n_noise):
         d[f"gamma_{u}"] = p.gamma[u]
         d[f"phi_0_{u}"] = p.phi_0[u]
@@ -74,4 +75,6 @@ def params_from_npz(z) -> HeomParams:
     return HeomParams(H=z["H"], V=V, gamma=[z[f"gamma_{u}"] for u in range(U)],
                       phi_0=[z[f"phi_0_{u}"] for u in range(U)], sigma=[z[f"sigma_{u}"] for u in range(U)],
                       S=[z[f"S_{u}"] for u in range(U)], A=[z[f"A_{u}"] for u in range(U)],
-                      s_delta=list(z["s_delta"]), max_depth=int(z["max_depth"]))
+                      s_delta=list(z["s_delta"]), max_depth=int(z["max_depth"]),
+                      normalization=str(z["normalization"]) if "normalization" in z.files else "integer",
+                      order=str(z["order"]) if "order" in z.files else "row_major")

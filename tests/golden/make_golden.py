@@ -45,14 +45,14 @@ def hrchy_fixture(ref: oracle.Oracle):
     np.savez_compressed(os.path.join(HERE, "hrchy.npz"), **out)
 
 
-def diff_fixture(ref, name, p: HeomParams, seed):
+def diff_fixture(ref, name, p: HeomParams, seed, forms=("hilb", "liou", "ado")):
     rng = np.random.default_rng(seed)
     shape = (p.n_hrchy(), p.n_level, p.n_level)
     rho = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
     drho = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
     alpha, beta = 0.7 - 0.2j, 0.3 + 0.1j
     out = dict(params_to_dict(p), rho=rho, drho=drho, alpha=np.array(alpha), beta=np.array(beta))
-    for form in ("hilb", "liou", "ado"):
+    for form in forms:
         out[f"out_{form}"] = ref.calc_diff(p, rho, drho, alpha, beta, form=form, threads=4)
         out[f"out0_{form}"] = ref.calc_diff(p, rho, None, 1.0, 0.0, form=form, threads=4)
     np.savez_compressed(os.path.join(HERE, f"diff_{name}.npz"), **out)
@@ -66,6 +66,37 @@ def solve_fixture(ref, name, p: HeomParams, solver, t_list, dt, atol=1e-8, rtol=
         out[f"rho_t_{form}"] = ref.solve(p, rho0, t_list, solver=solver, dt=dt, atol=atol, rtol=rtol, form=form,
                                          threads=4)
     np.savez_compressed(os.path.join(HERE, f"solve_{name}.npz"), **out)
+
+
+def sqrt_fixtures():
+    """The reference built with LIBHEOM_SQRT_NORMALIZATION on the same cases."""
+    import dataclasses
+    ref = oracle.Oracle("ref_sqrt")
+    sq = lambda p: dataclasses.replace(p, normalization="sqrt")
+    diff_fixture(ref, "generic_sqrt", sq(generic_case()), 31)
+    diff_fixture(ref, "spin_boson_sqrt", sq(configs.spin_boson(depth=4)), 33)
+    solve_fixture(ref, "spin_boson_rk4_sqrt", sq(configs.spin_boson()), "rk4", [0.0, 0.25, 0.5], 0.005,
+                  forms=("hilb", "liou", "ado"))
+    solve_fixture(ref, "exciton7_rkdp_sqrt", sq(configs.exciton_7site(depth=2)), "rkdp", [0.0, 10.0, 20.0], 0.1,
+                  atol=1e-8, rtol=1e-8)
+
+
+def col_major_fixtures(ref):
+    """heom_hilb instantiated with the reference's col_major order (ADOs stored
+    column-major); the harness provides that order's set-up algebra for
+    heom_hilb only."""
+    import dataclasses
+    cm = lambda p: dataclasses.replace(p, order="col_major")
+    diff_fixture(ref, "generic_colmajor", cm(generic_case()), 41, forms=("hilb",))
+    diff_fixture(ref, "spin_boson_colmajor", cm(configs.spin_boson(depth=4)), 43, forms=("hilb",))
+    solve_fixture(ref, "spin_boson_rkdp_colmajor", cm(configs.spin_boson(eps=0.4)), "rkdp", [0.0, 0.5, 1.0], 0.01,
+                  atol=1e-8, rtol=1e-6)
+    g = cm(generic_case())
+    rng = np.random.default_rng(22)
+    r0 = np.zeros((g.n_hrchy(), g.n_level, g.n_level), complex)
+    v = rng.standard_normal(g.n_level) + 1j * rng.standard_normal(g.n_level)
+    r0[0] = np.outer(v, v.conj()).T / np.vdot(v, v).real   # column-major storage of |v><v|
+    solve_fixture(ref, "generic_rk4_colmajor", g, "rk4", [0.0, 0.1, 0.2], 0.01, rho0=r0)
 
 
 def main():
@@ -91,6 +122,8 @@ def main():
     solve_fixture(ref, "generic_rk4", g, "rk4", [0.0, 0.1, 0.2], 0.01, forms=("hilb", "liou", "ado"), rho0=r0)
     solve_fixture(ref, "generic_rkdp", g, "rkdp", [0.0, 0.2, 0.4], 0.02, atol=1e-9, rtol=1e-7, rho0=r0)
     solve_fixture(ref, "generic_lsrk4", g, "lsrk4", [0.0, 0.1, 0.2], 0.01, rho0=r0)
+    sqrt_fixtures()
+    col_major_fixtures(ref)
     print("fixtures written to", HERE)
 
 

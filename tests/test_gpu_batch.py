@@ -90,3 +90,20 @@ def test_range_guard_splits_mixed_batch():
         r1 = ps[k].rho0_ground().ravel().copy()
         lh.qme_solver(q1, lh.rk4()).solve(r1, [0.0, 0.05, 0.1], None, {"dt": 0.005})
         assert np.abs(rho[off[k]:off[k + 1]] - r1).max() <= tol * max(1.0, np.abs(r1).max())
+
+
+def test_col_major_batch_matches_row_major():
+    """A batch of col_major models (ADOs stored column-major at the boundary)
+    equals the row-major batch on the transposed states."""
+    import dataclasses
+    ps = sample_instances(3, 2)
+    row, _ = run_batch(ps, "fp64", t=(0.0, 0.1))
+    cm = [dataclasses.replace(p, order="col_major") for p in ps]
+    qmes = [lh.from_params(p) for p in cm]
+    bs = lh.batch_solver(qmes, lh.rk4())
+    rho = np.concatenate([p.rho0_ground().transpose(0, 2, 1).ravel() for p in cm])
+    bs.solve(rho, [0.0, 0.1], None, {"dt": 0.005})
+    off = bs.offsets()
+    for i, p in enumerate(cm):
+        got = rho[off[i]:off[i + 1]].reshape(p.n_hrchy(), p.n_level, p.n_level).transpose(0, 2, 1)
+        assert np.abs(got - row[i]).max() <= 1e-13 * max(1.0, np.abs(row[i]).max())

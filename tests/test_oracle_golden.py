@@ -49,6 +49,8 @@ def test_calc_diff_matches_reference(port, path):
     z = np.load(path)
     p = params_from_npz(z)
     for form in ("hilb", "liou", "ado"):
+        if f"out_{form}" not in z.files:   # col_major fixtures hold heom_hilb only
+            continue
         got = port.calc_diff(p, z["rho"], z["drho"], complex(z["alpha"]), complex(z["beta"]), form=form)
         ref = z[f"out_{form}"]
         scale = np.abs(ref).max()

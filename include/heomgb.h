@@ -34,8 +34,17 @@ typedef enum heomgb_status {
 } heomgb_status;
 
 /* Model forms: heom_hilb (heom_hilb.h:18-216), heom_liou (heom_liou.h:18-259),
- * heom_ado (heom_ado.h:18-204). */
-typedef enum heomgb_form { HEOMGB_HILB = 0, HEOMGB_LIOU = 1, HEOMGB_ADO = 2 } heomgb_form;
+ * heom_ado (heom_ado.h:18-204); and the Redfield models redfield_hilb
+ * (redfield_hilb.h:18-91) and redfield_liou (redfield_liou.h:18-104), built
+ * from the same H and noise members (redfield.h:42-173; max_depth is ignored,
+ * the state is one n x n matrix, main_size() = n^2). */
+typedef enum heomgb_form {
+  HEOMGB_HILB = 0,
+  HEOMGB_LIOU = 1,
+  HEOMGB_ADO = 2,
+  HEOMGB_REDFIELD_HILB = 3,
+  HEOMGB_REDFIELD_LIOU = 4
+} heomgb_form;
 
 /* Integrators: rk4 (solver/rk4.h:15-66), lsrk4 (solver/lsrk4.h:15-48),
  * rkdp (solver/rkdp.h:15-180). */

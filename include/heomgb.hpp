@@ -168,6 +168,16 @@ using heom_hilb = heom_model<HEOMGB_HILB>;
 using heom_liou = heom_model<HEOMGB_LIOU>;
 using heom_ado = heom_model<HEOMGB_ADO>;
 
+// redfield_hilb() / redfield_liou() -- redfield_hilb.h:36-37, redfield_liou.h:38-39
+template <heomgb_form Form>
+class redfield_model : public qme_base {
+ public:
+  redfield_model() = default;
+  void set_param(void* /*engine*/ = nullptr) { build(Form, 0, 1, 1); }
+};
+using redfield_hilb = redfield_model<HEOMGB_REDFIELD_HILB>;
+using redfield_liou = redfield_model<HEOMGB_REDFIELD_LIOU>;
+
 class solver_base {
  public:
   explicit solver_base(heomgb_solver_kind k) { check(heomgb_solver_create(k, &h_)); }

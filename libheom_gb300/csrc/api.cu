@@ -345,6 +345,138 @@ void require(bool c, const char* msg) {
 }
 
 // ------------------------------------------------------------------ set_param
+// ------------------------------------------------------------------ Redfield set-up
+// Eigen-decomposition of a Hermitian matrix by cyclic Jacobi rotations:
+// U^dagger A U = diag(w); U row-major, column k the k-th eigenvector.  Each
+// rotation makes a_pq real with a phase factor on column q, then applies the
+// real 2x2 rotation that zeroes it.
+void hermitian_eigen(std::vector<cd> A, int n, std::vector<double>& w, std::vector<cd>& U) {
+  U.assign(static_cast<size_t>(n) * n, cd(0.0, 0.0));
+  for (int i = 0; i < n; ++i) U[static_cast<size_t>(i) * n + i] = cd(1.0, 0.0);
+  auto at = [&](std::vector<cd>& M, int r, int c) -> cd& { return M[static_cast<size_t>(r) * n + c]; };
+  double total = 0.0;
+  for (const cd& x : A) total += std::norm(x);
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) off += std::norm(at(A, p, q));
+    if (off <= 1e-32 * total) break;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const cd apq = at(A, p, q);
+        const double mag = std::abs(apq);
+        if (mag == 0.0) continue;
+        const cd phase = apq / mag;
+        const double diff = at(A, q, q).real() - at(A, p, p).real();
+        const double theta = diff / (2.0 * mag);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (std::abs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        const cd pc = std::conj(phase);
+        for (int k = 0; k < n; ++k) {  // columns p, q of A and U
+          const cd ap = at(A, k, p), aq = at(A, k, q);
+          at(A, k, p) = c * ap - sn * pc * aq;
+          at(A, k, q) = sn * ap + c * pc * aq;
+          const cd up = at(U, k, p), uq = at(U, k, q);
+          at(U, k, p) = c * up - sn * pc * uq;
+          at(U, k, q) = sn * up + c * pc * uq;
+        }
+        for (int k = 0; k < n; ++k) {  // rows p, q of A
+          const cd ap = at(A, p, k), aq = at(A, q, k);
+          at(A, p, k) = c * ap - sn * phase * aq;
+          at(A, q, k) = sn * ap + c * phase * aq;
+        }
+      }
+  }
+  w.resize(n);
+  for (int i = 0; i < n; ++i) w[i] = at(A, i, i).real();
+}
+
+// x with M x = b (k x k, row-major), Gaussian elimination with partial pivoting.
+std::vector<cd> solve_dense(std::vector<cd> M, int k, std::vector<cd> b) {
+  for (int i = 0; i < k; ++i) {
+    int piv = i;
+    for (int r = i + 1; r < k; ++r)
+      if (std::abs(M[static_cast<size_t>(r) * k + i]) > std::abs(M[static_cast<size_t>(piv) * k + i])) piv = r;
+    if (M[static_cast<size_t>(piv) * k + i] == cd(0.0, 0.0)) throw arg_error("Redfield: singular gamma - i omega");
+    if (piv != i) {
+      for (int c = 0; c < k; ++c) std::swap(M[static_cast<size_t>(i) * k + c], M[static_cast<size_t>(piv) * k + c]);
+      std::swap(b[i], b[piv]);
+    }
+    for (int r = i + 1; r < k; ++r) {
+      const cd f = M[static_cast<size_t>(r) * k + i] / M[static_cast<size_t>(i) * k + i];
+      if (f == cd(0.0, 0.0)) continue;
+      for (int c = i; c < k; ++c) M[static_cast<size_t>(r) * k + c] -= f * M[static_cast<size_t>(i) * k + c];
+      b[r] -= f * b[i];
+    }
+  }
+  for (int i = k - 1; i >= 0; --i) {
+    cd acc = b[i];
+    for (int c = i + 1; c < k; ++c) acc -= M[static_cast<size_t>(i) * k + c] * b[c];
+    b[i] = acc / M[static_cast<size_t>(i) * k + i];
+  }
+  return b;
+}
+
+// Redfield operators of every bath (redfield.h:32-41, 101-173): in the
+// eigenbasis of H, Lambda_ij = V_ij C(w_j - w_i) with the bath correlation
+// C(omega) = sigma^T (S + iA) (gamma - i omega)^-1 phi_0 + s_delta (the full
+// gamma, off-diagonal entries included); back-transformed, concatenated.
+void redfield_lambda(const heomgb_qme* q, std::vector<cd>& lam, std::vector<cd>& lamd) {
+  const int n = q->n, n2 = n * n;
+  for (int a = 0; a < n; ++a)
+    for (int b = 0; b < n; ++b)
+      if (std::abs(q->H[static_cast<size_t>(a) * n + b] - std::conj(q->H[static_cast<size_t>(b) * n + a])) >
+          1e-12 * (1.0 + std::abs(q->H[static_cast<size_t>(a) * n + b])))
+        throw unsupported_error("Redfield models need a Hermitian H");
+  std::vector<double> w;
+  std::vector<cd> U;
+  hermitian_eigen(q->H, n, w, U);
+  lam.assign(static_cast<size_t>(q->U) * n2, cd(0.0, 0.0));
+  lamd.assign(static_cast<size_t>(q->U) * n2, cd(0.0, 0.0));
+  const cd I(0.0, 1.0);
+  for (int u = 0; u < q->U; ++u) {
+    const Bath& bt = q->baths[u];
+    const int L = bt.len;
+    std::vector<cd> stc(L, cd(0.0, 0.0));  // sigma^T (S + iA)
+    for (int j = 0; j < L; ++j)
+      for (int k = 0; k < L; ++k)
+        stc[k] += bt.sigma[j] * (bt.S[static_cast<size_t>(j) * L + k] + I * bt.A[static_cast<size_t>(j) * L + k]);
+    auto corr = [&](double omega) {
+      std::vector<cd> M(bt.gamma.begin(), bt.gamma.end());
+      for (int k = 0; k < L; ++k) M[static_cast<size_t>(k) * L + k] -= I * omega;
+      const std::vector<cd> x = L > 0 ? solve_dense(M, L, bt.phi0) : std::vector<cd>();
+      cd acc = bt.sdelta;
+      for (int k = 0; k < L; ++k) acc += stc[k] * x[k];
+      return acc;
+    };
+    // Vv = U^dagger V U, then Lambda_v = Vv o C(w_j - w_i), Lambda = U Lambda_v U^dagger
+    std::vector<cd> T(n2, cd(0.0, 0.0)), Vv(n2, cd(0.0, 0.0)), Lv(n2), T2(n2, cd(0.0, 0.0));
+    for (int a = 0; a < n; ++a)
+      for (int j = 0; j < n; ++j)
+        for (int b = 0; b < n; ++b) T[a * n + j] += bt.V[static_cast<size_t>(a) * n + b] * U[static_cast<size_t>(b) * n + j];
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j)
+        for (int a = 0; a < n; ++a) Vv[i * n + j] += std::conj(U[static_cast<size_t>(a) * n + i]) * T[a * n + j];
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) Lv[i * n + j] = Vv[i * n + j] * corr(w[j] - w[i]);
+    for (int a = 0; a < n; ++a)
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) T2[a * n + j] += U[static_cast<size_t>(a) * n + i] * Lv[i * n + j];
+    cd* Lu = lam.data() + static_cast<size_t>(u) * n2;
+    cd* LDu = lamd.data() + static_cast<size_t>(u) * n2;
+    for (int a = 0; a < n; ++a)
+      for (int b = 0; b < n; ++b) {
+        cd acc(0.0, 0.0);
+        for (int j = 0; j < n; ++j) acc += T2[a * n + j] * std::conj(U[static_cast<size_t>(b) * n + j]);
+        Lu[a * n + b] = acc;
+      }
+    for (int a = 0; a < n; ++a)
+      for (int b = 0; b < n; ++b) LDu[a * n + b] = std::conj(Lu[b * n + a]);
+  }
+}
+
+bool is_redfield(int form) { return form == HEOMGB_REDFIELD_HILB || form == HEOMGB_REDFIELD_LIOU; }
+
 void build_model(heomgb_qme* q) {
   if (q->n <= 0) throw state_error("set_param: Hamiltonian not set");
   if (q->U < 0) throw state_error("set_param: alloc_noises not called");
@@ -492,7 +624,18 @@ void build_model(heomgb_qme* q) {
   m.a_f = q->arena.upload(to_f2(av), s);
   m.sdelta_f = q->arena.upload(to_f2(sdelta), s);
 
-  if (q->form == HEOMGB_HILB) {
+  if (is_redfield(q->form)) {
+    // redfield_hilb and redfield_liou apply the same operator; one kernel serves both
+    q->path = PATH_REDFIELD;
+    if (rhs_smem_bytes(m, PATH_REDFIELD, false) > 200 * 1024)
+      throw unsupported_error("Redfield path supports n_level <= 66");
+    std::vector<cd> lam, lamd;
+    redfield_lambda(q, lam, lamd);
+    m.lam = q->arena.upload(to_d2(lam), s);
+    m.lam_f = q->arena.upload(to_f2(lam), s);
+    m.lamd = q->arena.upload(to_d2(lamd), s);
+    m.lamd_f = q->arena.upload(to_f2(lamd), s);
+  } else if (q->form == HEOMGB_HILB) {
     q->path = diag ? PATH_DIAG : PATH_GENERAL;
   } else {
     q->path = PATH_LIOU;
@@ -1138,11 +1281,11 @@ heomgb_status heomgb_qme_create(heomgb_form form, int max_depth, int n_inner_thr
   (void)n_outer_threads;
   return guard([&] {
     require(out != nullptr, "null out");
-    require(form == HEOMGB_HILB || form == HEOMGB_LIOU || form == HEOMGB_ADO, "unknown form");
+    require(form == HEOMGB_HILB || form == HEOMGB_LIOU || form == HEOMGB_ADO || is_redfield(form), "unknown form");
     require(max_depth >= 0, "max_depth must be >= 0");
     auto q = std::make_unique<heomgb_qme>();
     q->form = form;
-    q->max_depth = max_depth;
+    q->max_depth = is_redfield(form) ? 0 : max_depth;  // Redfield: one n x n state, no hierarchy
     ck(cudaGetDevice(&q->device), "cudaGetDevice");
     ck(cudaDeviceGetAttribute(&q->n_sm, cudaDevAttrMultiProcessorCount, q->device), "device attribute");
     ck(cudaStreamCreateWithFlags(&q->own_stream, cudaStreamNonBlocking), "stream create");

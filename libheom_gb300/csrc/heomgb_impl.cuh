@@ -72,6 +72,11 @@ struct RhsModel {
   const float2* s_f;
   const float2* a_f;
   const float2* sdelta_f;
+  // Redfield path: Lambda_u and Lambda_u^dagger (U*n2 each, redfield.h:101-173)
+  const double2* lam;
+  const float2* lam_f;
+  const double2* lamd;
+  const float2* lamd_f;
   // Liouville path: CSR superoperators (n2 x n2): R_0 = L + sum_u Xi_u, Phi_u, Psi_u
   const int* r0_ptr;                // n2+1
   const int* r0_idx;
@@ -109,7 +114,7 @@ struct Stage {
   double* partials;          // EPI_DP7 per-CTA partial sums
 };
 
-enum Path : int { PATH_DIAG = 0, PATH_GENERAL = 1, PATH_LIOU = 2 };
+enum Path : int { PATH_DIAG = 0, PATH_GENERAL = 1, PATH_LIOU = 2, PATH_REDFIELD = 3 };
 
 // One instance of the diagonal-coupling kernel: a model's sizes, where its
 // elements start in the (possibly concatenated) state vector, and its tables.

@@ -863,6 +863,74 @@ __global__ void __launch_bounds__(256) k_rhs_liou(const RhsModel m, const Stage 
   if (st.kind == EPI_DP7) dp7_finish(st, local, static_cast<long long>(m.n_hrchy) * n2);
 }
 
+// ------------------------------------------------------------------ RHS, Redfield
+// redfield_hilb (redfield_hilb.h:66-89): one n x n state,
+//   D = i[H, rho] + sum_u [V_u, Lambda_u rho - rho Lambda_u^dagger],
+// with Lambda_u the Redfield operator of bath u built at set-up.  One CTA; the
+// products run from shared memory; the stage epilogue is the solvers' own.
+template <typename TC, typename TB>
+__global__ void __launch_bounds__(256) k_rhs_redfield(const RhsModel m, const Stage st) {
+  using C = cx_t<TC>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double dt;
+  int cur;
+  if (!stage_prologue(st, dt, cur)) return;
+  const TB* __restrict__ y = stage_input<TB>(st, cur);
+  const int n = m.n, n2 = m.n2;
+  C* ys = reinterpret_cast<C*>(smem_raw);
+  C* Dm = ys + n2;
+  C* T = Dm + n2;
+  const C* __restrict__ H = pick<TC>(m.H, m.H_f);
+  const C* __restrict__ Vall = pick<TC>(m.V, m.V_f);
+  const C* __restrict__ Lall = pick<TC>(m.lam, m.lam_f);
+  const C* __restrict__ LDall = pick<TC>(m.lamd, m.lamd_f);
+  double local = 0.0;
+  if (blockIdx.x == 0) {
+    for (int e = threadIdx.x; e < n2; e += blockDim.x) ys[e] = ldc<TC>(y + e);
+    __syncthreads();
+    for (int e = threadIdx.x; e < n2; e += blockDim.x) {  // i[H, rho]
+      const int a = e / n, b = e - a * n;
+      C acc = cx<TC>(0, 0), neg = cx<TC>(0, 0);
+      for (int c = 0; c < n; ++c) {
+        cfma(acc, H[a * n + c], ys[c * n + b]);
+        cfma(neg, ys[a * n + c], H[c * n + b]);
+      }
+      Dm[e] = cx<TC>(-(acc.y - neg.y), acc.x - neg.x);
+    }
+    for (int u = 0; u < m.U; ++u) {
+      const C* V = Vall + static_cast<size_t>(u) * n2;
+      const C* L = Lall + static_cast<size_t>(u) * n2;
+      const C* LD = LDall + static_cast<size_t>(u) * n2;
+      __syncthreads();
+      for (int e = threadIdx.x; e < n2; e += blockDim.x) {  // T = Lambda rho - rho Lambda^dagger
+        const int a = e / n, b = e - a * n;
+        C acc = cx<TC>(0, 0), neg = cx<TC>(0, 0);
+        for (int c = 0; c < n; ++c) {
+          cfma(acc, L[a * n + c], ys[c * n + b]);
+          cfma(neg, ys[a * n + c], LD[c * n + b]);
+        }
+        T[e] = cx<TC>(acc.x - neg.x, acc.y - neg.y);
+      }
+      __syncthreads();
+      for (int e = threadIdx.x; e < n2; e += blockDim.x) {  // D += [V, T]
+        const int a = e / n, b = e - a * n;
+        C acc = cx<TC>(0, 0), neg = cx<TC>(0, 0);
+        for (int c = 0; c < n; ++c) {
+          cfma(acc, V[a * n + c], T[c * n + b]);
+          cfma(neg, T[a * n + c], V[c * n + b]);
+        }
+        C D = Dm[e];
+        D.x += acc.x - neg.x;
+        D.y += acc.y - neg.y;
+        Dm[e] = D;
+      }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n2; e += blockDim.x) local += epilogue<TC>(st, static_cast<size_t>(e), Dm[e], dt, cur);
+  }
+  if (st.kind == EPI_DP7) dp7_finish(st, local, static_cast<long long>(n2));
+}
+
 // ------------------------------------------------------------------ launch configuration
 int rhs_block_size(const RhsModel& m, int path) {
   if (path != PATH_DIAG) {
@@ -874,8 +942,8 @@ int rhs_block_size(const RhsModel& m, int path) {
 }
 
 int rhs_grid_size(const RhsModel& m, int path, int block, int n_sm) {
-  (void)path;
   (void)block;
+  if (path == PATH_REDFIELD) return 1;
   const int per_sm = 4;
   return static_cast<int>(std::min<long long>(m.n_hrchy, static_cast<long long>(n_sm) * per_sm * 4));
 }
@@ -884,6 +952,7 @@ size_t rhs_smem_bytes(const RhsModel& m, int path, bool mixed) {
   const size_t cb = mixed ? sizeof(float2) : sizeof(double2);
   if (path == PATH_GENERAL) return 5 * cb * m.n2;
   if (path == PATH_LIOU) return 4 * cb * m.n2;
+  if (path == PATH_REDFIELD) return 3 * cb * m.n2;
   return 0;
 }
 
@@ -918,6 +987,13 @@ static cudaError_t launch_typed(const RhsModel& m, const DiagSet* ds, const Stag
       if (e != cudaSuccess) return e;
     }
     k_rhs_general<TC, TB><<<grid, block, smem, s>>>(m, st);
+  } else if (path == PATH_REDFIELD) {
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(k_rhs_redfield<TC, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(smem));
+      if (e != cudaSuccess) return e;
+    }
+    k_rhs_redfield<TC, TB><<<1, block, smem, s>>>(m, st);
   } else {
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(k_rhs_liou<TC, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -27,7 +27,7 @@ import numpy as np
 from . import _lib
 from ._lib import CALLBACK, Kwargs, check
 
-_FORMS = {"hilb": 0, "liou": 1, "ado": 2}
+_FORMS = {"hilb": 0, "liou": 1, "ado": 2, "redfield_hilb": 3, "redfield_liou": 4}
 _PRECISION = {"fp64": 0, "mixed": 1}
 
 
@@ -201,6 +201,25 @@ class heom_liou(heom):
 class heom_ado(heom):
     """ADO-space HEOM: one global block-sparse generator (heom_ado.h:18-204)."""
     form = "ado"
+
+
+class _redfield(heom):
+    """Redfield models (redfield.h:21-173): the same H and noise members, no
+    hierarchy; the state is one n x n matrix.  The constructor takes no depth
+    (redfield_hilb() in the reference); thread-count arguments are accepted."""
+
+    def __init__(self, *args, **kwargs):
+        super().__init__(0)
+
+
+class redfield_hilb(_redfield):
+    """Hilbert-space Redfield (redfield_hilb.h:18-91)."""
+    form = "redfield_hilb"
+
+
+class redfield_liou(_redfield):
+    """Liouville-space Redfield (redfield_liou.h:18-104)."""
+    form = "redfield_liou"
 
 
 class solver_base:
@@ -454,7 +473,8 @@ class batch_solver:
 
 def from_params(p, form: str = "hilb", precision: str = "fp64", stream=None) -> heom:
     """Build and set up a model from a HeomParams."""
-    cls = {"hilb": heom_hilb, "liou": heom_liou, "ado": heom_ado}[form]
+    cls = {"hilb": heom_hilb, "liou": heom_liou, "ado": heom_ado, "redfield_hilb": redfield_hilb,
+           "redfield_liou": redfield_liou}[form]
     q = cls(p.max_depth, 1, 1)
     q.n_level = p.n_level
     q.n_level_2 = p.n_level ** 2

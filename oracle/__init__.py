@@ -33,7 +33,18 @@ class _Case(ctypes.Structure):
                 ("H", ctypes.c_void_p), ("V", ctypes.c_void_p), ("len_gamma", ctypes.c_void_p),
                 ("gamma", ctypes.c_void_p), ("phi_0", ctypes.c_void_p), ("sigma", ctypes.c_void_p),
                 ("S", ctypes.c_void_p), ("A", ctypes.c_void_p), ("s_delta", ctypes.c_void_p),
-                ("sqrt_normalization", ctypes.c_int), ("col_major", ctypes.c_int)]
+                ("sqrt_normalization", ctypes.c_int), ("col_major", ctypes.c_int),
+                ("hrchy_filter", ctypes.c_void_p), ("filter_user", ctypes.c_void_p)]
+
+# int filter(const int* index, int n_dim, int depth, void* user): nonzero keeps
+FILTER = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int, ctypes.c_void_p)
+
+
+def make_filter(fn):
+    """ctypes callback of fn(index: list[int], depth: int) -> bool (None: no filter)."""
+    if fn is None:
+        return None
+    return FILTER(lambda idx, n_dim, depth, _u: 1 if fn([idx[i] for i in range(n_dim)], depth) else 0)
 
 
 class PackedCase:
@@ -56,6 +67,9 @@ class PackedCase:
                             ptr(self.gamma), ptr(self.phi_0), ptr(self.sigma), ptr(self.S), ptr(self.A),
                             ptr(self.s_delta), 1 if getattr(p, "normalization", "integer") == "sqrt" else 0,
                             1 if getattr(p, "order", "row_major") == "col_major" else 0)
+        self.filter = make_filter(getattr(p, "hrchy_filter", None))  # kept alive with the struct
+        if self.filter is not None:
+            self.struct.hrchy_filter = ctypes.cast(self.filter, ctypes.c_void_p)
 
 
 def build(which: str = "port") -> None:
@@ -104,15 +118,24 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"oracle ({self.which}) failed: {self._err().decode()}")
 
-    def hrchy(self, n_dim: int, max_depth: int):
+    def hrchy(self, n_dim: int, max_depth: int, hrchy_filter=None):
+        """Hierarchy tables (n, ptr_p1, ptr_m1); hrchy_filter(index, depth) -> bool
+        enables the reference's filter_flag."""
         cnt = ctypes.c_int(0)
-        self._check(self._hrchy(n_dim, max_depth, ctypes.byref(cnt), None, None, None))
+        if hrchy_filter is None:
+            call = lambda *tabs: self._hrchy(n_dim, max_depth, ctypes.byref(cnt), *tabs)
+        else:
+            f = make_filter(hrchy_filter)
+            fn = getattr(self.lib, self._pre + "hrchy_filtered")
+            fn.argtypes = [ctypes.c_int, ctypes.c_int, FILTER, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
+                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+            call = lambda *tabs: fn(n_dim, max_depth, f, None, ctypes.byref(cnt), *tabs)
+        self._check(call(None, None, None))
         c = cnt.value
         n = np.zeros((c, n_dim), dtype=np.int32)
         p1 = np.zeros((c + 1, n_dim), dtype=np.int32)
         m1 = np.zeros((c + 1, n_dim), dtype=np.int32)
-        self._check(self._hrchy(n_dim, max_depth, ctypes.byref(cnt), n.ctypes.data, p1.ctypes.data,
-                                m1.ctypes.data))
+        self._check(call(n.ctypes.data, p1.ctypes.data, m1.ctypes.data))
         return n, p1, m1
 
     def calc_diff(self, params, rho, drho=None, alpha=1.0, beta=0.0, form="hilb", threads=0):

@@ -27,6 +27,10 @@ typedef struct heom_case {
   const double* s_delta; /* U complex                                       */
   int sqrt_normalization; /* 1: LIBHEOM_SQRT_NORMALIZATION (heom_hilb.h:140-196) */
   int col_major;          /* 1: the `col_major` order: each ADO stored column-major */
+  /* hrchy_filter of alloc_hrchy_space (hrchy_space.h:29-36) with filter_flag
+   * true when non-null: nonzero keeps the candidate multi-index */
+  int (*hrchy_filter)(const int* index, int n_dim, int depth, void* user);
+  void* filter_user;
 } heom_case;
 
 /* form: 0 = heom_hilb, 1 = heom_liou (CSR superoperators), 2 = heom_ado.

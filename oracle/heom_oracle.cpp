@@ -59,10 +59,15 @@ struct Hierarchy {
   std::vector<int> p1, m1;  // (count+1)*K, sentinel = count
 };
 
+using Filter = int (*)(const int*, int, int, void*);
+
 // Breadth-first enumeration: a multi-index only spawns children by raising
 // modes at or after the one it was created by, so each index is made once;
-// the FIFO queue yields tier order (src/hrchy_space.cc:160-198).
-Hierarchy build_hierarchy(int K, int depth) {
+// the FIFO queue yields tier order (src/hrchy_space.cc:160-198).  With a
+// filter, a candidate enters only if the filter accepts it (filter_flag,
+// src/hrchy_space.cc:182-191), so a rejected index also drops the subtree it
+// would have spawned.
+Hierarchy build_hierarchy(int K, int depth, Filter filter = nullptr, void* user = nullptr) {
   Hierarchy h;
   h.K = K;
   h.depth = depth;
@@ -79,7 +84,7 @@ Hierarchy build_hierarchy(int K, int depth) {
     if (tier + 1 > depth) continue;
     for (int k = first_mode; k < K; ++k) {
       ++idx[k];
-      pending.push({idx, k});
+      if (!filter || filter(idx.data(), K, tier + 1, user)) pending.push({idx, k});
       --idx[k];
     }
   }
@@ -155,7 +160,7 @@ Model make_model(const heom_case* c) {
     off2 += static_cast<size_t>(L) * L;
   }
   m.K = static_cast<int>(m.bath_of.size());
-  m.hs = build_hierarchy(m.K, c->max_depth);
+  m.hs = build_hierarchy(m.K, c->max_depth, c->hrchy_filter, c->filter_user);
   // ngamma_diag[l] = sum_k n_k gamma_kk, accumulated mode by mode (heom.h:94-104).
   m.ngamma.assign(m.hs.count, cx{0, 0});
   for (int l = 0; l < m.hs.count; ++l) {
@@ -414,6 +419,21 @@ int oracle_set_threads(int n) {
 #endif
 }
 
+int oracle_hrchy_filtered(int n_dim, int max_depth, Filter filter, void* user, int* n_hrchy, int* n_tab, int* p1_tab,
+                          int* m1_tab) {
+  try {
+    Hierarchy h = build_hierarchy(n_dim, max_depth, filter, user);
+    *n_hrchy = h.count;
+    if (n_tab) std::copy(h.n.begin(), h.n.end(), n_tab);
+    if (p1_tab) std::copy(h.p1.begin(), h.p1.end(), p1_tab);
+    if (m1_tab) std::copy(h.m1.begin(), h.m1.end(), m1_tab);
+    return 0;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
 int oracle_hrchy(int n_dim, int max_depth, int* n_hrchy, int* n_tab, int* p1_tab, int* m1_tab) {
   try {
     Hierarchy h = build_hierarchy(n_dim, max_depth);
@@ -433,7 +453,7 @@ int oracle_n_hrchy(const heom_case* c, int* n_hrchy) {
     check_case(c);
     int K = 0;
     for (int u = 0; u < c->n_noise; ++u) K += c->len_gamma[u];
-    *n_hrchy = build_hierarchy(K, c->max_depth).count;
+    *n_hrchy = build_hierarchy(K, c->max_depth, c->hrchy_filter, c->filter_user).count;
     return 0;
   } catch (std::exception& e) {
     g_err = e.what();

@@ -8,6 +8,7 @@
 #include <any>
 #include <cstring>
 #include <exception>
+#include <iostream>
 #include <memory>
 #include <string>
 
@@ -201,6 +202,31 @@ int heomref_hrchy(int n_dim, int max_depth, int* n_hrchy, int* n_tab, int* p1_ta
     hrchy_space hs;
     hs.n_dim = n_dim;
     const int count = alloc_hrchy_space(hs, max_depth);
+    *n_hrchy = count;
+    for (int l = 0; l <= count; ++l)
+      for (int k = 0; k < n_dim; ++k) {
+        if (n_tab && l < count) n_tab[static_cast<size_t>(l) * n_dim + k] = hs.n[l][k];
+        if (p1_tab) p1_tab[static_cast<size_t>(l) * n_dim + k] = hs.ptr_p1[l][k];
+        if (m1_tab) m1_tab[static_cast<size_t>(l) * n_dim + k] = hs.ptr_m1[l][k];
+      }
+    return 0;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+}
+
+// alloc_hrchy_space with a hierarchy filter and filter_flag = true
+// (hrchy_space.cc:137-231); heom::set_param never passes one (heom.h:80-91).
+int heomref_hrchy_filtered(int n_dim, int max_depth, int (*filter)(const int*, int, int, void*), void* user,
+                           int* n_hrchy, int* n_tab, int* p1_tab, int* m1_tab) {
+  try {
+    hrchy_space hs;
+    hs.n_dim = n_dim;
+    auto f = [&](std::vector<int> index, int depth) -> bool { return filter(index.data(), n_dim, depth, user) != 0; };
+    std::streambuf* keep = std::cerr.rdbuf(nullptr);  // the reference warns on stderr at max_depth
+    const int count = alloc_hrchy_space(hs, max_depth, [](int, int) {}, 1024, f, true);
+    std::cerr.rdbuf(keep);
     *n_hrchy = count;
     for (int l = 0; l <= count; ++l)
       for (int k = 0; k < n_dim; ++k) {

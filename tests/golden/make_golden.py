@@ -99,6 +99,34 @@ def col_major_fixtures(ref):
     solve_fixture(ref, "generic_rk4_colmajor", g, "rk4", [0.0, 0.1, 0.2], 0.01, rho0=r0)
 
 
+def redfield_fixtures(ref):
+    """The reference's redfield_hilb / redfield_liou (no hierarchy: one n x n state)."""
+    import dataclasses
+    forms = ("redfield_hilb", "redfield_liou")
+    for name, p, seed in [("spin_boson", configs.spin_boson(eps=0.4, depth=0), 51),
+                          ("exciton7", configs.exciton_7site(depth=0), 52),
+                          ("generic", dataclasses.replace(generic_case(), max_depth=0), 53)]:
+        rng = np.random.default_rng(seed)
+        n = p.n_level
+        rho = rng.standard_normal((1, n, n)) + 1j * rng.standard_normal((1, n, n))
+        drho = rng.standard_normal((1, n, n)) + 1j * rng.standard_normal((1, n, n))
+        alpha, beta = 0.7 - 0.2j, 0.3 + 0.1j
+        out = dict(params_to_dict(p), rho=rho, drho=drho, alpha=np.array(alpha), beta=np.array(beta))
+        for form in forms:
+            out[f"out_{form}"] = ref.calc_diff(p, rho, drho, alpha, beta, form=form, threads=1)
+        np.savez_compressed(os.path.join(HERE, f"redfield_diff_{name}.npz"), **out)
+    for name, p, solver, t_list, dt in [
+            ("spin_boson_rk4", configs.spin_boson(eps=0.4, depth=0), "rk4", [0.0, 1.0, 2.0], 0.005),
+            ("exciton7_rkdp", configs.exciton_7site(depth=0), "rkdp", [0.0, 50.0, 100.0], 0.1)]:
+        rho0 = p.rho0_ground()
+        out = dict(params_to_dict(p), rho0=rho0, t_list=np.asarray(t_list, float), dt=np.array(dt),
+                   atol=np.array(1e-8), rtol=np.array(1e-8), solver=np.array(solver))
+        for form in forms:
+            out[f"rho_t_{form}"] = ref.solve(p, rho0, t_list, solver=solver, dt=dt, atol=1e-8, rtol=1e-8, form=form,
+                                             threads=1)
+        np.savez_compressed(os.path.join(HERE, f"redfield_solve_{name}.npz"), **out)
+
+
 def main():
     oracle.build("ref")
     ref = oracle.Oracle("ref")
@@ -124,6 +152,7 @@ def main():
     solve_fixture(ref, "generic_lsrk4", g, "lsrk4", [0.0, 0.1, 0.2], 0.01, rho0=r0)
     sqrt_fixtures()
     col_major_fixtures(ref)
+    redfield_fixtures(ref)
     print("fixtures written to", HERE)
 
 

@@ -115,6 +115,15 @@ heomgb_status heomgb_qme_set_normalization(heomgb_qme* q, heomgb_normalization n
  * The device keeps row-major ADOs and transposes at the boundary. */
 typedef enum heomgb_order { HEOMGB_ROW_MAJOR = 0, HEOMGB_COL_MAJOR = 1 } heomgb_order;
 heomgb_status heomgb_qme_set_order(heomgb_qme* q, heomgb_order order);
+/* Hierarchy filter: alloc_hrchy_space's hrchy_filter with filter_flag = true
+ * (hrchy_space.h:29-36, hrchy_space.cc:182-191; heom::set_param passes none,
+ * heom.h:80-91).  At set_param the filter is called, on the host, for every
+ * candidate multi-index (n_dim ints) of total `depth` whose parent was kept, in
+ * the reference's breadth-first order; nonzero keeps it.  A rejected index
+ * takes the indices it would have spawned with it.  NULL: no filter (the
+ * default).  Not with the learned terminator. */
+typedef int (*heomgb_hrchy_filter)(const int* index, int n_dim, int depth, void* user);
+heomgb_status heomgb_qme_set_hrchy_filter(heomgb_qme* q, heomgb_hrchy_filter filter, void* user);
 /* Precision after set_param (no reference counterpart: the reference has one
  * compile-time precision).  A MIXED request runs with FP64 arithmetic
  * (effective = FP64) when the bath expansion makes FP32 arithmetic unsafe.

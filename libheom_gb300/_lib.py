@@ -19,6 +19,8 @@ c_int_p = ctypes.POINTER(ctypes.c_int)
 c_ll_p = ctypes.POINTER(ctypes.c_longlong)
 c_double_p = ctypes.POINTER(ctypes.c_double)
 CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_double, ctypes.c_void_p)
+HRCHY_FILTER = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int,
+                                ctypes.c_void_p)
 
 
 class Kwargs(ctypes.Structure):
@@ -49,6 +51,7 @@ SIGNATURES = {
     "heomgb_qme_set_precision": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "heomgb_qme_set_normalization": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "heomgb_qme_set_order": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "heomgb_qme_set_hrchy_filter": (ctypes.c_int, [ctypes.c_void_p, HRCHY_FILTER, ctypes.c_void_p]),
     "heomgb_qme_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "heomgb_qme_get_precision": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_double_p, c_double_p]),
     "heomgb_qme_set_param": (ctypes.c_int, [ctypes.c_void_p]),

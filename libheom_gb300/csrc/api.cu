@@ -266,6 +266,8 @@ struct heomgb_qme {
   int precision = HEOMGB_FP64;       // requested
   int sqrt_norm = 0;                 // HEOMGB_NORM_SQRT
   int col_major = 0;                 // HEOMGB_COL_MAJOR: ADOs stored column-major at the boundary
+  heomgb_hrchy_filter filter = nullptr;  // hierarchy filter (alloc_hrchy_space's filter_flag)
+  void* filter_user = nullptr;
   double2* tx = nullptr;             // col_major transposes of calc_diff (in scratch)
   double2* ty = nullptr;
   int precision_eff = HEOMGB_FP64;   // in use: a MIXED request falls back to FP64 under the range guard
@@ -477,6 +479,53 @@ void redfield_lambda(const heomgb_qme* q, std::vector<cd>& lam, std::vector<cd>&
 
 bool is_redfield(int form) { return form == HEOMGB_REDFIELD_HILB || form == HEOMGB_REDFIELD_LIOU; }
 
+// Hierarchy filter (alloc_hrchy_space with filter_flag, hrchy_space.cc:
+// 182-191).  In the breadth-first build every multi-index is spawned by its
+// canonical parent n - 1_k, k its last nonzero mode; a candidate the filter
+// rejects never enters and spawns nothing.  So an ADO survives when its parent
+// survives and the filter accepts it, and the survivors keep their relative
+// order.  Walking the full tables in rank order calls the filter on exactly
+// the candidates, in the order, that the reference's build does.  The tables
+// are then compacted and the +-1 links remapped (void where a neighbour is gone).
+void filter_hierarchy(heomgb_qme* q, int K, int nh_full, cudaStream_t s, int*& nidx, int*& p1, int*& m1, int& nh) {
+  std::vector<int> n_h(static_cast<size_t>(nh_full) * K), p1_h(static_cast<size_t>(nh_full + 1) * K),
+      m1_h(static_cast<size_t>(nh_full + 1) * K);
+  ck(cudaMemcpyAsync(n_h.data(), nidx, sizeof(int) * n_h.size(), cudaMemcpyDeviceToHost, s), "tables out");
+  ck(cudaMemcpyAsync(p1_h.data(), p1, sizeof(int) * p1_h.size(), cudaMemcpyDeviceToHost, s), "tables out");
+  ck(cudaMemcpyAsync(m1_h.data(), m1, sizeof(int) * m1_h.size(), cudaMemcpyDeviceToHost, s), "tables out");
+  ck(cudaStreamSynchronize(s), "tables sync");
+  std::vector<int> rank(nh_full, -1);
+  int cnt = 0;
+  rank[0] = cnt++;
+  for (int l = 1; l < nh_full; ++l) {
+    const int* row = n_h.data() + static_cast<size_t>(l) * K;
+    int kmax = K - 1, depth = 0;
+    while (row[kmax] == 0) --kmax;
+    for (int k = 0; k < K; ++k) depth += row[k];
+    const int parent = m1_h[static_cast<size_t>(l) * K + kmax];
+    if (rank[parent] < 0) continue;
+    if (q->filter(row, K, depth, q->filter_user)) rank[l] = cnt++;
+  }
+  nh = cnt;
+  std::vector<int> n_c(static_cast<size_t>(nh) * K), p1_c(static_cast<size_t>(nh + 1) * K, nh),
+      m1_c(static_cast<size_t>(nh + 1) * K, nh);
+  for (int l = 0; l < nh_full; ++l) {
+    const int r = rank[l];
+    if (r < 0) continue;
+    for (int k = 0; k < K; ++k) {
+      const size_t src = static_cast<size_t>(l) * K + k, dst = static_cast<size_t>(r) * K + k;
+      n_c[dst] = n_h[src];
+      const int a = p1_h[src], b = m1_h[src];
+      p1_c[dst] = a < nh_full && rank[a] >= 0 ? rank[a] : nh;
+      m1_c[dst] = b < nh_full && rank[b] >= 0 ? rank[b] : nh;
+    }
+  }
+  nidx = q->arena.upload(n_c, s);
+  p1 = q->arena.upload(p1_c, s);
+  m1 = q->arena.upload(m1_c, s);
+  ck(cudaStreamSynchronize(s), "filtered tables");
+}
+
 void build_model(heomgb_qme* q) {
   if (q->n <= 0) throw state_error("set_param: Hamiltonian not set");
   if (q->U < 0) throw state_error("set_param: alloc_noises not called");
@@ -552,8 +601,27 @@ void build_model(heomgb_qme* q) {
   if (count > INT_MAX - 1) throw arg_error("hierarchy too large: more than 2^31-2 ADOs");
   if (static_cast<long long>(n2) * count > (1LL << 40)) throw arg_error("state vector too large");
   q->K = K;
-  q->n_hrchy = static_cast<int>(count);
-  const int nh = q->n_hrchy;
+  const int nh_full = static_cast<int>(count);
+
+  // hierarchy tables on the device (hrchy_space.cc:137-231)
+  DeviceArena full_tables;  // the unfiltered tables when a filter compacts them
+  DeviceArena& ta = q->filter ? full_tables : q->arena;
+  int* nidx = static_cast<int*>(ta.alloc(sizeof(int) * std::max<size_t>(1, static_cast<size_t>(nh_full) * K)));
+  int* p1 = static_cast<int*>(ta.alloc(sizeof(int) * std::max<size_t>(1, static_cast<size_t>(nh_full + 1) * K)));
+  int* m1 = static_cast<int*>(ta.alloc(sizeof(int) * std::max<size_t>(1, static_cast<size_t>(nh_full + 1) * K)));
+  if (K > 0) {
+    const int bd = K + q->max_depth + 2;
+    std::vector<long long> bt(static_cast<size_t>(bd) * bd);
+    for (int a = 0; a < bd; ++a)
+      for (int b = 0; b < bd; ++b) bt[static_cast<size_t>(a) * bd + b] = binom_sat(a, b);
+    DeviceArena tmp;
+    long long* dbt = tmp.upload(bt, s);
+    ck(launch_hrchy_build(K, q->max_depth, nh_full, dbt, bd, nidx, p1, m1, s), "hierarchy build");
+    ck(cudaStreamSynchronize(s), "hierarchy build sync");
+  }
+  int nh = nh_full;
+  if (q->filter && K > 0) filter_hierarchy(q, K, nh_full, s, nidx, p1, m1, nh);
+  q->n_hrchy = nh;
 
   RhsModel& m = q->dm;
   m = RhsModel{};
@@ -562,21 +630,6 @@ void build_model(heomgb_qme* q) {
   m.K = K;
   m.U = U;
   m.n_hrchy = nh;
-
-  // hierarchy tables on the device (hrchy_space.cc:137-231)
-  int* nidx = static_cast<int*>(q->arena.alloc(sizeof(int) * std::max<size_t>(1, static_cast<size_t>(nh) * K)));
-  int* p1 = static_cast<int*>(q->arena.alloc(sizeof(int) * std::max<size_t>(1, static_cast<size_t>(nh + 1) * K)));
-  int* m1 = static_cast<int*>(q->arena.alloc(sizeof(int) * std::max<size_t>(1, static_cast<size_t>(nh + 1) * K)));
-  if (K > 0) {
-    const int bd = K + q->max_depth + 2;
-    std::vector<long long> bt(static_cast<size_t>(bd) * bd);
-    for (int a = 0; a < bd; ++a)
-      for (int b = 0; b < bd; ++b) bt[static_cast<size_t>(a) * bd + b] = binom_sat(a, b);
-    DeviceArena tmp;
-    long long* dbt = tmp.upload(bt, s);
-    ck(launch_hrchy_build(K, q->max_depth, nh, dbt, bd, nidx, p1, m1, s), "hierarchy build");
-    ck(cudaStreamSynchronize(s), "hierarchy build sync");
-  }
   m.p1 = p1;
   m.m1 = m1;
   m.nidx = nidx;
@@ -1373,6 +1426,15 @@ heomgb_status heomgb_qme_set_precision(heomgb_qme* q, heomgb_precision p) {
   });
 }
 
+heomgb_status heomgb_qme_set_hrchy_filter(heomgb_qme* q, heomgb_hrchy_filter filter, void* user) {
+  return guard([&] {
+    require(q != nullptr, "null qme");
+    if (q->live_solvers > 0) throw state_error("set_hrchy_filter: destroy the qme_solvers of this model first");
+    q->filter = filter;
+    q->filter_user = user;
+  });
+}
+
 heomgb_status heomgb_qme_set_order(heomgb_qme* q, heomgb_order order) {
   return guard([&] {
     require(q != nullptr, "null qme");
@@ -1424,6 +1486,7 @@ heomgb_status heomgb_qme_set_terminator(heomgb_qme* q, heomgb_mlp* mlp) {
     if (mlp) {
       if (q->path != PATH_DIAG) throw unsupported_error("the learned terminator needs diagonal couplings V (heom_hilb)");
       if (q->sqrt_norm) throw unsupported_error("the learned terminator is trained for the integer normalisation");
+      if (q->filter) throw unsupported_error("the learned terminator needs the complete truncated tier (no filter)");
       int din = 0, h = 0, dout = 0;
       mlp_dims(mlp, &din, &h, &dout);
       const int n2 = q->n * q->n;

@@ -60,6 +60,9 @@ class heom:
         self.normalization = "integer"
         # storage of every ADO in the caller's state arrays: the reference's `order`
         self.order = "row_major"
+        # hrchy_filter(index: list[int], depth: int) -> bool, the filter of
+        # alloc_hrchy_space (hrchy_space.h:29-36); None: the full hierarchy
+        self.hrchy_filter = None
         self.stream = None  # optional cudaStream_t handle (int)
         self._h = ctypes.c_void_p()
         self._lib = _lib.load()
@@ -109,6 +112,11 @@ class heom:
         check(lib.heomgb_qme_set_precision(h, _PRECISION[self.precision]))
         check(lib.heomgb_qme_set_normalization(h, {"integer": 0, "sqrt": 1}[self.normalization]))
         check(lib.heomgb_qme_set_order(h, {"row_major": 0, "col_major": 1}[self.order]))
+        if self.hrchy_filter is not None:
+            fn = self.hrchy_filter
+            self._filter_cb = _lib.HRCHY_FILTER(lambda idx, k, depth, _u: 1 if fn([idx[i] for i in range(k)], depth)
+                                                else 0)
+            check(lib.heomgb_qme_set_hrchy_filter(h, self._filter_cb, None))
         if self.stream:
             check(lib.heomgb_qme_set_stream(h, ctypes.c_void_p(int(self.stream))))
         check(lib.heomgb_qme_set_param(h))
@@ -492,6 +500,7 @@ def from_params(p, form: str = "hilb", precision: str = "fp64", stream=None) -> 
     q.precision = precision
     q.normalization = p.normalization
     q.order = p.order
+    q.hrchy_filter = p.hrchy_filter
     q.stream = stream
     q.set_param()
     return q

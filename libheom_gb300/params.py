@@ -31,6 +31,8 @@ class HeomParams:
     normalization: str = "integer"
     # storage of every ADO in the state vector: the reference's `order`
     order: str = "row_major"
+    # hrchy_filter(index, depth) -> bool of alloc_hrchy_space; None: full hierarchy
+    hrchy_filter: object = None
 
     def __post_init__(self):
         self.H = np.ascontiguousarray(self.H, dtype=np.complex128)
@@ -78,7 +80,9 @@ class HeomParams:
 
     def n_hrchy(self) -> int:
         from math import comb
-        return comb(self.n_modes + self.max_depth, self.max_depth)
+        if self.hrchy_filter is None:
+            return comb(self.n_modes + self.max_depth, self.max_depth)
+        return len(hierarchy_indices(self.n_modes, self.max_depth, self.hrchy_filter))
 
     def rho0_ground(self) -> np.ndarray:
         """|0><0| in the system block, zero auxiliary ADOs."""
@@ -86,3 +90,21 @@ class HeomParams:
         rho = np.zeros((self.n_hrchy(), n, n), dtype=np.complex128)
         rho[0, 0, 0] = 1.0
         return rho
+
+
+def hierarchy_indices(n_dim: int, max_depth: int, hrchy_filter=None):
+    """Multi-indices in the reference's breadth-first order (hrchy_space.cc:
+    160-198), with the optional filter applied to each candidate."""
+    from collections import deque
+    out, pending = [], deque([((0,) * n_dim, 0)])
+    while pending:
+        idx, first = pending.popleft()
+        out.append(idx)
+        depth = sum(idx)
+        if depth + 1 > max_depth:
+            continue
+        for k in range(first, n_dim):
+            child = idx[:k] + (idx[k] + 1,) + idx[k + 1:]
+            if hrchy_filter is None or hrchy_filter(list(child), depth + 1):
+                pending.append((child, k))
+    return out

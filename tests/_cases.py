@@ -78,3 +78,17 @@ def params_from_npz(z) -> HeomParams:
                       s_delta=list(z["s_delta"]), max_depth=int(z["max_depth"]),
                       normalization=str(z["normalization"]) if "normalization" in z.files else "integer",
                       order=str(z["order"]) if "order" in z.files else "row_major")
+
+
+# Hierarchy filters (alloc_hrchy_space's hrchy_filter, filter_flag on) used by
+# the golden fixtures and the tests: name -> (n_dim, max_depth, filter).
+def _weighted(idx, depth):
+    w = [1, 2, 1, 3, 1, 2]
+    return sum(a * b for a, b in zip(idx, w)) <= 5
+
+
+FILTERS = {
+    "weighted": (5, 4, _weighted),
+    "cap0": (4, 6, lambda idx, depth: idx[0] <= 2 and depth <= 5),
+    "nonmonotone": (6, 5, lambda idx, depth: idx[5] == 0 or idx[0] > 0),
+}

@@ -25,7 +25,7 @@ from libheom_gb300 import configs  # noqa: E402
 from libheom_gb300.params import HeomParams  # noqa: E402
 
 sys.path.insert(0, os.path.dirname(HERE))
-from _cases import generic_case, projector_case, params_to_dict  # noqa: E402
+from _cases import FILTERS, generic_case, projector_case, params_to_dict  # noqa: E402
 
 
 def hrchy_fixture(ref: oracle.Oracle):
@@ -127,6 +127,15 @@ def redfield_fixtures(ref):
         np.savez_compressed(os.path.join(HERE, f"redfield_solve_{name}.npz"), **out)
 
 
+def filter_fixture(ref):
+    """alloc_hrchy_space with the filters of tests/_cases.py (filter_flag on)."""
+    out = {}
+    for name, (K, N, f) in FILTERS.items():
+        n, p1, m1 = ref.hrchy(K, N, f)
+        out[f"n_{name}"], out[f"p1_{name}"], out[f"m1_{name}"] = n, p1, m1
+    np.savez_compressed(os.path.join(HERE, "hrchy_filtered.npz"), **out)
+
+
 def main():
     oracle.build("ref")
     ref = oracle.Oracle("ref")
@@ -153,6 +162,7 @@ def main():
     sqrt_fixtures()
     col_major_fixtures(ref)
     redfield_fixtures(ref)
+    filter_fixture(ref)
     print("fixtures written to", HERE)
 
 

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import oracle
-from _cases import params_from_npz
+from _cases import FILTERS, params_from_npz
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
 
@@ -74,3 +74,17 @@ def test_solve_matches_reference(port, path):
         # relative to the largest element of each ADO (deep tiers are tiny)
         scale = np.abs(ref).max(axis=(2, 3), keepdims=True) + 1e-300
         assert (np.abs(got - ref) / scale).max() <= 1e-10, form
+
+
+@pytest.mark.parametrize("name", sorted(FILTERS))
+def test_filtered_hierarchy_matches_reference(port, name):
+    """The port's breadth-first build with a hierarchy filter against the
+    reference's alloc_hrchy_space with filter_flag on."""
+    z = np.load(os.path.join(GOLD, "hrchy_filtered.npz"))
+    K, N, f = FILTERS[name]
+    n, p1, m1 = port.hrchy(K, N, f)
+    assert np.array_equal(n, z[f"n_{name}"])
+    assert np.array_equal(p1, z[f"p1_{name}"])
+    assert np.array_equal(m1, z[f"m1_{name}"])
+    from libheom_gb300.params import hierarchy_indices
+    assert [tuple(r) for r in n] == hierarchy_indices(K, N, f)

@@ -12,7 +12,8 @@ Hamiltonian.  The chosen form is mixed precision (FP32 bulk products, FP64
 state / accumulation / error norm / step control); its final state is
 checked against the FP64 path (max |delta rho| <= 1e-6), and the FP64 plain
 form is timed beside it.  Other workloads: --workload spin_boson | batched |
-aggregate24.
+aggregate24 | exciton7_ensemble (16 disorder realisations of the 7-site
+aggregate in one batch, RK4 dt = 1 fs).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -40,6 +41,9 @@ WORKLOADS = {
                     cpu_sample_instances=24),
     "aggregate24": dict(maker="aggregate_24site", solver="lsrk4", t_final=1000.0, kw=dict(dt=0.5),
                         cpu_sample_t=0.5),
+    # 16 disorder realisations of the 7-site aggregate in one batch (RK4: batches take fixed steps)
+    "exciton7_ensemble": dict(maker="exciton_7site_ensemble", solver="rk4", t_final=1000.0, kw=dict(dt=1.0),
+                              cpu_sample_t=20.0, cpu_sample_instances=1),
 }
 L2_FLUSH_BYTES = 512 << 20
 
@@ -152,7 +156,12 @@ class Workload:
         maker = getattr(configs, self.wl["maker"])
         # a batched sweep gives every rank its own seeded shard (weak scaling);
         # a single model is replicated
-        made = maker(seed=shard_seed(2, rank)) if self.wl["maker"] == "batched_sweep" else maker()
+        if self.wl["maker"] == "batched_sweep":
+            made = maker(seed=shard_seed(2, rank))
+        elif self.wl["maker"] == "exciton_7site_ensemble":
+            made = maker(seed=1 + 16 * rank)
+        else:
+            made = maker()
         self.ps = made if isinstance(made, list) else [made]
         self.batched = len(self.ps) > 1
         self.n_hrchy = sum(p.n_hrchy() for p in self.ps)

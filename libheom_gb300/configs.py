@@ -71,9 +71,10 @@ def exciton_7site(seed=1, depth=4) -> HeomParams:
                       dict(solver="rkdp", dt=0.1, atol=1e-8, rtol=1e-8, t_final=1000.0))
 
 
-def aggregate_24site(seed=3, depth=3) -> HeomParams:
+def aggregate_24site(seed=3, depth=3, n_sites=24) -> HeomParams:
+    """Random aggregate (24 sites unless n_sites says otherwise)."""
     rng = np.random.default_rng(seed)
-    n = 24
+    n = n_sites
     eps = rng.normal(0.0, 200.0, n)
     J = rng.uniform(-50.0, 50.0, (n, n))
     J = np.triu(J, 1)
@@ -112,3 +113,9 @@ def batched_sweep(seed=2, n_spin_boson=768, n_chain=256):
         depth = int(rng.integers(4, 9))
         out.append(chain_4level(J, eps, depth))
     return out
+
+
+def exciton_7site_ensemble(seed=1, count=16, depth=4):
+    """Static-disorder ensemble of the 7-site aggregate: `count` seeded
+    Hamiltonians (seeds seed .. seed+count-1), the same baths."""
+    return [exciton_7site(seed=seed + i, depth=depth) for i in range(count)]

@@ -192,6 +192,12 @@ heomgb_status heomgb_qme_solver_main_size(const heomgb_qme_solver* qs, long long
  * instead of searching, for reproducible profiles. */
 heomgb_status heomgb_qme_solver_tuning(const heomgb_qme_solver* qs, int* block, int* elems_per_thread,
                                        int* n_tiles, int* min_blocks);
+/* 1 when the autotuner put the mixed form's commutators [H, rho] on the
+ * tensor cores (3xTF32 tcgen05 MMAs with tensor-memory accumulators; real
+ * symmetric H, n_level in {8, 12, 16, 24, 32}), else 0.  HEOMGB_TILE=tc pins
+ * that variant, HEOMGB_TCORE=0 keeps it out of the search.  No reference
+ * counterpart: the reference evaluates every term on CUDA cores. */
+heomgb_status heomgb_qme_solver_tensor_cores(const heomgb_qme_solver* qs, int* on);
 
 /* qme_solver::solve(rho, t_list, n_t, callback, kwargs) -- qme_solver.h:44-52,
  * solver_base.h:64-79.  rho: host array of main_size() complex, updated in

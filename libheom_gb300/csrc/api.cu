@@ -216,24 +216,49 @@ struct DiagPlan {
   DeviceArena arena;
   DiagSet ds{};
   int block = 128, ept = 4, grid = 1, min_blocks = 1;
+  bool tcore = false;  // commutators on the tensor cores (k_rhs_diag_tc)
 };
 
+// Whether an instance can take the tensor-core commutator: mixed form, a
+// micro-tiled n_state whose operands fit (n in {8, 12, 16, 24, 32}), real
+// symmetric H, no terminator.
+bool tcore_eligible(const DiagInst& I, bool mixed) {
+  const bool mt4 = (I.n & 3) == 0 && I.n >= 8;
+  return mixed && mt4 && I.n <= 32 && I.n != 20 && I.n != 28 && I.h_sym && !I.term_p;
+}
+
 void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int ept, int min_blocks, bool mixed,
-                int n_sm, cudaStream_t s) {
+                int n_sm, cudaStream_t s, bool tcore = false) {
   P.arena.release();
   P.inst = insts;
   std::vector<DiagTile> tiles;
   size_t smem = 0;
   long long total = 0;
   const size_t cap = 200 * 1024;
+  int tmem_cols = 32;
+  if (tcore) {
+    if (block != 256) throw unsupported_error("tensor-core commutator: 256-thread CTAs");
+    for (const DiagInst& I : insts)
+      if (!tcore_eligible(I, mixed)) throw unsupported_error("tensor-core commutator: instance not eligible");
+  }
   for (size_t i = 0; i < P.inst.size(); ++i) {
     DiagInst& I = P.inst[i];
-    int tile = std::max(1, (ept * block) / std::max(1, I.n2));
-    while (tile > 1 && diag_tile_smem(I.n2, I.K, tile, mixed) > cap) tile /= 2;
-    if (diag_tile_smem(I.n2, I.K, tile, mixed) > cap)
-      throw unsupported_error("diagonal-coupling path: one ADO tile exceeds shared memory");
+    int tile;
+    if (tcore) {  // the tile is fixed by the GEMM shape (4 n rows per ADO, 128-row blocks)
+      tile = tc_tile(I.n);
+      if (diag_tile_smem_tc(I.n, I.K, tile) > cap) throw unsupported_error("tensor-core tile exceeds shared memory");
+      if ((tile * I.n2 + block - 1) / block > kTcPerThread)
+        throw unsupported_error("tensor-core tile exceeds the elements a thread holds");
+      smem = std::max(smem, diag_tile_smem_tc(I.n, I.K, tile));
+      tmem_cols = std::max(tmem_cols, tc_tmem_cols(I.n));
+    } else {
+      tile = std::max(1, (ept * block) / std::max(1, I.n2));
+      while (tile > 1 && diag_tile_smem(I.n2, I.K, tile, mixed) > cap) tile /= 2;
+      if (diag_tile_smem(I.n2, I.K, tile, mixed) > cap)
+        throw unsupported_error("diagonal-coupling path: one ADO tile exceeds shared memory");
+      smem = std::max(smem, diag_tile_smem(I.n2, I.K, tile, mixed));
+    }
     I.tile = tile;
-    smem = std::max(smem, diag_tile_smem(I.n2, I.K, tile, mixed));
     for (int l0 = 0; l0 < I.nh; l0 += tile) tiles.push_back(DiagTile{static_cast<int>(i), l0, std::min(tile, I.nh - l0), 0});
     total = std::max(total, I.elem_off + static_cast<long long>(I.n2) * I.nh);
   }
@@ -243,6 +268,9 @@ void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int 
   P.ds.total = total;
   P.ds.smem = smem;
   P.ds.min_blocks = mixed ? min_blocks : 1;
+  P.ds.tcore = tcore ? 1 : 0;
+  P.ds.tmem_cols = tmem_cols;
+  P.tcore = tcore;
   P.block = block;
   P.ept = ept;
   P.min_blocks = P.ds.min_blocks;
@@ -739,6 +767,12 @@ void build_model(heomgb_qme* q) {
     di.K = K;
     di.nh = nh;
     di.h_real = m.h_real;
+    {
+      bool sym = m.h_real != 0;
+      for (int a = 0; a < n && sym; ++a)
+        for (int b = 0; b < a && sym; ++b) sym = q->H[static_cast<size_t>(a) * n + b] == q->H[static_cast<size_t>(b) * n + a];
+      di.h_sym = sym ? 1 : 0;
+    }
     di.sqrt_norm = m.sqrt_norm;
     di.elem_off = 0;
     di.p1 = m.p1;
@@ -1006,11 +1040,52 @@ void autotune(heomgb_qme_solver* qs) {
   // (reproducible profiles: a profiler's replay distorts the timings the
   // search relies on)
   int pin_b = 0, pin_e = 0, pin_m = 1;
+  bool pin_tc = false;
   if (const char* env = std::getenv("HEOMGB_TILE")) {
-    const int got = std::sscanf(env, "%dx%dx%d", &pin_b, &pin_e, &pin_m);
-    if (got < 2 || (pin_b != 64 && pin_b != 128 && pin_b != 256) || pin_e < 1 || pin_e > 8 ||
-        (pin_m != 1 && pin_m != 3))
-      throw arg_error("HEOMGB_TILE must be <64|128|256>x<1..8>[x<1|3>]");
+    if (std::string(env) == "tc") {
+      pin_tc = true;
+    } else {
+      const int got = std::sscanf(env, "%dx%dx%d", &pin_b, &pin_e, &pin_m);
+      if (got < 2 || (pin_b != 64 && pin_b != 128 && pin_b != 256) || pin_e < 1 || pin_e > 8 ||
+          (pin_m != 1 && pin_m != 3))
+        throw arg_error("HEOMGB_TILE must be tc or <64|128|256>x<1..8>[x<1|3>]");
+    }
+  }
+  // the tensor-core commutator joins the search where every instance is
+  // eligible; HEOMGB_TCORE=0 keeps it out
+  bool tc_ok = qs->mixed;
+  for (const DiagInst& I : insts) tc_ok = tc_ok && tcore_eligible(I, qs->mixed);
+  if (const char* env = std::getenv("HEOMGB_TCORE"))
+    if (std::string(env) == "0") tc_ok = false;
+  if (pin_tc && !tc_ok) throw unsupported_error("HEOMGB_TILE=tc: the tensor-core commutator does not apply");
+  bool best_tc = false;
+  auto time_plan = [&](int b) {
+    const bool in_double = !qs->separate;
+    ck(launch_rhs(q->dm, &qs->plan.ds, st, PATH_DIAG, qs->mixed, in_double, qs->plan.grid, b, qs->stream), "tune");
+    ck(cudaEventRecord(e0, qs->stream), "event");
+    for (int r = 0; r < 3; ++r)
+      ck(launch_rhs(q->dm, &qs->plan.ds, st, PATH_DIAG, qs->mixed, in_double, qs->plan.grid, b, qs->stream),
+         "tune");
+    ck(cudaEventRecord(e1, qs->stream), "event");
+    ck(cudaEventSynchronize(e1), "event sync");
+    float ms = 0.f;
+    ck(cudaEventElapsedTime(&ms, e0, e1), "event time");
+    return ms;
+  };
+  if (tc_ok && (pin_tc || !pin_b)) {
+    build_plan(qs->plan, insts, 256, 1, 1, qs->mixed, q->n_sm, qs->stream, true);
+    const float ms = pin_tc ? 0.f : time_plan(256);
+    // the stage flags a tensor-core wait that ran out; such a plan is not kept
+    DpCtl probe;
+    ck(cudaMemcpyAsync(&probe, qs->ctl, sizeof(DpCtl), cudaMemcpyDeviceToHost, qs->stream), "ctl read");
+    ck(cudaStreamSynchronize(qs->stream), "ctl sync");
+    if (probe.status == 2) {
+      ck(cudaMemsetAsync(&qs->ctl->status, 0, sizeof(int), qs->stream), "ctl reset");
+      if (pin_tc) throw cuda_error("tensor-core stage did not complete");
+    } else if (pin_tc || ms < best) {
+      best = ms;
+      best_tc = true;
+    }
   }
   const int blocks[3] = {64, 128, 256}, epts[4] = {1, 2, 4, 8};
   const int n_minb = qs->mixed ? 2 : 1, minbs[2] = {1, 3};
@@ -1018,7 +1093,7 @@ void autotune(heomgb_qme_solver* qs) {
     for (int e : epts)
       for (int mi = 0; mi < n_minb; ++mi) {
       const int m = minbs[mi];
-      if (pin_b && (b != pin_b || e != pin_e || m != pin_m)) continue;
+      if (pin_tc || (pin_b && (b != pin_b || e != pin_e || m != pin_m))) continue;
       try {
         build_plan(qs->plan, insts, b, e, m, qs->mixed, q->n_sm, qs->stream);
       } catch (const unsupported_error&) {
@@ -1030,26 +1105,21 @@ void autotune(heomgb_qme_solver* qs) {
         best_m = m;
         break;
       }
-      const bool in_double = !qs->separate;
-      ck(launch_rhs(q->dm, &qs->plan.ds, st, PATH_DIAG, qs->mixed, in_double, qs->plan.grid, b, qs->stream), "tune");
-      ck(cudaEventRecord(e0, qs->stream), "event");
-      for (int r = 0; r < 3; ++r)
-        ck(launch_rhs(q->dm, &qs->plan.ds, st, PATH_DIAG, qs->mixed, in_double, qs->plan.grid, b, qs->stream),
-           "tune");
-      ck(cudaEventRecord(e1, qs->stream), "event");
-      ck(cudaEventSynchronize(e1), "event sync");
-      float ms = 0.f;
-      ck(cudaEventElapsedTime(&ms, e0, e1), "event time");
+      const float ms = time_plan(b);
       if (ms < best) {
         best = ms;
         best_b = b;
         best_e = e;
         best_m = m;
+        best_tc = false;
       }
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  build_plan(qs->plan, insts, best_b, best_e, best_m, qs->mixed, q->n_sm, qs->stream);
+  if (best_tc)
+    build_plan(qs->plan, insts, 256, 1, 1, qs->mixed, q->n_sm, qs->stream, true);
+  else
+    build_plan(qs->plan, insts, best_b, best_e, best_m, qs->mixed, q->n_sm, qs->stream);
 }
 
 Stage solver_stage(heomgb_qme_solver* qs) {
@@ -1222,6 +1292,11 @@ void solve_fixed(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwarg
   ck(launch_ctl_set_fixed(qs->ctl, last, qs->stream), "ctl dt");
   replay(qs, false);
   busy_end(qs);
+  if (qs->plan.tcore) {  // a tensor-core stage that gave up flags the controller
+    ck(cudaMemcpyAsync(qs->ctl_host, qs->ctl, sizeof(DpCtl), cudaMemcpyDeviceToHost, qs->stream), "ctl read");
+    ck(cudaStreamSynchronize(qs->stream), "ctl sync");
+    if (qs->ctl_host->status == 2) throw cuda_error("tensor-core stage did not complete");
+  }
   qs->n_rhs += 4 * (m + 1);
   qs->n_attempts += m + 1;
   qs->n_accepted += m + 1;
@@ -1253,6 +1328,7 @@ int solve_adaptive(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwa
     big = true;
     if (launched > cap) throw numeric_error("Dormand-Prince attempt cap reached");
   }
+  if (qs->ctl_host->status == 2) throw cuda_error("tensor-core stage did not complete");
   if (qs->ctl_host->status) throw numeric_error("non-finite step size in Dormand-Prince control");
   qs->dt_save = qs->ctl_host->dt;
   qs->n_attempts += qs->ctl_host->attempts;
@@ -1666,6 +1742,13 @@ heomgb_status heomgb_qme_solver_tuning(const heomgb_qme_solver* qs, int* block, 
     if (elems_per_thread) *elems_per_thread = diag ? qs->plan.ept : 0;
     if (n_tiles) *n_tiles = diag ? qs->plan.ds.n_tiles : 0;
     if (min_blocks) *min_blocks = diag ? qs->plan.min_blocks : 0;
+  });
+}
+
+heomgb_status heomgb_qme_solver_tensor_cores(const heomgb_qme_solver* qs, int* on) {
+  return guard([&] {
+    require(qs != nullptr && on != nullptr, "null argument");
+    *on = (qs->q->path == PATH_DIAG && qs->plan.tcore) ? 1 : 0;
   });
 }
 

@@ -116,6 +116,10 @@ struct Stage {
 
 enum Path : int { PATH_DIAG = 0, PATH_GENERAL = 1, PATH_LIOU = 2, PATH_REDFIELD = 3 };
 
+// Elements of one tile per thread in the tensor-core stage (256 threads; the
+// largest tile, n_state 24: 4 ADOs x 576 elements).
+constexpr int kTcPerThread = 9;
+
 // One instance of the diagonal-coupling kernel: a model's sizes, where its
 // elements start in the (possibly concatenated) state vector, and its tables.
 // A single model is a set of one instance; a batch concatenates many.
@@ -146,6 +150,8 @@ struct DiagInst {
   const float2* term_p;
   int term_first;
   int sqrt_norm;            // 1: +1 terms scale by sqrt(n_k+1), -1 terms by sqrt(n_k) (else 1 and n_k)
+  int h_sym;                // H real and symmetric (the tensor-core commutator's condition)
+  int pad_;
 };
 struct DiagTile {
   int inst, l0, nt, pad;
@@ -157,6 +163,8 @@ struct DiagSet {
   long long total;          // elements over all instances
   size_t smem;              // dynamic shared memory of the largest tile
   int min_blocks;           // 1, or 3: the mixed kernel compiled for 3 resident 256-thread CTAs (<= 80 registers)
+  int tcore;                // 1: micro-tiled commutators on the tensor cores (k_rhs_diag_tc)
+  int tmem_cols;            // tensor-memory columns a CTA of k_rhs_diag_tc allocates
 };
 
 // Launchers (kernels.cu).  `mixed` selects FP32 bulk arithmetic; `in_double`
@@ -168,6 +176,10 @@ int rhs_block_size(const RhsModel& m, int path);
 int rhs_grid_size(const RhsModel& m, int path, int block, int n_sm);
 size_t rhs_smem_bytes(const RhsModel& m, int path, bool mixed);
 size_t diag_tile_smem(int n2, int K, int tile, bool mixed);
+// tensor-core variant: shared memory of one tile, ADOs per tile, tensor-memory columns
+size_t diag_tile_smem_tc(int n, int K, int tile);
+int tc_tile(int n);
+int tc_tmem_cols(int n);
 
 cudaError_t launch_hrchy_build(int K, int depth, int n_hrchy, const long long* binom, int binom_dim, int* nidx,
                                int* p1, int* m1, cudaStream_t s);

@@ -436,6 +436,198 @@ __device__ __forceinline__ bool stage_prologue(const Stage& st, double& dt, int&
   return true;
 }
 
+// ------------------------------------------------------------------ tensor-core commutator (tcgen05)
+// For real symmetric H the commutator of ADO l needs X H for X in {R, I, R^T,
+// I^T} (rho = R + iI): rows of R H and I H give -rho H, rows of R^T H = (H R)^T
+// and I^T H give H rho.  One GEMM per tile: A = the 4n rows of every tile ADO
+// stacked (M = 4 n nt, a multiple of 128), B = H (N padded to 16 or 32), K = n
+// padded to 8.  Operands are split into TF32 hi + lo (3xTF32: hi*hi + hi*lo +
+// lo*hi, FP32 accumulation in tensor memory), staged in shared memory in the
+// K-major layout without swizzle: 8-row x 16-byte core matrices, the core
+// matrices of one 8-row group adjacent along K (leading byte offset 128), row
+// groups (K/4)*128 bytes apart (stride byte offset).  One thread issues the
+// MMAs; completion arrives on an mbarrier; the CTA gathers the tile's bath
+// terms meanwhile, then every warp reads its sub-partition of tensor-memory
+// lanes back.
+struct TcGeom {
+  int rows_per_ado;  // 4n
+  int m_total;       // rows of A: 4 n nt, a multiple of 128
+  int k_pad;         // n rounded up to 8
+  int n_pad;         // n rounded up to 16 (16 or 32)
+};
+__host__ __device__ inline int tc_tile_ados(int n) {
+  int g = 4 * n, a = 128;
+  while (a) {
+    const int t = g % a;
+    g = a;
+    a = t;
+  }
+  return 128 / g;  // 128 / gcd(4n, 128)
+}
+__host__ __device__ inline TcGeom tc_geom(int n) {
+  TcGeom t;
+  t.rows_per_ado = 4 * n;
+  t.m_total = 4 * n * tc_tile_ados(n);
+  t.k_pad = (n + 7) / 8 * 8;
+  t.n_pad = n <= 16 ? 16 : 32;
+  return t;
+}
+__host__ __device__ inline size_t tc_operand_bytes(int n) {
+  const TcGeom t = tc_geom(n);
+  return 2 * sizeof(float) * (static_cast<size_t>(t.m_total) * t.k_pad);  // A hi + lo
+}
+// the operand region: A (hi | lo), later the four product arrays
+__host__ __device__ inline size_t tc_region_bytes(int n, int tile) {
+  const size_t prod = 4 * sizeof(float) * static_cast<size_t>(tile) * n * (n + 1);
+  return tc_operand_bytes(n) > prod ? tc_operand_bytes(n) : prod;
+}
+__host__ __device__ inline size_t tc_b_bytes(int n) {
+  const TcGeom t = tc_geom(n);
+  return 2 * sizeof(float) * (static_cast<size_t>(t.n_pad) * t.k_pad);
+}
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+// tcgen05 shared-memory matrix descriptor: start, leading and stride byte
+// offsets in 16-byte units, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return static_cast<uint64_t>((saddr >> 4) & 0x3FFF) | (static_cast<uint64_t>((lbo >> 4) & 0x3FFF) << 16) |
+         (static_cast<uint64_t>((sbo >> 4) & 0x3FFF) << 32) | (static_cast<uint64_t>(1) << 46);
+}
+__device__ __forceinline__ float tf32_hi(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, int acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void tc_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+
+// Bounded wait for the completion of mbarrier phase `parity` (the MMAs of one
+// tile take microseconds; the limit is orders of magnitude above that).
+__device__ __forceinline__ uint32_t tc_wait(uint64_t* mbar, uint32_t parity) {
+  uint32_t done = 0;
+  for (int it = 0; it < (1 << 24) && !done; ++it) {
+    asm volatile(
+        "{\n .reg .pred q;\n mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n selp.b32 %0, 1, 0, q;\n}\n"
+        : "=r"(done)
+        : "r"(smem_addr(mbar)), "r"(parity));
+  }
+  return done;
+}
+
+// Stages A (the tile's rho rows and transposed rows, hi | lo) and B (H^T,
+// hi | lo), then thread 0 issues the MMAs and commits them to mbar.  Each warp
+// writes whole 8-row x 4-column units (32 consecutive words of the K-major
+// layout), so the stores are free of bank conflicts.
+__device__ __forceinline__ void tc_issue(const float2* yt, const float2* __restrict__ Hg, int n, int nt, float* Ah,
+                                         float* Al, float* Bh, float* Bl, uint64_t* mbar, uint32_t tmem) {
+  const TcGeom g = tc_geom(n);
+  const int n2 = n * n, kq = g.k_pad >> 2, lane = threadIdx.x & 31;
+  const int rr = lane >> 2, kk = lane & 3;
+  const int units_a = (g.m_total >> 3) * kq, units_b = (g.n_pad >> 3) * kq;
+  for (int u = threadIdx.x >> 5; u < units_a + units_b; u += blockDim.x >> 5) {
+    const bool is_a = u < units_a;
+    const int uu = is_a ? u : u - units_a;
+    const int m = (uu / kq) * 8 + rr, k = (uu % kq) * 4 + kk;
+    float x = 0.f;
+    if (is_a) {
+      const int l = m / g.rows_per_ado, rem = m - l * g.rows_per_ado;
+      const int part = rem / n, r = rem - part * n;
+      if (l < nt && k < n) {
+        const float2 v = part < 2 ? yt[l * n2 + r * n + k] : yt[l * n2 + k * n + r];
+        x = (part & 1) ? v.y : v.x;
+      }
+    } else if (m < n && k < n) {
+      x = __ldg(Hg + k * n + m).x;  // B[j][k] = H[k][j]
+    }
+    const float hi = tf32_hi(x);
+    float* dh = is_a ? Ah : Bh;
+    float* dl = is_a ? Al : Bl;
+    dh[uu * 32 + lane] = hi;
+    dl[uu * 32 + lane] = x - hi;
+  }
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (threadIdx.x == 0) {
+    const uint32_t sbo = static_cast<uint32_t>(kq) * 128u;
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | (static_cast<uint32_t>(g.n_pad >> 3) << 17) |
+                           (static_cast<uint32_t>(128 >> 4) << 24);
+    const uint32_t ah = smem_addr(Ah), al = smem_addr(Al), bh = smem_addr(Bh), bl = smem_addr(Bl);
+    for (int t = 0; t < g.m_total / 128; ++t) {
+      const uint32_t d = tmem + static_cast<uint32_t>(t * g.n_pad);
+      const uint32_t a_off = static_cast<uint32_t>(t) * 16u * sbo;
+      for (int s = 0; s < g.k_pad / 8; ++s) {
+        const uint32_t k_off = static_cast<uint32_t>(s) * 256u;
+        const uint64_t dah = tc_desc(ah + a_off + k_off, 128, sbo), dal = tc_desc(al + a_off + k_off, 128, sbo);
+        const uint64_t dbh = tc_desc(bh + k_off, 128, sbo), dbl = tc_desc(bl + k_off, 128, sbo);
+        tc_mma(d, dah, dbh, idesc, s > 0);
+        tc_mma(d, dah, dbl, idesc, 1);
+        tc_mma(d, dal, dbh, idesc, 1);
+      }
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+        smem_addr(mbar)));
+  }
+}
+
+// Waits (bounded) for the tile's MMAs and writes the products out of tensor
+// memory into four FP32 arrays of nt * n * (n + 1) words (row stride n + 1):
+// X1 / Y1 take the R H / I H rows (x: (I H)_rc, y: -(R H)_rc), X2 / Y2 the
+// transposed H R / H I rows (x: -(H I)_cr, y: (H R)_cr); i[H, rho]_ab =
+// (X1 + X2, Y1 + Y2)_ab.  The odd row stride keeps a warp's 32 rows in 32
+// banks.  The arrays may overlay A: they are written only after the MMAs
+// completed.  Returns false (CTA-uniform) if the wait gave up.
+__device__ __forceinline__ bool tc_readback(int n, int nt, float* X1, float* Y1, float* X2, float* Y2,
+                                            uint64_t* mbar, uint32_t tmem, uint32_t parity) {
+  const TcGeom g = tc_geom(n);
+  uint32_t done = tc_wait(mbar, parity);
+  done = __syncthreads_and(done);  // one verdict for the whole CTA
+  tc_fence_after();
+  if (done) {
+    const int warp = threadIdx.x >> 5, sp = warp & 3, lane = threadIdx.x & 31;
+    const int half = warp >> 2, halves = blockDim.x >> 7;  // warps w and w + 4 share a lane sub-partition
+    const int ld = n + 1, P = n * ld;
+    for (int t = 0; t < g.m_total / 128; ++t) {
+      const int m = t * 128 + sp * 32 + lane;
+      const int l = m / g.rows_per_ado, rem = m - l * g.rows_per_ado;
+      const int part = rem / n, r = rem - part * n;
+      float* dst = part == 0 ? Y1 : part == 1 ? X1 : part == 2 ? Y2 : X2;
+      const float sgn = (part == 0 || part == 3) ? -1.f : 1.f;
+      for (int q = half; q < g.n_pad / 8; q += halves) {
+        float v[8];
+        tc_ld8(tmem + (static_cast<uint32_t>(sp * 32) << 16) + static_cast<uint32_t>(t * g.n_pad + 8 * q), v);
+        if (l >= nt) continue;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int c = 8 * q + j;
+          if (c < n) dst[l * P + (part < 2 ? r * ld + c : c * ld + r)] = sgn * v[j];
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  return done != 0;
+}
+
 // ------------------------------------------------------------------ RHS, diagonal V
 // For every bath u with diagonal V_u the coupling terms are elementwise:
 // [V,X]_ab = (v_a - v_b) X_ab and {V,X}_ab = (v_a + v_b) X_ab, so element e
@@ -656,6 +848,184 @@ __global__ void __launch_bounds__(256, MINB) k_rhs_diag(const DiagSet ds, const 
     else
       local += diag_tile<TC, TB, false>(I, td, st, y, dt, cur, smem_raw);
   }
+  if (st.kind == EPI_DP7) dp7_finish(st, local, ds.total);
+}
+
+// One tile of the diagonal-coupling stage with the commutators on the tensor
+// cores (tc_issue / tc_readback): FP32 arithmetic (the mixed form), real
+// symmetric H, a micro-tiled n_state, no terminator.  While the MMAs run, each
+// thread gathers the bath terms and the damping of its (at most
+// kTcPerThread) elements into registers; after the read-back it adds the
+// commutator and runs the stage epilogue.  Shared memory: the tile's input
+// rows, its hierarchy rows, the operand region (A, reused for the products)
+// and B.
+template <typename TB>
+__device__ __forceinline__ double diag_tile_tc(const DiagInst* __restrict__ I, const DiagTile td, const Stage& st,
+                                               const TB* __restrict__ y, double dt, int cur, unsigned char* smem_raw,
+                                               uint64_t* mbar, uint32_t tmem, uint32_t parity, int* fail) {
+  const int n = I->n, n2 = I->n2, K = I->K, void_idx = I->nh, tile = I->tile;
+  const long long base = I->elem_off;
+  float2* yt = reinterpret_cast<float2*>(smem_raw);  // tile*n2
+  int* p1s = reinterpret_cast<int*>(yt + static_cast<size_t>(tile) * n2);
+  int* m1s = p1s + tile * K;
+  int* nks = m1s + tile * K;
+  unsigned char* opnd = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(nks + tile * K) + 127) & ~static_cast<uintptr_t>(127));
+  float* Ah = reinterpret_cast<float*>(opnd);
+  float* Al = Ah + tc_operand_bytes(n) / (2 * sizeof(float));
+  float* Bh = reinterpret_cast<float*>(opnd + (tc_region_bytes(n, tile) + 127) / 128 * 128);
+  float* Bl = Bh + tc_b_bytes(n) / (2 * sizeof(float));
+  const int ld = n + 1, P = n * ld;
+  float* X1 = reinterpret_cast<float*>(opnd);
+  float* Y1 = X1 + tile * P;
+  float* X2 = Y1 + tile * P;
+  float* Y2 = X2 + tile * P;
+  const float2* __restrict__ ngd = I->ngd_f;
+  const float2* __restrict__ cpl = I->c_plus_f;
+  const float2* __restrict__ cmi = I->c_minus_f;
+  const float2* __restrict__ csd = I->c_sd_f;
+  const bool sqn = I->sqrt_norm != 0;
+  const int* __restrict__ plus_ptr = I->plus_ptr;
+  const int* __restrict__ plus_mode = I->plus_mode;
+  const int* __restrict__ minus_ptr = I->minus_ptr;
+  const int* __restrict__ minus_mode = I->minus_mode;
+  const TB* __restrict__ yi = y + base;
+  const int l0 = td.l0, nt = td.nt, ne = nt * n2;
+  const TB* __restrict__ ysrc = yi + static_cast<size_t>(l0) * n2;
+  for (int i = threadIdx.x; i < ne; i += blockDim.x) yt[i] = ldc<float>(ysrc + i);
+  for (int i = threadIdx.x; i < nt * K; i += blockDim.x) {
+    const size_t gi = static_cast<size_t>(l0) * K + i;
+    p1s[i] = __ldg(I->p1 + gi);
+    m1s[i] = __ldg(I->m1 + gi);
+    nks[i] = __ldg(I->nidx + gi);
+  }
+  __syncthreads();
+  tc_issue(yt, I->H_f, n, nt, Ah, Al, Bh, Bl, mbar, tmem);
+  // damping and bath terms while the tensor cores work
+  float2 part[kTcPerThread];
+#pragma unroll
+  for (int j = 0; j < kTcPerThread; ++j) {
+    const int i = threadIdx.x + j * blockDim.x;
+    float2 D = make_float2(0.f, 0.f);
+    if (i < ne) {
+      const int lt = i / n2, e = i - lt * n2;
+      const float2 g0 = ngd[l0 + lt], g1 = csd[e];
+      cfma(D, make_float2(g0.x + g1.x, g0.y + g1.y), yt[i]);
+      const int* p1row = p1s + lt * K;
+      const int* m1row = m1s + lt * K;
+      const int* nrow = nks + lt * K;
+      const int pb = __ldg(plus_ptr + e), pe = __ldg(plus_ptr + e + 1);
+      const int mb = __ldg(minus_ptr + e), me = __ldg(minus_ptr + e + 1);
+      for (int pp = pb, mp = mb; pp < pe || mp < me; pp += 4, mp += 4) {
+        float2 v[8], cf[8];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int p = pp + q;
+          v[q] = cf[q] = make_float2(0.f, 0.f);
+          if (p < pe) {
+            const int k = __ldg(plus_mode + p);
+            const int lp = p1row[k];
+            if (lp != void_idx) {
+              v[q] = ldc<float>(yi + static_cast<size_t>(lp) * n2 + e);
+              cf[q] = cpl[p];
+              if (sqn) {
+                const float f = sqrtf(static_cast<float>(nrow[k] + 1));
+                cf[q] = make_float2(f * cf[q].x, f * cf[q].y);
+              }
+            }
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int p = mp + q;
+          v[4 + q] = cf[4 + q] = make_float2(0.f, 0.f);
+          if (p < me) {
+            const int k = __ldg(minus_mode + p);
+            const int lm = m1row[k];
+            if (lm != void_idx) {
+              const float nk = sqn ? sqrtf(static_cast<float>(nrow[k])) : static_cast<float>(nrow[k]);
+              const float2 cm = cmi[p];
+              v[4 + q] = ldc<float>(yi + static_cast<size_t>(lm) * n2 + e);
+              cf[4 + q] = make_float2(nk * cm.x, nk * cm.y);
+            }
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) cfma(D, cf[q], v[q]);
+      }
+    }
+    part[j] = D;
+  }
+  if (!tc_readback(n, nt, X1, Y1, X2, Y2, mbar, tmem, parity)) {
+    if (threadIdx.x == 0 && st.ctl) st.ctl->status = 2;  // tensor-core wait gave up
+    *fail = 1;                                             // (every thread: the verdict is CTA-wide)
+    return 0.0;
+  }
+  double local = 0.0;
+#pragma unroll
+  for (int j = 0; j < kTcPerThread; ++j) {
+    const int i = threadIdx.x + j * blockDim.x;
+    if (i < ne) {
+      const int lt = i / n2, e = i - lt * n2, a = e / n, b = e - a * n;
+      const int o = lt * P + a * ld + b;
+      float2 D = part[j];
+      D.x += X1[o] + X2[o];
+      D.y += Y1[o] + Y2[o];
+      const size_t gi = static_cast<size_t>(base + static_cast<long long>(l0) * n2 + i);
+      const EpiPre pre = epi_pre<float>(st, gi, cur);
+      local += epi_post<float>(st, gi, D, dt, cur, pre);
+    }
+  }
+  __syncthreads();  // the next tile restages shared memory
+  return local;
+}
+
+// The diagonal-coupling stage with the commutators on the tensor cores
+// (diag_tile_tc); every instance of the plan is eligible.  256 threads;
+// tensor memory is allocated per CTA (at most two CTAs reside on an SM, so
+// the allocations never exceed the SM's 512 columns).
+template <typename TB>
+__global__ void __launch_bounds__(256, 2) k_rhs_diag_tc(const DiagSet ds, const Stage st) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  double dt;
+  int cur;
+  // one verdict per CTA: another CTA of this launch may flag the controller
+  // meanwhile, and the allocation below is warp-synchronous
+  if (!__syncthreads_and(stage_prologue(st, dt, cur))) return;
+  const TB* __restrict__ y = stage_input<TB>(st, cur);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + ds.smem - 16);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + ds.smem - 8);
+  if (threadIdx.x < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(tslot)),
+                 "r"(static_cast<uint32_t>(ds.tmem_cols)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(mbar)));
+    asm volatile("fence.mbarrier_init.release.cluster;\n");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  double local = 0.0;
+  uint32_t parity = 0;
+  int fail = 0;
+  for (int t = blockIdx.x; t < ds.n_tiles; t += gridDim.x) {
+    const DiagTile td = ds.tiles[t];
+    const DiagInst* I = ds.inst + td.inst;
+    local += diag_tile_tc<TB>(I, td, st, y, dt, cur, smem_raw, mbar, tmem, parity, &fail);
+    if (fail) break;
+    parity ^= 1u;
+  }
+  // an abandoned tile's MMAs drain (bounded) before the tensor memory is freed
+  if (fail) tc_wait(mbar, parity);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (threadIdx.x < 32)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+                 "r"(static_cast<uint32_t>(ds.tmem_cols)));
   if (st.kind == EPI_DP7) dp7_finish(st, local, ds.total);
 }
 
@@ -956,6 +1326,22 @@ size_t rhs_smem_bytes(const RhsModel& m, int path, bool mixed) {
   return 0;
 }
 
+size_t diag_tile_smem_tc(int n, int K, int tile) {
+  const size_t n2 = static_cast<size_t>(n) * n;
+  size_t b = sizeof(float2) * n2 * tile + 3 * sizeof(int) * static_cast<size_t>(tile) * K;
+  b = (b + 127) / 128 * 128;
+  b += (tc_region_bytes(n, tile) + 127) / 128 * 128 + tc_b_bytes(n);
+  return (b + 15) / 16 * 16 + 128 + 16;  // alignment slack, then the mbarrier and tensor-memory address slot
+}
+
+int tc_tile(int n) { return tc_tile_ados(n); }
+int tc_tmem_cols(int n) {
+  const TcGeom g = tc_geom(n);
+  int need = g.m_total / 128 * g.n_pad, c = 32;
+  while (c < need) c <<= 1;
+  return c;
+}
+
 size_t diag_tile_smem(int n2, int K, int tile, bool mixed) {
   const size_t cb = mixed ? sizeof(float2) : sizeof(double2);
   const int n = static_cast<int>(std::lround(std::sqrt(static_cast<double>(n2))));
@@ -974,6 +1360,7 @@ static cudaError_t launch_typed(const RhsModel& m, const DiagSet* ds, const Stag
     auto kern = k_rhs_diag<TC, TB, 1>;
     if constexpr (std::is_same<TC, float>::value) {
       if (ds->min_blocks == 3) kern = k_rhs_diag<TC, TB, 3>;
+      if (ds->tcore) kern = k_rhs_diag_tc<TB>;
     }
     if (dsm > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dsm));

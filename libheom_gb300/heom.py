@@ -323,7 +323,10 @@ class qme_solver:
         b, e, t, m = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         check(self._lib.heomgb_qme_solver_tuning(self._h, ctypes.byref(b), ctypes.byref(e), ctypes.byref(t),
                                                  ctypes.byref(m)))
-        return dict(block=b.value, elems_per_thread=e.value, n_tiles=t.value, min_blocks=m.value)
+        tc = ctypes.c_int()
+        check(self._lib.heomgb_qme_solver_tensor_cores(self._h, ctypes.byref(tc)))
+        return dict(block=b.value, elems_per_thread=e.value, n_tiles=t.value, min_blocks=m.value,
+                    tensor_cores=bool(tc.value))
 
     def stats(self) -> dict:
         r, a, c = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()

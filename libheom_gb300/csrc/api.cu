@@ -237,7 +237,7 @@ void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int 
   const size_t cap = 200 * 1024;
   int tmem_cols = 32;
   if (tcore) {
-    if (block != 256) throw unsupported_error("tensor-core commutator: 256-thread CTAs");
+    if (block != 128 && block != 256) throw unsupported_error("tensor-core commutator: 128- or 256-thread CTAs");
     for (const DiagInst& I : insts)
       if (!tcore_eligible(I, mixed)) throw unsupported_error("tensor-core commutator: instance not eligible");
   }
@@ -247,8 +247,6 @@ void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int 
     if (tcore) {  // the tile is fixed by the GEMM shape (4 n rows per ADO, 128-row blocks)
       tile = tc_tile(I.n);
       if (diag_tile_smem_tc(I.n, I.K, tile) > cap) throw unsupported_error("tensor-core tile exceeds shared memory");
-      if ((tile * I.n2 + block - 1) / block > kTcPerThread)
-        throw unsupported_error("tensor-core tile exceeds the elements a thread holds");
       smem = std::max(smem, diag_tile_smem_tc(I.n, I.K, tile));
       tmem_cols = std::max(tmem_cols, tc_tmem_cols(I.n));
     } else {
@@ -1072,19 +1070,25 @@ void autotune(heomgb_qme_solver* qs) {
     ck(cudaEventElapsedTime(&ms, e0, e1), "event time");
     return ms;
   };
+  int best_tc_m = 3, best_tc_b = 256;
   if (tc_ok && (pin_tc || !pin_b)) {
-    build_plan(qs->plan, insts, 256, 1, 1, qs->mixed, q->n_sm, qs->stream, true);
-    const float ms = pin_tc ? 0.f : time_plan(256);
-    // the stage flags a tensor-core wait that ran out; such a plan is not kept
-    DpCtl probe;
-    ck(cudaMemcpyAsync(&probe, qs->ctl, sizeof(DpCtl), cudaMemcpyDeviceToHost, qs->stream), "ctl read");
-    ck(cudaStreamSynchronize(qs->stream), "ctl sync");
-    if (probe.status == 2) {
-      ck(cudaMemsetAsync(&qs->ctl->status, 0, sizeof(int), qs->stream), "ctl reset");
-      if (pin_tc) throw cuda_error("tensor-core stage did not complete");
-    } else if (pin_tc || ms < best) {
-      best = ms;
-      best_tc = true;
+    for (int b : {128, 256})
+    for (int m : {3, 2}) {  // register caps 80 and 128
+      build_plan(qs->plan, insts, b, 1, m, qs->mixed, q->n_sm, qs->stream, true);
+      const float ms = time_plan(b);
+      // the stage flags a tensor-core wait that ran out; such a plan is not kept
+      DpCtl probe;
+      ck(cudaMemcpyAsync(&probe, qs->ctl, sizeof(DpCtl), cudaMemcpyDeviceToHost, qs->stream), "ctl read");
+      ck(cudaStreamSynchronize(qs->stream), "ctl sync");
+      if (probe.status == 2) {
+        ck(cudaMemsetAsync(&qs->ctl->status, 0, sizeof(int), qs->stream), "ctl reset");
+        if (pin_tc) throw cuda_error("tensor-core stage did not complete");
+      } else if (ms < best) {
+        best = ms;
+        best_tc = true;
+        best_tc_m = m;
+        best_tc_b = b;
+      }
     }
   }
   const int blocks[3] = {64, 128, 256}, epts[4] = {1, 2, 4, 8};
@@ -1117,7 +1121,7 @@ void autotune(heomgb_qme_solver* qs) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (best_tc)
-    build_plan(qs->plan, insts, 256, 1, 1, qs->mixed, q->n_sm, qs->stream, true);
+    build_plan(qs->plan, insts, best_tc_b, 1, best_tc_m, qs->mixed, q->n_sm, qs->stream, true);
   else
     build_plan(qs->plan, insts, best_b, best_e, best_m, qs->mixed, q->n_sm, qs->stream);
 }

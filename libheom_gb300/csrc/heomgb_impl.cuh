@@ -116,10 +116,6 @@ struct Stage {
 
 enum Path : int { PATH_DIAG = 0, PATH_GENERAL = 1, PATH_LIOU = 2, PATH_REDFIELD = 3 };
 
-// Elements of one tile per thread in the tensor-core stage (256 threads; the
-// largest tile, n_state 24: 4 ADOs x 576 elements).
-constexpr int kTcPerThread = 9;
-
 // One instance of the diagonal-coupling kernel: a model's sizes, where its
 // elements start in the (possibly concatenated) state vector, and its tables.
 // A single model is a set of one instance; a batch concatenates many.

@@ -440,8 +440,8 @@ __device__ __forceinline__ bool stage_prologue(const Stage& st, double& dt, int&
 // For real symmetric H the commutator of ADO l needs X H for X in {R, I, R^T,
 // I^T} (rho = R + iI): rows of R H and I H give -rho H, rows of R^T H = (H R)^T
 // and I^T H give H rho.  One GEMM per tile: A = the 4n rows of every tile ADO
-// stacked (M = 4 n nt, a multiple of 128), B = H (N padded to 16 or 32), K = n
-// padded to 8.  Operands are split into TF32 hi + lo (3xTF32: hi*hi + hi*lo +
+// stacked (M = 128, zero-padded), B = H (N padded to 16 or 32), K = n padded
+// to 8.  Operands are split into TF32 hi + lo (3xTF32: hi*hi + hi*lo +
 // lo*hi, FP32 accumulation in tensor memory), staged in shared memory in the
 // K-major layout without swizzle: 8-row x 16-byte core matrices, the core
 // matrices of one 8-row group adjacent along K (leading byte offset 128), row
@@ -451,23 +451,17 @@ __device__ __forceinline__ bool stage_prologue(const Stage& st, double& dt, int&
 // lanes back.
 struct TcGeom {
   int rows_per_ado;  // 4n
-  int m_total;       // rows of A: 4 n nt, a multiple of 128
+  int m_total;       // rows of A: one 128-row MMA block
   int k_pad;         // n rounded up to 8
   int n_pad;         // n rounded up to 16 (16 or 32)
 };
-__host__ __device__ inline int tc_tile_ados(int n) {
-  int g = 4 * n, a = 128;
-  while (a) {
-    const int t = g % a;
-    g = a;
-    a = t;
-  }
-  return 128 / g;  // 128 / gcd(4n, 128)
-}
+// ADOs of one tile: as many as fill one 128-row MMA (n = 8: 4, n = 12 and 16:
+// 2, n = 24 and 32: 1; rows past nt * 4n are zero padding)
+__host__ __device__ inline int tc_tile_ados(int n) { return 128 / (4 * n) > 0 ? 128 / (4 * n) : 1; }
 __host__ __device__ inline TcGeom tc_geom(int n) {
   TcGeom t;
   t.rows_per_ado = 4 * n;
-  t.m_total = 4 * n * tc_tile_ados(n);
+  t.m_total = 128;
   t.k_pad = (n + 7) / 8 * 8;
   t.n_pad = n <= 16 ? 16 : 32;
   return t;
@@ -476,10 +470,15 @@ __host__ __device__ inline size_t tc_operand_bytes(int n) {
   const TcGeom t = tc_geom(n);
   return 2 * sizeof(float) * (static_cast<size_t>(t.m_total) * t.k_pad);  // A hi + lo
 }
-// the operand region: A (hi | lo), later the four product arrays
-__host__ __device__ inline size_t tc_region_bytes(int n, int tile) {
-  const size_t prod = 4 * sizeof(float) * static_cast<size_t>(tile) * n * (n + 1);
-  return tc_operand_bytes(n) > prod ? tc_operand_bytes(n) : prod;
+// the four product arrays of a tile (row stride n + 1), then the partial sums
+__host__ __device__ inline size_t tc_product_bytes(int n, int tile) {
+  return 4 * sizeof(float) * static_cast<size_t>(tile) * n * (n + 1) + sizeof(float2) * static_cast<size_t>(tile) * n * n;
+}
+// x / d for 0 <= x < 2^12 and 1 <= d <= 2^10 from rd = 1.0f / d: (x + 0.5) / d
+// lies at least 0.5 / d away from an integer and the two roundings move it by
+// less than (x / d + 1) * 2^-23, so truncation gives the exact quotient
+__device__ __forceinline__ int small_div(int x, float rd) {
+  return __float2int_rz(__fmul_rn(static_cast<float>(x) + 0.5f, rd));
 }
 __host__ __device__ inline size_t tc_b_bytes(int n) {
   const TcGeom t = tc_geom(n);
@@ -530,36 +529,51 @@ __device__ __forceinline__ uint32_t tc_wait(uint64_t* mbar, uint32_t parity) {
   return done;
 }
 
-// Stages A (the tile's rho rows and transposed rows, hi | lo) and B (H^T,
-// hi | lo), then thread 0 issues the MMAs and commits them to mbar.  Each warp
-// writes whole 8-row x 4-column units (32 consecutive words of the K-major
-// layout), so the stores are free of bank conflicts.
-__device__ __forceinline__ void tc_issue(const float2* yt, const float2* __restrict__ Hg, int n, int nt, float* Ah,
-                                         float* Al, float* Bh, float* Bl, uint64_t* mbar, uint32_t tmem) {
+// Stages A (the tile's rho rows and transposed rows, hi | lo) and, when
+// build_b, B (H^T, hi | lo; it stays valid while the instance does not
+// change), then thread 0 issues the MMAs and commits them to mbar.  A warp
+// fills whole 8-row groups: a lane keeps its row for the group and writes
+// one word of each consecutive 32-word core-matrix pair, so the stores are
+// free of bank conflicts and the row arithmetic runs once per group.
+__device__ __forceinline__ void tc_issue(const float2* yt, const float2* __restrict__ Hg, bool build_b, int n, int nt,
+                                         float* Ah, float* Al, float* Bh, float* Bl, uint64_t* mbar, uint32_t tmem) {
   const TcGeom g = tc_geom(n);
-  const int n2 = n * n, kq = g.k_pad >> 2, lane = threadIdx.x & 31;
+  const int n2 = n * n, kq = g.k_pad >> 2, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const int rr = lane >> 2, kk = lane & 3;
-  const int units_a = (g.m_total >> 3) * kq, units_b = (g.n_pad >> 3) * kq;
-  for (int u = threadIdx.x >> 5; u < units_a + units_b; u += blockDim.x >> 5) {
-    const bool is_a = u < units_a;
-    const int uu = is_a ? u : u - units_a;
-    const int m = (uu / kq) * 8 + rr, k = (uu % kq) * 4 + kk;
-    float x = 0.f;
+  const float r_n = 1.0f / n, r_rows = 1.0f / g.rows_per_ado;
+  const int groups_a = g.m_total >> 3, groups = groups_a + (build_b ? g.n_pad >> 3 : 0);
+  for (int grp = threadIdx.x >> 5; grp < groups; grp += nw) {
+    const bool is_a = grp < groups_a;
+    const int gg = is_a ? grp : grp - groups_a;
+    const int m = gg * 8 + rr;
+    const float2* src;
+    int kstride;
+    bool live, im = false;
     if (is_a) {
-      const int l = m / g.rows_per_ado, rem = m - l * g.rows_per_ado;
-      const int part = rem / n, r = rem - part * n;
-      if (l < nt && k < n) {
-        const float2 v = part < 2 ? yt[l * n2 + r * n + k] : yt[l * n2 + k * n + r];
-        x = (part & 1) ? v.y : v.x;
-      }
-    } else if (m < n && k < n) {
-      x = __ldg(Hg + k * n + m).x;  // B[j][k] = H[k][j]
+      const int l = small_div(m, r_rows), rem = m - l * g.rows_per_ado;
+      const int part = small_div(rem, r_n), r = rem - part * n;
+      live = l < nt;
+      src = yt + (live ? l : 0) * n2 + (part < 2 ? r * n : r);  // row r of rho_l, or of its transpose
+      kstride = part < 2 ? 1 : n;
+      im = (part & 1) != 0;
+    } else {
+      live = m < n;
+      src = Hg + (live ? m : 0);  // B[j][k] = H[k][j]
+      kstride = n;
     }
-    const float hi = tf32_hi(x);
-    float* dh = is_a ? Ah : Bh;
-    float* dl = is_a ? Al : Bl;
-    dh[uu * 32 + lane] = hi;
-    dl[uu * 32 + lane] = x - hi;
+    float* dh = (is_a ? Ah : Bh) + gg * kq * 32 + lane;
+    float* dl = (is_a ? Al : Bl) + gg * kq * 32 + lane;
+    for (int qi = 0; qi < kq; ++qi) {
+      const int k = qi * 4 + kk;
+      float x = 0.f;
+      if (live && k < n) {
+        const float2 v = is_a ? src[k * kstride] : __ldg(src + k * kstride);
+        x = im ? v.y : v.x;
+      }
+      const float hi = tf32_hi(x);
+      dh[qi * 32] = hi;
+      dl[qi * 32] = x - hi;
+    }
   }
   asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
   tc_fence_before();
@@ -592,13 +606,13 @@ __device__ __forceinline__ void tc_issue(const float2* yt, const float2* __restr
 // X1 / Y1 take the R H / I H rows (x: (I H)_rc, y: -(R H)_rc), X2 / Y2 the
 // transposed H R / H I rows (x: -(H I)_cr, y: (H R)_cr); i[H, rho]_ab =
 // (X1 + X2, Y1 + Y2)_ab.  The odd row stride keeps a warp's 32 rows in 32
-// banks.  The arrays may overlay A: they are written only after the MMAs
-// completed.  Returns false (CTA-uniform) if the wait gave up.
+// banks.  Returns false (CTA-uniform) if the wait gave up.
 __device__ __forceinline__ bool tc_readback(int n, int nt, float* X1, float* Y1, float* X2, float* Y2,
                                             uint64_t* mbar, uint32_t tmem, uint32_t parity) {
   const TcGeom g = tc_geom(n);
-  uint32_t done = tc_wait(mbar, parity);
-  done = __syncthreads_and(done);  // one verdict for the whole CTA
+  uint32_t done = 0;
+  if (threadIdx.x == 0) done = tc_wait(mbar, parity);  // one waiter; the others sleep in the barrier
+  done = __syncthreads_or(done);                         // its verdict for the whole CTA
   tc_fence_after();
   if (done) {
     const int warp = threadIdx.x >> 5, sp = warp & 3, lane = threadIdx.x & 31;
@@ -606,8 +620,8 @@ __device__ __forceinline__ bool tc_readback(int n, int nt, float* X1, float* Y1,
     const int ld = n + 1, P = n * ld;
     for (int t = 0; t < g.m_total / 128; ++t) {
       const int m = t * 128 + sp * 32 + lane;
-      const int l = m / g.rows_per_ado, rem = m - l * g.rows_per_ado;
-      const int part = rem / n, r = rem - part * n;
+      const int l = small_div(m, 1.0f / g.rows_per_ado), rem = m - l * g.rows_per_ado;
+      const int part = small_div(rem, 1.0f / n), r = rem - part * n;
       float* dst = part == 0 ? Y1 : part == 1 ? X1 : part == 2 ? Y2 : X2;
       const float sgn = (part == 0 || part == 3) ? -1.f : 1.f;
       for (int q = half; q < g.n_pad / 8; q += halves) {
@@ -854,15 +868,14 @@ __global__ void __launch_bounds__(256, MINB) k_rhs_diag(const DiagSet ds, const 
 // One tile of the diagonal-coupling stage with the commutators on the tensor
 // cores (tc_issue / tc_readback): FP32 arithmetic (the mixed form), real
 // symmetric H, a micro-tiled n_state, no terminator.  While the MMAs run, each
-// thread gathers the bath terms and the damping of its (at most
-// kTcPerThread) elements into registers; after the read-back it adds the
-// commutator and runs the stage epilogue.  Shared memory: the tile's input
-// rows, its hierarchy rows, the operand region (A, reused for the products)
-// and B.
+// thread gathers the bath terms and the damping of its elements; after the
+// read-back it adds the commutator and runs the stage epilogue.  Shared memory: the tile's input
+// rows, its hierarchy rows, A, B and the products.
 template <typename TB>
 __device__ __forceinline__ double diag_tile_tc(const DiagInst* __restrict__ I, const DiagTile td, const Stage& st,
                                                const TB* __restrict__ y, double dt, int cur, unsigned char* smem_raw,
-                                               uint64_t* mbar, uint32_t tmem, uint32_t parity, int* fail) {
+                                               uint64_t* mbar, uint32_t tmem, uint32_t parity, bool build_b,
+                                               int* fail) {
   const int n = I->n, n2 = I->n2, K = I->K, void_idx = I->nh, tile = I->tile;
   const long long base = I->elem_off;
   float2* yt = reinterpret_cast<float2*>(smem_raw);  // tile*n2
@@ -873,13 +886,14 @@ __device__ __forceinline__ double diag_tile_tc(const DiagInst* __restrict__ I, c
       (reinterpret_cast<uintptr_t>(nks + tile * K) + 127) & ~static_cast<uintptr_t>(127));
   float* Ah = reinterpret_cast<float*>(opnd);
   float* Al = Ah + tc_operand_bytes(n) / (2 * sizeof(float));
-  float* Bh = reinterpret_cast<float*>(opnd + (tc_region_bytes(n, tile) + 127) / 128 * 128);
+  float* Bh = reinterpret_cast<float*>(opnd + tc_operand_bytes(n));
   float* Bl = Bh + tc_b_bytes(n) / (2 * sizeof(float));
   const int ld = n + 1, P = n * ld;
-  float* X1 = reinterpret_cast<float*>(opnd);
+  float* X1 = reinterpret_cast<float*>(opnd + tc_operand_bytes(n) + tc_b_bytes(n));
   float* Y1 = X1 + tile * P;
   float* X2 = Y1 + tile * P;
   float* Y2 = X2 + tile * P;
+  float2* Dp = reinterpret_cast<float2*>(Y2 + tile * P);  // tile*n2 damping + bath partial sums
   const float2* __restrict__ ngd = I->ngd_f;
   const float2* __restrict__ cpl = I->c_plus_f;
   const float2* __restrict__ cmi = I->c_minus_f;
@@ -892,6 +906,7 @@ __device__ __forceinline__ double diag_tile_tc(const DiagInst* __restrict__ I, c
   const TB* __restrict__ yi = y + base;
   const int l0 = td.l0, nt = td.nt, ne = nt * n2;
   const TB* __restrict__ ysrc = yi + static_cast<size_t>(l0) * n2;
+  const float r_n = 1.0f / n, r_n2 = 1.0f / n2;
   for (int i = threadIdx.x; i < ne; i += blockDim.x) yt[i] = ldc<float>(ysrc + i);
   for (int i = threadIdx.x; i < nt * K; i += blockDim.x) {
     const size_t gi = static_cast<size_t>(l0) * K + i;
@@ -900,15 +915,13 @@ __device__ __forceinline__ double diag_tile_tc(const DiagInst* __restrict__ I, c
     nks[i] = __ldg(I->nidx + gi);
   }
   __syncthreads();
-  tc_issue(yt, I->H_f, n, nt, Ah, Al, Bh, Bl, mbar, tmem);
-  // damping and bath terms while the tensor cores work
-  float2 part[kTcPerThread];
-#pragma unroll
-  for (int j = 0; j < kTcPerThread; ++j) {
-    const int i = threadIdx.x + j * blockDim.x;
+  tc_issue(yt, I->H_f, build_b, n, nt, Ah, Al, Bh, Bl, mbar, tmem);
+  // damping and bath terms while the tensor cores work (each thread keeps its
+  // elements' partial sums in Dp and reads them back itself)
+  for (int i = threadIdx.x; i < ne; i += blockDim.x) {
     float2 D = make_float2(0.f, 0.f);
-    if (i < ne) {
-      const int lt = i / n2, e = i - lt * n2;
+    {
+      const int lt = small_div(i, r_n2), e = i - lt * n2;
       const float2 g0 = ngd[l0 + lt], g1 = csd[e];
       cfma(D, make_float2(g0.x + g1.x, g0.y + g1.y), yt[i]);
       const int* p1row = p1s + lt * K;
@@ -954,7 +967,7 @@ __device__ __forceinline__ double diag_tile_tc(const DiagInst* __restrict__ I, c
         for (int q = 0; q < 8; ++q) cfma(D, cf[q], v[q]);
       }
     }
-    part[j] = D;
+    Dp[i] = D;
   }
   if (!tc_readback(n, nt, X1, Y1, X2, Y2, mbar, tmem, parity)) {
     if (threadIdx.x == 0 && st.ctl) st.ctl->status = 2;  // tensor-core wait gave up
@@ -962,30 +975,30 @@ __device__ __forceinline__ double diag_tile_tc(const DiagInst* __restrict__ I, c
     return 0.0;
   }
   double local = 0.0;
-#pragma unroll
-  for (int j = 0; j < kTcPerThread; ++j) {
-    const int i = threadIdx.x + j * blockDim.x;
-    if (i < ne) {
-      const int lt = i / n2, e = i - lt * n2, a = e / n, b = e - a * n;
-      const int o = lt * P + a * ld + b;
-      float2 D = part[j];
-      D.x += X1[o] + X2[o];
-      D.y += Y1[o] + Y2[o];
-      const size_t gi = static_cast<size_t>(base + static_cast<long long>(l0) * n2 + i);
-      const EpiPre pre = epi_pre<float>(st, gi, cur);
-      local += epi_post<float>(st, gi, D, dt, cur, pre);
-    }
+  for (int i = threadIdx.x; i < ne; i += blockDim.x) {
+    const int lt = small_div(i, r_n2), e = i - lt * n2, a = small_div(e, r_n);
+    const int o = i + lt * n + a;  // lt * P + a * (n + 1) + b
+    float2 D = Dp[i];
+    D.x += X1[o] + X2[o];
+    D.y += Y1[o] + Y2[o];
+    const size_t gi = static_cast<size_t>(base + static_cast<long long>(l0) * n2 + i);
+    const EpiPre pre = epi_pre<float>(st, gi, cur);
+    local += epi_post<float>(st, gi, D, dt, cur, pre);
   }
-  __syncthreads();  // the next tile restages shared memory
+  // no barrier here: the next tile overwrites the input rows and A only after
+  // this tile's read-back barriers (their last readers ran before them), and
+  // the products only after its own MMA wait
   return local;
 }
 
 // The diagonal-coupling stage with the commutators on the tensor cores
-// (diag_tile_tc); every instance of the plan is eligible.  256 threads;
-// tensor memory is allocated per CTA (at most two CTAs reside on an SM, so
-// the allocations never exceed the SM's 512 columns).
-template <typename TB>
-__global__ void __launch_bounds__(256, 2) k_rhs_diag_tc(const DiagSet ds, const Stage st) {
+// (diag_tile_tc); every instance of the plan is eligible.  128 or 256
+// threads (four warps cover the 128 tensor-memory lanes); tensor memory is
+// allocated per CTA (at most 16 CTAs of 128 threads reside on an SM, each
+// holding at most 32 columns: the SM's 512).  MINB 2 or 3: the register cap
+// (128 or 80) the autotuner picks between.
+template <typename TB, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_rhs_diag_tc(const DiagSet ds, const Stage st) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   double dt;
   int cur;
@@ -1010,11 +1023,12 @@ __global__ void __launch_bounds__(256, 2) k_rhs_diag_tc(const DiagSet ds, const 
   const uint32_t tmem = *tslot;
   double local = 0.0;
   uint32_t parity = 0;
-  int fail = 0;
+  int fail = 0, b_inst = -1;
   for (int t = blockIdx.x; t < ds.n_tiles; t += gridDim.x) {
     const DiagTile td = ds.tiles[t];
     const DiagInst* I = ds.inst + td.inst;
-    local += diag_tile_tc<TB>(I, td, st, y, dt, cur, smem_raw, mbar, tmem, parity, &fail);
+    local += diag_tile_tc<TB>(I, td, st, y, dt, cur, smem_raw, mbar, tmem, parity, td.inst != b_inst, &fail);
+    b_inst = td.inst;
     if (fail) break;
     parity ^= 1u;
   }
@@ -1330,7 +1344,7 @@ size_t diag_tile_smem_tc(int n, int K, int tile) {
   const size_t n2 = static_cast<size_t>(n) * n;
   size_t b = sizeof(float2) * n2 * tile + 3 * sizeof(int) * static_cast<size_t>(tile) * K;
   b = (b + 127) / 128 * 128;
-  b += (tc_region_bytes(n, tile) + 127) / 128 * 128 + tc_b_bytes(n);
+  b += tc_operand_bytes(n) + tc_b_bytes(n) + tc_product_bytes(n, tile);
   return (b + 15) / 16 * 16 + 128 + 16;  // alignment slack, then the mbarrier and tensor-memory address slot
 }
 
@@ -1360,7 +1374,7 @@ static cudaError_t launch_typed(const RhsModel& m, const DiagSet* ds, const Stag
     auto kern = k_rhs_diag<TC, TB, 1>;
     if constexpr (std::is_same<TC, float>::value) {
       if (ds->min_blocks == 3) kern = k_rhs_diag<TC, TB, 3>;
-      if (ds->tcore) kern = k_rhs_diag_tc<TB>;
+      if (ds->tcore) kern = ds->min_blocks == 3 ? k_rhs_diag_tc<TB, 3> : k_rhs_diag_tc<TB, 2>;
     }
     if (dsm > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dsm));

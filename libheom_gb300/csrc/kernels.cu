@@ -474,9 +474,11 @@ __host__ __device__ inline size_t tc_operand_bytes(int n) {
 __host__ __device__ inline size_t tc_product_bytes(int n, int tile) {
   return 4 * sizeof(float) * static_cast<size_t>(tile) * n * (n + 1) + sizeof(float2) * static_cast<size_t>(tile) * n * n;
 }
-// x / d for 0 <= x < 2^12 and 1 <= d <= 2^10 from rd = 1.0f / d: (x + 0.5) / d
-// lies at least 0.5 / d away from an integer and the two roundings move it by
-// less than (x / d + 1) * 2^-23, so truncation gives the exact quotient
+// x / d for 0 <= x < 2^16 and 1 <= d <= 2^12 from rd = 1.0f / d (correctly
+// rounded): (x + 0.5) / d lies at least 0.5 / d away from an integer and the
+// two roundings move it by less than (x / d + 1) * 2^-23, so truncation gives
+// the exact quotient (checked exhaustively over that range against integer
+// division)
 __device__ __forceinline__ int small_div(int x, float rd) {
   return __float2int_rz(__fmul_rn(static_cast<float>(x) + 0.5f, rd));
 }

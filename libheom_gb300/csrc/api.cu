@@ -357,6 +357,13 @@ struct heomgb_qme_solver {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double busy_ms = 0.0;
   long long replayed_kernels = 0;
+  // resident Dormand-Prince interval (k_dp_resident): one cooperative launch
+  // per output interval instead of graph replays of the stage kernels
+  bool resident = false;
+  int res_grid = 0, res_apc = 0, res_block = 0;
+  size_t res_smem = 0;
+  unsigned long long* res_bar = nullptr;
+  double* res_partials = nullptr;
   ~heomgb_qme_solver() {
     if (g_small) cudaGraphExecDestroy(g_small);
     if (g_big) cudaGraphExecDestroy(g_big);
@@ -940,6 +947,25 @@ void run_diff_rm(heomgb_qme* q, double2* drho, const double2* rho, const double*
 
 // ------------------------------------------------------------------ solvers
 void autotune(heomgb_qme_solver* qs);
+void plan_resident(heomgb_qme_solver* qs);
+
+// Arguments of k_dp_resident for the solver's buffers and its tuned shape.
+ResidentArgs resident_args(heomgb_qme_solver* qs) {
+  ResidentArgs a{};
+  a.inst = qs->q->dinst;
+  a.ctl = qs->ctl;
+  for (int i = 0; i < 2; ++i) {
+    a.S[i] = qs->S[i];
+    a.Yb[i] = static_cast<float2*>(qs->Yb[i]);
+    a.Ytmp[i] = static_cast<float2*>(qs->Ytmp[i]);
+  }
+  a.partials = qs->res_partials;
+  a.bar = qs->res_bar;
+  a.n_total = qs->N;
+  a.max_attempts = 2000000LL;
+  a.ados_per_cta = qs->res_apc;
+  return a;
+}
 Stage solver_stage(heomgb_qme_solver* qs);
 
 void alloc_solver(heomgb_qme_solver* qs) {
@@ -985,6 +1011,7 @@ void alloc_solver(heomgb_qme_solver* qs) {
     qs->grid = rhs_grid_size(q->dm, q->path, qs->block, q->n_sm);
   }
   qs->partials = static_cast<double*>(A.alloc(sizeof(double) * std::max(qs->grid, 1)));
+  plan_resident(qs);
 }
 
 // Tile shape search for the diagonal-coupling kernel: CTA size x elements per
@@ -1130,6 +1157,99 @@ void autotune(heomgb_qme_solver* qs) {
     build_plan(qs->plan, insts, best_tc_b, 1, best_tc_m, qs->mixed, q->n_sm, qs->stream, true);
   else
     build_plan(qs->plan, insts, best_b, best_e, best_m, qs->mixed, q->n_sm, qs->stream);
+}
+
+// The resident Dormand-Prince interval applies to one mixed-form model on the
+// diagonal-coupling path without a terminator, when a co-resident grid holds
+// its state in shared memory.  Fewer ADOs per CTA shorten each stage, more
+// CTAs lengthen each grid barrier, so the grid is tuned: every co-resident
+// shape (1 to 8 CTAs per SM) runs one Dormand-Prince attempt over the
+// solver's zeroed buffers and the fastest is kept.  HEOMGB_RESIDENT=0 keeps
+// the stage kernels; HEOMGB_RESIDENT_PER_SM=<n> pins the shape.
+void plan_resident(heomgb_qme_solver* qs) {
+  heomgb_qme* q = qs->q;
+  qs->resident = false;
+  if (qs->kind != HEOMGB_RKDP || !qs->mixed || q->path != PATH_DIAG || qs->qmes.size() != 1 || qs->term) return;
+  if (const char* env = std::getenv("HEOMGB_RESIDENT"))
+    if (std::string(env) == "0") return;
+  int coop = 0;
+  ck(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, q->device), "device attribute");
+  if (!coop) return;
+  const DiagInst& I = q->dinst;
+  const bool hreal = I.h_real != 0;
+  int pin = 0;
+  if (const char* env = std::getenv("HEOMGB_RESIDENT_PER_SM")) pin = std::atoi(env);
+  struct Shape {
+    int grid, apc, block;
+    size_t smem;
+  };
+  std::vector<Shape> shapes;
+  int last_grid = -1;
+  for (int per_sm = 8; per_sm >= 1; --per_sm) {
+    if (pin && per_sm != pin) continue;
+    const int target = per_sm * q->n_sm;
+    const int apc = (I.nh + target - 1) / target;
+    const int grid = (I.nh + apc - 1) / apc;
+    if (grid == last_grid) continue;
+    const size_t smem = resident_smem(I.n2, apc);
+    if (smem > 200 * 1024) continue;
+    const int E = apc * I.n2;  // kResidentEpt elements per thread
+    const int block = std::max(64, ((E + kResidentEpt - 1) / kResidentEpt + 31) / 32 * 32);
+    if (block > kResidentMaxBlock) continue;
+    const int nb = resident_blocks_per_sm(hreal, block, smem);
+    if (nb < 1 || static_cast<long long>(nb) * q->n_sm < grid) continue;
+    shapes.push_back(Shape{grid, apc, block, smem});
+    last_grid = grid;
+  }
+  if (shapes.empty()) return;
+  qs->res_bar = static_cast<unsigned long long*>(qs->arena.alloc(kResidentBarWords * sizeof(unsigned long long)));
+  qs->res_partials = static_cast<double*>(qs->arena.alloc(sizeof(double) * shapes.front().grid));
+  size_t best = 0;
+  if (shapes.size() > 1) {
+    const size_t bd = sizeof(double2) * qs->N, bb = sizeof(float2) * qs->N;
+    for (int i = 0; i < 2; ++i) {
+      ck(cudaMemsetAsync(qs->S[i], 0, bd, qs->stream), "memset");
+      ck(cudaMemsetAsync(qs->Yb[i], 0, bb, qs->stream), "memset");
+    }
+    cudaEvent_t e0, e1;
+    ck(cudaEventCreate(&e0), "event");
+    ck(cudaEventCreate(&e1), "event");
+    float best_ms = 1e30f;
+    for (size_t i = 0; i < shapes.size(); ++i) {
+      qs->res_grid = shapes[i].grid;
+      qs->res_apc = shapes[i].apc;
+      qs->res_block = shapes[i].block;
+      qs->res_smem = shapes[i].smem;
+      float ms_i = 1e30f;
+      for (int r = 0; r < 4; ++r) {  // one warm-up, best of three
+        // one attempt: zero state, zero error, accepted, t_bound reached
+        ck(launch_ctl_init(qs->ctl, 0.0, 1e-3, 1e-3, 1e-8, 1e-8, 0, qs->stream), "ctl init");
+        ck(cudaMemsetAsync(qs->res_bar, 0, kResidentBarWords * sizeof(unsigned long long), qs->stream), "memset");
+        ck(cudaEventRecord(e0, qs->stream), "event");
+        ck(launch_dp_resident(resident_args(qs), hreal, qs->res_grid, qs->res_block, qs->res_smem, qs->stream),
+           "resident tune");
+        ck(cudaEventRecord(e1, qs->stream), "event");
+        ck(cudaEventSynchronize(e1), "event sync");
+        float ms = 0.f;
+        ck(cudaEventElapsedTime(&ms, e0, e1), "event time");
+        if (r > 0) ms_i = std::min(ms_i, ms);
+      }
+      unsigned long long flag = 0;
+      ck(cudaMemcpy(&flag, qs->res_bar + 16, sizeof(flag), cudaMemcpyDeviceToHost), "barrier read");
+      if (flag) throw cuda_error("resident Dormand-Prince interval: a grid barrier wait ran out");
+      if (ms_i < best_ms) {
+        best_ms = ms_i;
+        best = i;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  qs->res_grid = shapes[best].grid;
+  qs->res_apc = shapes[best].apc;
+  qs->res_block = shapes[best].block;
+  qs->res_smem = shapes[best].smem;
+  qs->resident = true;
 }
 
 Stage solver_stage(heomgb_qme_solver* qs) {
@@ -1312,6 +1432,37 @@ void solve_fixed(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwarg
   qs->n_accepted += m + 1;
 }
 
+// adaptive_step_size_solver::solve_1 + rkdp::solve_adaptive_step as one
+// resident launch (k_dp_resident).
+int solve_resident(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwargs* kw, int cur) {
+  if (qs->dt_save == -1.0) qs->dt_save = need_kw(kw, kw ? kw->has_dt : 0, kw ? kw->dt : 0, "dt");
+  const double atol = need_kw(kw, kw ? kw->has_atol : 0, kw ? kw->atol : 0, "atol");
+  const double rtol = need_kw(kw, kw ? kw->has_rtol : 0, kw ? kw->rtol : 0, "rtol");
+  double dt = qs->dt_save;
+  if (t0 + dt > t1) dt = t1 - t0;
+  ck(launch_ctl_init(qs->ctl, t0, dt, t1, atol, rtol, cur, qs->stream), "ctl init");
+  ck(cudaMemsetAsync(qs->res_bar, 0, kResidentBarWords * sizeof(unsigned long long), qs->stream), "barrier reset");
+  busy_begin(qs);
+  ck(launch_dp_resident(resident_args(qs), qs->q->dinst.h_real != 0, qs->res_grid, qs->res_block, qs->res_smem,
+                        qs->stream),
+     "resident interval");
+  busy_end(qs);
+  qs->replayed_kernels += 1;
+  unsigned long long flag = 0;
+  ck(cudaMemcpyAsync(qs->ctl_host, qs->ctl, sizeof(DpCtl), cudaMemcpyDeviceToHost, qs->stream), "ctl read");
+  ck(cudaMemcpyAsync(&flag, qs->res_bar + 16, sizeof(flag), cudaMemcpyDeviceToHost, qs->stream), "barrier read");
+  ck(cudaStreamSynchronize(qs->stream), "solve sync");
+  busy_collect(qs);
+  if (flag) throw cuda_error("resident Dormand-Prince interval: a grid barrier wait ran out");
+  if (qs->ctl_host->status == 3) throw numeric_error("Dormand-Prince attempt cap reached");
+  if (qs->ctl_host->status) throw numeric_error("non-finite step size in Dormand-Prince control");
+  qs->dt_save = qs->ctl_host->dt;
+  qs->n_attempts += qs->ctl_host->attempts;
+  qs->n_accepted += qs->ctl_host->accepted;
+  qs->n_rhs += 7 * qs->ctl_host->attempts;
+  return qs->ctl_host->cur;
+}
+
 // adaptive_step_size_solver::solve_1 + rkdp::solve_adaptive_step
 // (adaptive_step_size_solver.h:32-56, rkdp.h:81-179) with the controller on
 // the device; the host only polls the `done` flag between graph replays.
@@ -1385,7 +1536,8 @@ void solve_impl(heomgb_qme_solver* qs, void* rho, bool host, const double* t_lis
     state_to_bulk(qs, 0);
     int cur = 0;
     if (qs->kind == HEOMGB_RKDP)
-      cur = solve_adaptive(qs, t_list[i], t_list[i + 1], kw, 0);
+      cur = qs->resident ? solve_resident(qs, t_list[i], t_list[i + 1], kw, 0)
+                         : solve_adaptive(qs, t_list[i], t_list[i + 1], kw, 0);
     else
       solve_fixed(qs, t_list[i], t_list[i + 1], kw);
     if (qs->col_major) {
@@ -1752,6 +1904,15 @@ heomgb_status heomgb_qme_solver_tuning(const heomgb_qme_solver* qs, int* block, 
     if (elems_per_thread) *elems_per_thread = diag ? qs->plan.ept : 0;
     if (n_tiles) *n_tiles = diag ? qs->plan.ds.n_tiles : 0;
     if (min_blocks) *min_blocks = diag ? qs->plan.min_blocks : 0;
+  });
+}
+
+heomgb_status heomgb_qme_solver_resident(const heomgb_qme_solver* qs, int* on, int* grid, int* ados_per_cta) {
+  return guard([&] {
+    require(qs != nullptr && on != nullptr, "null argument");
+    *on = qs->resident ? 1 : 0;
+    if (grid) *grid = qs->resident ? qs->res_grid : 0;
+    if (ados_per_cta) *ados_per_cta = qs->resident ? qs->res_apc : 0;
   });
 }
 

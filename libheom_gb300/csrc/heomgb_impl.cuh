@@ -163,6 +163,30 @@ struct DiagSet {
   int tmem_cols;            // tensor-memory columns a CTA of k_rhs_diag_tc allocates
 };
 
+// Resident Dormand-Prince interval (k_dp_resident): one cooperative launch of
+// CTAs of at most kResidentMaxBlock threads, CTA b owning ADOs
+// [b*ados_per_cta, ...).
+constexpr int kResidentMaxBlock = 320;
+constexpr int kResidentEpt = 2;            // elements per thread (fixed for the interval)
+constexpr int kResidentBarWords = 32;       // grid-barrier counter and flag (64-bit words)
+struct ResidentArgs {
+  DiagInst inst;            // the model (diagonal coupling, mixed form, one instance)
+  DpCtl* ctl;               // controller: initialised before the launch, final state written back
+  double2* S[2];            // FP64 states; S[ctl->cur] holds the interval's initial state
+  float2* Yb[2];            // FP32 copies of the states (Yb[ctl->cur] valid at launch)
+  float2* Ytmp[2];          // stage inputs 2..6 for the neighbour gathers (alternating)
+  double* partials;         // per-CTA error-norm partial sums (grid entries)
+  unsigned long long* bar;  // grid barrier: kResidentBarWords words, zero at launch (grid_barrier)
+  long long n_total;        // elements of the state
+  long long max_attempts;   // attempts before the interval gives up (status 3)
+  int ados_per_cta;
+  int pad_;
+};
+size_t resident_smem(int n2, int ados_per_cta);
+int resident_blocks_per_sm(bool hreal, int block, size_t smem);
+cudaError_t launch_dp_resident(const ResidentArgs& args, bool hreal, int grid, int block, size_t smem,
+                               cudaStream_t s);
+
 // Launchers (kernels.cu).  `mixed` selects FP32 bulk arithmetic; `in_double`
 // says the RHS input is a double2 array even in mixed mode.  `ds` describes
 // the diagonal-coupling work (PATH_DIAG only).

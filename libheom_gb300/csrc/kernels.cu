@@ -1045,6 +1045,306 @@ __global__ void __launch_bounds__(256, MINB) k_rhs_diag_tc(const DiagSet ds, con
   if (st.kind == EPI_DP7) dp7_finish(st, local, ds.total);
 }
 
+// ------------------------------------------------------------------ resident Dormand-Prince interval
+// The whole output interval of the mixed form's Dormand-Prince solver in one
+// cooperative launch, for models small enough that the CTAs together hold
+// the state in shared memory.  A CTA owns a contiguous range of ADOs and
+// keeps their FP64 state and candidate state, the six FP32 stage vectors and
+// two FP32 stage-input copies in shared memory; of each stage only the stage
+// input goes through global memory (written for the neighbour gathers of the
+// other CTAs and read back with L1-bypassing loads after a grid barrier).
+// The arithmetic per element is that of k_rhs_diag with the mixed form's
+// Dormand-Prince epilogues (epi_pre/epi_post: EPI_DP, EPI_DP7), in the same
+// operation order.  The error norm is summed per CTA and published; after
+// one more barrier every CTA adds the partial sums in index order and runs
+// the step controller on its own copy of the controller state, so all CTAs
+// take the same decisions without a further exchange.  Grid barriers are
+// bounded spins: one that runs out sets the failure flag and the CTAs leave.
+// Grid barrier of a cooperative launch (every CTA resident), in the
+// arrive/wait pattern of CUTLASS's GenericBarrier: each CTA syncs, one thread
+// adds 1 to a monotonic 64-bit arrival counter with release semantics and
+// spins with acquire loads until the counter reaches the barrier's target
+// (gen + 1) * gridDim.x, then the CTA syncs again.  bar[0] is the counter,
+// bar[16] the failure flag (its own 128-byte line); both zero at launch.  The
+// spin is bounded; returns false, CTA-uniformly, if it ran out.
+__device__ bool grid_barrier(unsigned long long* bar, unsigned long long& gen) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned long long target = (gen + 1) * gridDim.x;
+    const unsigned long long one = 1;
+    asm volatile("red.release.gpu.global.add.u64 [%0], %1;\n" ::"l"(bar), "l"(one) : "memory");
+    for (int it = 0;; ++it) {
+      unsigned long long v;
+      asm volatile("ld.acquire.gpu.global.u64 %0, [%1];\n" : "=l"(v) : "l"(bar) : "memory");
+      if (v >= target) break;
+      if (it >= (1 << 24)) {
+        ok = 0;
+        atomicOr(bar + 16, 1ull);
+        break;
+      }
+    }
+    ++gen;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+template <bool HREAL>
+__global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const ResidentArgs R) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ DpCtl c;
+  const DiagInst& I = R.inst;
+  const int n = I.n, n2 = I.n2, K = I.K, void_idx = I.nh;
+  const int l0 = min(I.nh, static_cast<int>(blockIdx.x) * R.ados_per_cta);
+  const int l1 = min(I.nh, l0 + R.ados_per_cta);
+  const int E = (l1 - l0) * n2;
+  const size_t gb = static_cast<size_t>(l0) * n2;
+  float2* Hs = reinterpret_cast<float2*>(smem_raw);
+  double2* Sv = reinterpret_cast<double2*>(smem_raw + ((sizeof(float2) * n2 + 15) & ~static_cast<size_t>(15)));
+  float2* Kv = reinterpret_cast<float2*>(Sv + 2 * static_cast<size_t>(E));  // k_1..k_6
+  float2* yt = Kv + 6 * static_cast<size_t>(E);                             // stage inputs (two copies)
+  const float2* __restrict__ ngd = I.ngd_f;
+  const float2* __restrict__ cpl = I.c_plus_f;
+  const float2* __restrict__ cmi = I.c_minus_f;
+  const float2* __restrict__ csd = I.c_sd_f;
+  const bool sqn = I.sqrt_norm != 0;
+  for (int i = threadIdx.x; i < n2; i += blockDim.x) Hs[i] = I.H_f[i];
+  if (threadIdx.x == 0) c = *R.ctl;
+  __syncthreads();
+  {
+    const int cur = c.cur;
+    for (int le = threadIdx.x; le < E; le += blockDim.x) {
+      const double2 v = R.S[cur][gb + le];
+      Sv[static_cast<size_t>(cur) * E + le] = v;
+      yt[le] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+    }
+  }
+  // the thread's elements, fixed for the interval: le = threadIdx.x + r * blockDim.x
+  // (r < kResidentEpt; the host sizes the CTA so that they cover E)
+  int el_lt[kResidentEpt], el_e[kResidentEpt], el_a[kResidentEpt], el_b[kResidentEpt];
+  int el_pb[kResidentEpt], el_pe[kResidentEpt], el_mb[kResidentEpt], el_me[kResidentEpt];
+  float2 el_g[kResidentEpt];
+#pragma unroll
+  for (int r = 0; r < kResidentEpt; ++r) {
+    const int le = threadIdx.x + r * blockDim.x;
+    const int lec = le < E ? le : 0;
+    const int lt = lec / n2, e = lec - lt * n2, a = e / n;
+    el_lt[r] = lt;
+    el_e[r] = e;
+    el_a[r] = a;
+    el_b[r] = e - a * n;
+    el_pb[r] = __ldg(I.plus_ptr + e);
+    el_pe[r] = __ldg(I.plus_ptr + e + 1);
+    el_mb[r] = __ldg(I.minus_ptr + e);
+    el_me[r] = __ldg(I.minus_ptr + e + 1);
+    const float2 g0 = ngd[min(l0 + lt, I.nh - 1)], g1 = csd[e];
+    el_g[r] = make_float2(g0.x + g1.x, g0.y + g1.y);
+  }
+  unsigned long long gen = 0;
+  bool ok = true;
+  long long attempts = 0;
+  while (!c.done) {
+    if (attempts++ >= R.max_attempts) {
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        c.status = 3;
+        c.done = 1;
+      }
+      __syncthreads();
+      break;
+    }
+    const double dt = c.dt;
+    const float fdt = static_cast<float>(dt);
+    const int cur = c.cur;
+    const double2* Sc = Sv + static_cast<size_t>(cur) * E;
+    double2* Sn = Sv + static_cast<size_t>(1 - cur) * E;
+    double local = 0.0;
+    for (int s = 0; s < 7 && ok; ++s) {
+      // stage input: own ADOs from shared memory, neighbours from global memory
+      const float2* __restrict__ Xg = s == 0 ? R.Yb[cur] : (s < 6 ? R.Ytmp[(s - 1) & 1] : R.Yb[1 - cur]);
+      const float2* Xs = yt + static_cast<size_t>(s & 1) * E;
+      float2* Xn = yt + static_cast<size_t>((s + 1) & 1) * E;
+#pragma unroll
+      for (int r = 0; r < kResidentEpt; ++r) {
+        const int le = threadIdx.x + r * blockDim.x;
+        if (le >= E) continue;
+        const int lt = el_lt[r], e = el_e[r], a = el_a[r], b = el_b[r];
+        const int l = l0 + lt;
+        const float2* yl = Xs + static_cast<size_t>(lt) * n2;
+        // i[H, rho]
+        float2 acc = make_float2(0.f, 0.f);
+        if (HREAL) {
+#pragma unroll 4
+          for (int cc = 0; cc < n; ++cc) {
+            const float hac = Hs[a * n + cc].x, hcb = Hs[cc * n + b].x;
+            const float2 ycb = yl[cc * n + b], yac = yl[a * n + cc];
+            acc.x = fmaf(hac, ycb.x, acc.x);
+            acc.x = fmaf(-hcb, yac.x, acc.x);
+            acc.y = fmaf(hac, ycb.y, acc.y);
+            acc.y = fmaf(-hcb, yac.y, acc.y);
+          }
+        } else {
+          float2 neg = make_float2(0.f, 0.f);
+#pragma unroll 4
+          for (int cc = 0; cc < n; ++cc) {
+            cfma(acc, Hs[a * n + cc], yl[cc * n + b]);
+            cfma(neg, yl[a * n + cc], Hs[cc * n + b]);
+          }
+          acc.x -= neg.x;
+          acc.y -= neg.y;
+        }
+        float2 D = make_float2(-acc.y, acc.x);
+        // damping and bath terms (as k_rhs_diag's finish)
+        cfma(D, el_g[r], yl[e]);
+        const int* __restrict__ p1row = I.p1 + static_cast<size_t>(l) * K;
+        const int* __restrict__ m1row = I.m1 + static_cast<size_t>(l) * K;
+        const int* __restrict__ nrow = I.nidx + static_cast<size_t>(l) * K;
+        const int pb = el_pb[r], pe = el_pe[r], mb = el_mb[r], me = el_me[r];
+        for (int pp = pb, mp = mb; pp < pe || mp < me; pp += 4, mp += 4) {
+          float2 v[8], cf[8];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int p = pp + j;
+            v[j] = cf[j] = make_float2(0.f, 0.f);
+            if (p < pe) {
+              const int k = __ldg(I.plus_mode + p);
+              const int lp = __ldg(p1row + k);
+              if (lp != void_idx) {
+                v[j] = __ldcg(Xg + static_cast<size_t>(lp) * n2 + e);
+                cf[j] = cpl[p];
+                if (sqn) {
+                  const float f = sqrtf(static_cast<float>(__ldg(nrow + k) + 1));
+                  cf[j] = make_float2(f * cf[j].x, f * cf[j].y);
+                }
+              }
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int p = mp + j;
+            v[4 + j] = cf[4 + j] = make_float2(0.f, 0.f);
+            if (p < me) {
+              const int k = __ldg(I.minus_mode + p);
+              const int lm = __ldg(m1row + k);
+              if (lm != void_idx) {
+                const int nk_i = __ldg(nrow + k);
+                const float nk = sqn ? sqrtf(static_cast<float>(nk_i)) : static_cast<float>(nk_i);
+                const float2 cm = cmi[p];
+                v[4 + j] = __ldcg(Xg + static_cast<size_t>(lm) * n2 + e);
+                cf[4 + j] = make_float2(nk * cm.x, nk * cm.y);
+              }
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < 8; ++j) cfma(D, cf[j], v[j]);
+        }
+        // stage epilogue (epi_pre + epi_post, mixed form)
+        const float2 k = make_float2(-fdt * D.x, -fdt * D.y);
+        const size_t g = gb + le;
+        if (s < 5) {  // k_s; next stage input Yb + sum_j A[s+1][j] k_j in FP32
+          Kv[static_cast<size_t>(s) * E + le] = k;
+          const double2 sc = Sc[le];
+          float2 y = make_float2(static_cast<float>(sc.x), static_cast<float>(sc.y));
+          for (int j = 0; j < s; ++j) {
+            const float cj = static_cast<float>(c_dpA[s + 1][j]);
+            const float2 kj = Kv[static_cast<size_t>(j) * E + le];
+            y.x = fmaf(cj, kj.x, y.x);
+            y.y = fmaf(cj, kj.y, y.y);
+          }
+          const float cs = static_cast<float>(c_dpA[s + 1][s]);
+          y = make_float2(fmaf(cs, k.x, y.x), fmaf(cs, k.y, y.y));
+          Xn[le] = y;
+          R.Ytmp[s & 1][g] = y;
+        } else if (s == 5) {  // candidate state rho + sum_j B_j k_j in FP64
+          Kv[5 * static_cast<size_t>(E) + le] = k;
+          double2 y = Sc[le];
+          for (int j = 0; j < 5; ++j) {
+            const double cj = c_dpA[6][j];
+            const float2 kj = Kv[static_cast<size_t>(j) * E + le];
+            y.x = fma(cj, static_cast<double>(kj.x), y.x);
+            y.y = fma(cj, static_cast<double>(kj.y), y.y);
+          }
+          y.x = fma(c_dpA[6][5], static_cast<double>(k.x), y.x);
+          y.y = fma(c_dpA[6][5], static_cast<double>(k.y), y.y);
+          Sn[le] = y;
+          const float2 yb = make_float2(static_cast<float>(y.x), static_cast<float>(y.y));
+          Xn[le] = yb;
+          R.Yb[1 - cur][g] = yb;
+        } else {  // stage 7: e = sum_j E_j k_j in FP32, scaled squared error
+          float2 ee = make_float2(0.f, 0.f);
+          for (int j = 0; j < 6; ++j) {
+            const float cj = static_cast<float>(c_dpE[j]);
+            const float2 kj = Kv[static_cast<size_t>(j) * E + le];
+            ee.x = fmaf(cj, kj.x, ee.x);
+            ee.y = fmaf(cj, kj.y, ee.y);
+          }
+          const float c6 = static_cast<float>(c_dpE[6]);
+          const float ex = fmaf(c6, k.x, ee.x), ey = fmaf(c6, k.y, ee.y);
+          const float2 x1 = Xs[le];
+          const double2 sc = Sc[le];
+          const float2 x2 = make_float2(static_cast<float>(sc.x), static_cast<float>(sc.y));
+          const double m = static_cast<double>(fmaxf(x1.x * x1.x + x1.y * x1.y, x2.x * x2.x + x2.y * x2.y));
+          const float sm = static_cast<float>(c.atol) + static_cast<float>(c.rtol) * sqrtf(static_cast<float>(m));
+          local += static_cast<double>((ex * ex + ey * ey) / (sm * sm));
+        }
+      }
+      if (s < 6) ok = grid_barrier(R.bar, gen);
+    }
+    if (!ok) break;
+    const double part = block_sum(local);
+    if (threadIdx.x == 0) R.partials[blockIdx.x] = part;
+    ok = grid_barrier(R.bar, gen);
+    if (!ok) break;
+    double v = 0.0;
+    for (int i = threadIdx.x; i < static_cast<int>(gridDim.x); i += blockDim.x) v += __ldcg(R.partials + i);
+    v = block_sum(v);
+    if (threadIdx.x == 0) dp_control(&c, v, R.n_total);
+    __syncthreads();
+    // the next attempt's stage-1 input (own part): the FP32 copy of the current state
+    const double2* Snow = Sv + static_cast<size_t>(c.cur) * E;
+    for (int le = threadIdx.x; le < E; le += blockDim.x) {
+      const double2 x = Snow[le];
+      yt[le] = make_float2(static_cast<float>(x.x), static_cast<float>(x.y));
+    }
+    __syncthreads();
+  }
+  if (ok) {
+    const int cur = c.cur;
+    for (int le = threadIdx.x; le < E; le += blockDim.x) R.S[cur][gb + le] = Sv[static_cast<size_t>(cur) * E + le];
+    if (blockIdx.x == 0 && threadIdx.x == 0) *R.ctl = c;
+  }
+}
+
+size_t resident_smem(int n2, int ados_per_cta) {
+  const size_t E = static_cast<size_t>(ados_per_cta) * n2;
+  return ((sizeof(float2) * n2 + 15) & ~static_cast<size_t>(15)) +
+         E * (2 * sizeof(double2) + 6 * sizeof(float2) + 2 * sizeof(float2));
+}
+
+int resident_blocks_per_sm(bool hreal, int block, size_t smem) {
+  auto kern = hreal ? k_dp_resident<true> : k_dp_resident<false>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
+    return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, block, smem) != cudaSuccess) return 0;
+  return nb;
+}
+
+cudaError_t launch_dp_resident(const ResidentArgs& args, bool hreal, int grid, int block, size_t smem,
+                               cudaStream_t s) {
+  auto kern = hreal ? k_dp_resident<true> : k_dp_resident<false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  ResidentArgs a = args;
+  void* params[] = {&a};
+  e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(grid), dim3(block), params, smem, s);
+  ++g_launches;
+  return e;
+}
+
 // ------------------------------------------------------------------ RHS, general V
 // One CTA per ADO at a time; Phi_u / Psi_u (heom_hilb.h:311-342) and the
 // commutators are formed in shared memory for any dense V_u.

@@ -323,10 +323,14 @@ class qme_solver:
         b, e, t, m = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         check(self._lib.heomgb_qme_solver_tuning(self._h, ctypes.byref(b), ctypes.byref(e), ctypes.byref(t),
                                                  ctypes.byref(m)))
-        tc = ctypes.c_int()
+        tc, rs, rg, ra = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         check(self._lib.heomgb_qme_solver_tensor_cores(self._h, ctypes.byref(tc)))
-        return dict(block=b.value, elems_per_thread=e.value, n_tiles=t.value, min_blocks=m.value,
-                    tensor_cores=bool(tc.value))
+        check(self._lib.heomgb_qme_solver_resident(self._h, ctypes.byref(rs), ctypes.byref(rg), ctypes.byref(ra)))
+        out = dict(block=b.value, elems_per_thread=e.value, n_tiles=t.value, min_blocks=m.value,
+                   tensor_cores=bool(tc.value), resident=bool(rs.value))
+        if rs.value:
+            out.update(resident_grid=rg.value, resident_ados_per_cta=ra.value)
+        return out
 
     def stats(self) -> dict:
         r, a, c = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()

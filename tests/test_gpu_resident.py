@@ -1,0 +1,78 @@
+"""Resident Dormand-Prince interval (one cooperative launch per output
+interval, every CTA holding its ADOs' state in shared memory between stages)
+against the per-stage kernels and the FP64 path on the same models.
+
+Both mixed-form variants do the same per-element arithmetic in the same order;
+they can differ only through the order of the error norm's sum over
+elements, which moves step sizes by rounding.  Budget: the system block
+within 1e-6 of FP64 (relative to its largest element), the two variants
+within 1e-6 of each other per ADO, attempt counts within two."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+import libheom_gb300 as lh
+from libheom_gb300 import configs
+
+pytestmark = pytest.mark.gpu
+KW = dict(dt=0.1, atol=1e-8, rtol=1e-8)
+
+
+def run(p, t, monkeypatch, resident, precision="mixed", kw=KW):
+    monkeypatch.setenv("HEOMGB_RESIDENT", "1" if resident else "0")
+    q = lh.from_params(p, precision=precision)
+    qs = lh.qme_solver(q, lh.rkdp())
+    rho = p.rho0_ground()
+    seen = []
+    qs.solve(rho, list(t), lambda tt: seen.append(tt), dict(kw))
+    monkeypatch.delenv("HEOMGB_RESIDENT")
+    assert seen == list(t)
+    return rho.reshape(p.n_hrchy(), p.n_level, p.n_level), qs.stats(), qs.tuning()
+
+
+def ado_rel(a, b):
+    scale = np.abs(b).max(axis=(1, 2), keepdims=True) + 1e-300
+    return float((np.abs(a - b) / scale).max())
+
+
+def compare(p, t, monkeypatch, kw=KW):
+    res, st_r, tune_r = run(p, t, monkeypatch, True, kw=kw)
+    stg, st_s, tune_s = run(p, t, monkeypatch, False, kw=kw)
+    ref, _, _ = run(p, t, monkeypatch, False, precision="fp64", kw=kw)
+    assert tune_r["resident"] and tune_r["resident_grid"] >= 1
+    assert not tune_s["resident"]
+    assert np.all(np.isfinite(res))
+    assert abs(st_r["attempts"] - st_s["attempts"]) <= 2
+    assert st_r["rhs"] == 7 * st_r["attempts"]
+    scale = np.abs(ref[0]).max()
+    assert np.abs(res[0] - ref[0]).max() / scale <= 1e-6
+    assert ado_rel(res, stg) <= 1e-6
+    return st_r
+
+
+def test_resident_exciton7_matches_stage_kernels(monkeypatch):
+    st = compare(configs.exciton_7site(), [0.0, 5.0, 10.0, 20.0], monkeypatch)
+    assert st["accepted"] >= 1
+
+
+def test_resident_complex_hamiltonian_sqrt_normalisation(monkeypatch):
+    p = configs.exciton_7site(depth=3)
+    rng = np.random.default_rng(11)
+    X = rng.uniform(-0.05, 0.05, (7, 7))
+    p = dataclasses.replace(p, H=p.H + 1j * (X - X.T), normalization="sqrt")
+    compare(p, [0.0, 4.0, 8.0], monkeypatch)
+
+
+def test_resident_spin_boson(monkeypatch):
+    p = configs.spin_boson(depth=8)
+    compare(p, [0.0, 2.0, 4.0], monkeypatch, kw=dict(dt=0.01, atol=1e-9, rtol=1e-9))
+
+
+def test_resident_only_where_it_applies(monkeypatch):
+    p = configs.exciton_7site(depth=2)
+    _, _, tune = run(p, [0.0, 1.0], monkeypatch, True, precision="fp64")
+    assert not tune["resident"]  # the FP64 form keeps the stage kernels
+    monkeypatch.setenv("HEOMGB_RESIDENT", "1")
+    qs = lh.qme_solver(lh.from_params(p, precision="mixed"), lh.rk4())
+    assert not qs.tuning()["resident"]  # fixed-step solvers keep the stage kernels

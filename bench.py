@@ -401,15 +401,22 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes_per_launch / avg_launch_s / 1e9
     flops = w.flops_per_launch()
+    tuning = qs.tuning()
+    resident = isinstance(tuning, dict) and tuning.get("resident", False)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": profile_traffic(args.workload, args.form), "peak_source": peak_kind,
-            "kernel": "k_rhs_diag (fused RHS + stage epilogue)",
+            "kernel": ("k_dp_resident (one cooperative launch per output interval: fused RHS, stage epilogues, "
+                       "error norm and step control; state in shared memory)") if resident
+            else "k_rhs_diag (fused RHS + stage epilogue)",
             "alg_bytes_per_launch": alg_bytes_per_launch, "avg_launch_us": avg_launch_s * 1e6,
             "alg_flops_per_launch": flops, "achieved_tflops": flops / avg_launch_s / 1e12,
             "fma_peaks_tflops": {"fp64": fma_peaks[0], "fp32": fma_peaks[1]},
-            "note": "avg launch time = CUDA-event time of the graph replays / stages evaluated (one stage "
-                    "over the whole state; intra-graph gaps and the no-op launches replayed after an interval "
-                    "ends are included in the time, not in the count)"}
+            "note": ("per stage: CUDA-event time of the resident launches / stages evaluated (grid barriers "
+                     "included); bytes per stage are the algorithmic bytes of one stage over the whole state, "
+                     "most of which stay in shared memory and L2") if resident
+            else ("avg launch time = CUDA-event time of the graph replays / stages evaluated (one stage "
+                  "over the whole state; intra-graph gaps and the no-op launches replayed after an interval "
+                  "ends are included in the time, not in the count)")}
     line = {"metric": "ADO-updates/s", "value": value, "unit": "ADO-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -417,7 +424,7 @@ def run_ours(args):
             "config": {"workload": args.workload, **w.describe(), "solver": wl["solver"], "t_final": wl["t_final"],
                        "kwargs": wl["kw"], "form": args.form, "parallelism": f"replicas x{world}",
                        "l2": "flushed between steps (512 MiB write)"},
-            "max_abs_err_vs_fp64": max_err, "plain_fp64": plain, "tuning": qs.tuning(),
+            "max_abs_err_vs_fp64": max_err, "plain_fp64": plain, "tuning": tuning,
             "attempts_per_step": rhs // max(1, args.steps) // per_rhs,
             "gpu_launches": launches, "e2e": e2e, "roofline": roof, "clocks": clocks}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -755,6 +755,8 @@ void build_model(heomgb_qme* q) {
         pp[e + 1] = static_cast<int>(pmode.size());
         pm[e + 1] = static_cast<int>(mmode.size());
       }
+    int max_terms = 0;
+    for (int e = 0; e < n2; ++e) max_terms = std::max({max_terms, pp[e + 1] - pp[e], pm[e + 1] - pm[e]});
     m.plus_ptr = q->arena.upload(pp, s);
     m.plus_mode = q->arena.upload(pmode, s);
     m.minus_ptr = q->arena.upload(pm, s);
@@ -779,6 +781,7 @@ void build_model(heomgb_qme* q) {
       di.h_sym = sym ? 1 : 0;
     }
     di.sqrt_norm = m.sqrt_norm;
+    di.max_terms = max_terms;
     di.elem_off = 0;
     di.p1 = m.p1;
     di.m1 = m.m1;
@@ -1170,6 +1173,7 @@ void plan_resident(heomgb_qme_solver* qs) {
   heomgb_qme* q = qs->q;
   qs->resident = false;
   if (qs->kind != HEOMGB_RKDP || !qs->mixed || q->path != PATH_DIAG || qs->qmes.size() != 1 || qs->term) return;
+  if (q->dinst.max_terms > kResidentTerms / 2) return;  // the per-element term table holds 4 + 4
   if (const char* env = std::getenv("HEOMGB_RESIDENT"))
     if (std::string(env) == "0") return;
   int coop = 0;

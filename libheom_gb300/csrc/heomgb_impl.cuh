@@ -147,7 +147,7 @@ struct DiagInst {
   int term_first;
   int sqrt_norm;            // 1: +1 terms scale by sqrt(n_k+1), -1 terms by sqrt(n_k) (else 1 and n_k)
   int h_sym;                // H real and symmetric (the tensor-core commutator's condition)
-  int pad_;
+  int max_terms;            // max over elements of max(+1 terms, -1 terms)
 };
 struct DiagTile {
   int inst, l0, nt, pad;
@@ -168,6 +168,7 @@ struct DiagSet {
 // [b*ados_per_cta, ...).
 constexpr int kResidentMaxBlock = 320;
 constexpr int kResidentEpt = 2;            // elements per thread (fixed for the interval)
+constexpr int kResidentTerms = 8;          // bath-term slots per element: 4 (+1 terms) + 4 (-1 terms)
 constexpr int kResidentBarWords = 32;       // grid-barrier counter and flag (64-bit words)
 struct ResidentArgs {
   DiagInst inst;            // the model (diagonal coupling, mixed form, one instance)

@@ -1106,6 +1106,11 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
   double2* Sv = reinterpret_cast<double2*>(smem_raw + ((sizeof(float2) * n2 + 15) & ~static_cast<size_t>(15)));
   float2* Kv = reinterpret_cast<float2*>(Sv + 2 * static_cast<size_t>(E));  // k_1..k_6
   float2* yt = Kv + 6 * static_cast<size_t>(E);                             // stage inputs (two copies)
+  // bath terms of every element, fixed for the interval (slot-major): the
+  // neighbour element's offset in the state (-1: none) and its coefficient;
+  // slots 0-3 hold the +1 terms, 4-7 the -1 terms, in k_rhs_diag's order
+  int* Toff = reinterpret_cast<int*>(yt + 2 * static_cast<size_t>(E));
+  float2* Tcf = reinterpret_cast<float2*>(Toff + kResidentTerms * static_cast<size_t>(E));
   const float2* __restrict__ ngd = I.ngd_f;
   const float2* __restrict__ cpl = I.c_plus_f;
   const float2* __restrict__ cmi = I.c_minus_f;
@@ -1123,9 +1128,10 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
     }
   }
   // the thread's elements, fixed for the interval: le = threadIdx.x + r * blockDim.x
-  // (r < kResidentEpt; the host sizes the CTA so that they cover E)
+  // (r < kResidentEpt; the host sizes the CTA so that they cover E), and
+  // their bath-term table (the host admits models with at most 4 + 4 terms
+  // per element)
   int el_lt[kResidentEpt], el_e[kResidentEpt], el_a[kResidentEpt], el_b[kResidentEpt];
-  int el_pb[kResidentEpt], el_pe[kResidentEpt], el_mb[kResidentEpt], el_me[kResidentEpt];
   float2 el_g[kResidentEpt];
 #pragma unroll
   for (int r = 0; r < kResidentEpt; ++r) {
@@ -1136,12 +1142,53 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
     el_e[r] = e;
     el_a[r] = a;
     el_b[r] = e - a * n;
-    el_pb[r] = __ldg(I.plus_ptr + e);
-    el_pe[r] = __ldg(I.plus_ptr + e + 1);
-    el_mb[r] = __ldg(I.minus_ptr + e);
-    el_me[r] = __ldg(I.minus_ptr + e + 1);
-    const float2 g0 = ngd[min(l0 + lt, I.nh - 1)], g1 = csd[e];
+    const int l = min(l0 + lt, I.nh - 1);
+    const float2 g0 = ngd[l], g1 = csd[e];
     el_g[r] = make_float2(g0.x + g1.x, g0.y + g1.y);
+    if (le < E) {
+      const int* __restrict__ p1row = I.p1 + static_cast<size_t>(l) * K;
+      const int* __restrict__ m1row = I.m1 + static_cast<size_t>(l) * K;
+      const int* __restrict__ nrow = I.nidx + static_cast<size_t>(l) * K;
+      const int pb = __ldg(I.plus_ptr + e), pe = __ldg(I.plus_ptr + e + 1);
+      const int mb = __ldg(I.minus_ptr + e), me = __ldg(I.minus_ptr + e + 1);
+      for (int j = 0; j < 4; ++j) {
+        int off = -1;
+        float2 cf = make_float2(0.f, 0.f);
+        const int p = pb + j;
+        if (p < pe) {
+          const int k = __ldg(I.plus_mode + p);
+          const int lp = __ldg(p1row + k);
+          if (lp != void_idx) {
+            off = lp * n2 + e;
+            cf = cpl[p];
+            if (sqn) {
+              const float f = sqrtf(static_cast<float>(__ldg(nrow + k) + 1));
+              cf = make_float2(f * cf.x, f * cf.y);
+            }
+          }
+        }
+        Toff[static_cast<size_t>(j) * E + le] = off;
+        Tcf[static_cast<size_t>(j) * E + le] = cf;
+      }
+      for (int j = 0; j < 4; ++j) {
+        int off = -1;
+        float2 cf = make_float2(0.f, 0.f);
+        const int p = mb + j;
+        if (p < me) {
+          const int k = __ldg(I.minus_mode + p);
+          const int lm = __ldg(m1row + k);
+          if (lm != void_idx) {
+            const int nk_i = __ldg(nrow + k);
+            const float nk = sqn ? sqrtf(static_cast<float>(nk_i)) : static_cast<float>(nk_i);
+            const float2 cm = cmi[p];
+            off = lm * n2 + e;
+            cf = make_float2(nk * cm.x, nk * cm.y);
+          }
+        }
+        Toff[static_cast<size_t>(4 + j) * E + le] = off;
+        Tcf[static_cast<size_t>(4 + j) * E + le] = cf;
+      }
+    }
   }
   unsigned long long gen = 0;
   bool ok = true;
@@ -1167,6 +1214,17 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
       const float2* __restrict__ Xg = s == 0 ? R.Yb[cur] : (s < 6 ? R.Ytmp[(s - 1) & 1] : R.Yb[1 - cur]);
       const float2* Xs = yt + static_cast<size_t>(s & 1) * E;
       float2* Xn = yt + static_cast<size_t>((s + 1) & 1) * E;
+      // the neighbour gathers of all the thread's elements first (independent loads)
+      float2 vv[kResidentEpt][kResidentTerms];
+#pragma unroll
+      for (int r = 0; r < kResidentEpt; ++r) {
+        const int le = threadIdx.x + r * blockDim.x;
+#pragma unroll
+        for (int j = 0; j < kResidentTerms; ++j) {
+          const int off = le < E ? Toff[static_cast<size_t>(j) * E + le] : -1;
+          vv[r][j] = off >= 0 ? __ldcg(Xg + off) : make_float2(0.f, 0.f);
+        }
+      }
 #pragma unroll
       for (int r = 0; r < kResidentEpt; ++r) {
         const int le = threadIdx.x + r * blockDim.x;
@@ -1197,50 +1255,10 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
           acc.y -= neg.y;
         }
         float2 D = make_float2(-acc.y, acc.x);
-        // damping and bath terms (as k_rhs_diag's finish)
+        // damping and bath terms (as k_rhs_diag's finish, same order)
         cfma(D, el_g[r], yl[e]);
-        const int* __restrict__ p1row = I.p1 + static_cast<size_t>(l) * K;
-        const int* __restrict__ m1row = I.m1 + static_cast<size_t>(l) * K;
-        const int* __restrict__ nrow = I.nidx + static_cast<size_t>(l) * K;
-        const int pb = el_pb[r], pe = el_pe[r], mb = el_mb[r], me = el_me[r];
-        for (int pp = pb, mp = mb; pp < pe || mp < me; pp += 4, mp += 4) {
-          float2 v[8], cf[8];
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int p = pp + j;
-            v[j] = cf[j] = make_float2(0.f, 0.f);
-            if (p < pe) {
-              const int k = __ldg(I.plus_mode + p);
-              const int lp = __ldg(p1row + k);
-              if (lp != void_idx) {
-                v[j] = __ldcg(Xg + static_cast<size_t>(lp) * n2 + e);
-                cf[j] = cpl[p];
-                if (sqn) {
-                  const float f = sqrtf(static_cast<float>(__ldg(nrow + k) + 1));
-                  cf[j] = make_float2(f * cf[j].x, f * cf[j].y);
-                }
-              }
-            }
-          }
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int p = mp + j;
-            v[4 + j] = cf[4 + j] = make_float2(0.f, 0.f);
-            if (p < me) {
-              const int k = __ldg(I.minus_mode + p);
-              const int lm = __ldg(m1row + k);
-              if (lm != void_idx) {
-                const int nk_i = __ldg(nrow + k);
-                const float nk = sqn ? sqrtf(static_cast<float>(nk_i)) : static_cast<float>(nk_i);
-                const float2 cm = cmi[p];
-                v[4 + j] = __ldcg(Xg + static_cast<size_t>(lm) * n2 + e);
-                cf[4 + j] = make_float2(nk * cm.x, nk * cm.y);
-              }
-            }
-          }
-#pragma unroll
-          for (int j = 0; j < 8; ++j) cfma(D, cf[j], v[j]);
-        }
+        for (int j = 0; j < kResidentTerms; ++j) cfma(D, Tcf[static_cast<size_t>(j) * E + le], vv[r][j]);
         // stage epilogue (epi_pre + epi_post, mixed form)
         const float2 k = make_float2(-fdt * D.x, -fdt * D.y);
         const size_t g = gb + le;
@@ -1321,7 +1339,8 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
 size_t resident_smem(int n2, int ados_per_cta) {
   const size_t E = static_cast<size_t>(ados_per_cta) * n2;
   return ((sizeof(float2) * n2 + 15) & ~static_cast<size_t>(15)) +
-         E * (2 * sizeof(double2) + 6 * sizeof(float2) + 2 * sizeof(float2));
+         E * (2 * sizeof(double2) + 6 * sizeof(float2) + 2 * sizeof(float2) +
+              kResidentTerms * (sizeof(int) + sizeof(float2)));
 }
 
 int resident_blocks_per_sm(bool hreal, int block, size_t smem) {

@@ -1061,20 +1061,26 @@ __global__ void __launch_bounds__(256, MINB) k_rhs_diag_tc(const DiagSet ds, con
 // take the same decisions without a further exchange.  Grid barriers are
 // bounded spins: one that runs out sets the failure flag and the CTAs leave.
 // Grid barrier of a cooperative launch (every CTA resident), in the
-// arrive/wait pattern of CUTLASS's GenericBarrier: each CTA syncs, one thread
-// adds 1 to a monotonic 64-bit arrival counter with release semantics and
-// spins with acquire loads until the counter reaches the barrier's target
-// (gen + 1) * gridDim.x, then the CTA syncs again.  bar[0] is the counter,
-// bar[16] the failure flag (its own 128-byte line); both zero at launch.  The
-// spin is bounded; returns false, CTA-uniformly, if it ran out.
-__device__ bool grid_barrier(unsigned long long* bar, unsigned long long& gen) {
-  __shared__ int s_ok;
+// arrive/wait pattern of CUTLASS's GenericBarrier, split in two so that a
+// CTA can work on its own data between them.  grid_arrive: the CTA syncs,
+// one thread adds 1 to a monotonic 64-bit arrival counter with release
+// semantics.  grid_wait: that thread spins with acquire loads until the
+// counter reaches (gen + 1) * gridDim.x (gen: barriers completed so far),
+// then the CTA syncs.  bar[0] is the counter, bar[16] the failure flag (its
+// own 128-byte line); both zero at launch.  The spin is bounded; grid_wait
+// returns false, CTA-uniformly, if it ran out.
+__device__ __forceinline__ void grid_arrive(unsigned long long* bar) {
   __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned long long one = 1;
+    asm volatile("red.release.gpu.global.add.u64 [%0], %1;\n" ::"l"(bar), "l"(one) : "memory");
+  }
+}
+__device__ bool grid_wait(unsigned long long* bar, unsigned long long& gen) {
+  __shared__ int s_ok;
   if (threadIdx.x == 0) {
     int ok = 1;
     const unsigned long long target = (gen + 1) * gridDim.x;
-    const unsigned long long one = 1;
-    asm volatile("red.release.gpu.global.add.u64 [%0], %1;\n" ::"l"(bar), "l"(one) : "memory");
     for (int it = 0;; ++it) {
       unsigned long long v;
       asm volatile("ld.acquire.gpu.global.u64 %0, [%1];\n" : "=l"(v) : "l"(bar) : "memory");
@@ -1214,23 +1220,15 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
       const float2* __restrict__ Xg = s == 0 ? R.Yb[cur] : (s < 6 ? R.Ytmp[(s - 1) & 1] : R.Yb[1 - cur]);
       const float2* Xs = yt + static_cast<size_t>(s & 1) * E;
       float2* Xn = yt + static_cast<size_t>((s + 1) & 1) * E;
-      // the neighbour gathers of all the thread's elements first (independent loads)
-      float2 vv[kResidentEpt][kResidentTerms];
+      // own part first (commutator and damping): it reads only this CTA's
+      // copy of the stage input, published by the last grid_arrive's sync
+      float2 Dp[kResidentEpt];
 #pragma unroll
       for (int r = 0; r < kResidentEpt; ++r) {
         const int le = threadIdx.x + r * blockDim.x;
-#pragma unroll
-        for (int j = 0; j < kResidentTerms; ++j) {
-          const int off = le < E ? Toff[static_cast<size_t>(j) * E + le] : -1;
-          vv[r][j] = off >= 0 ? __ldcg(Xg + off) : make_float2(0.f, 0.f);
-        }
-      }
-#pragma unroll
-      for (int r = 0; r < kResidentEpt; ++r) {
-        const int le = threadIdx.x + r * blockDim.x;
+        Dp[r] = make_float2(0.f, 0.f);
         if (le >= E) continue;
         const int lt = el_lt[r], e = el_e[r], a = el_a[r], b = el_b[r];
-        const int l = l0 + lt;
         const float2* yl = Xs + static_cast<size_t>(lt) * n2;
         // i[H, rho]
         float2 acc = make_float2(0.f, 0.f);
@@ -1255,8 +1253,31 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
           acc.y -= neg.y;
         }
         float2 D = make_float2(-acc.y, acc.x);
-        // damping and bath terms (as k_rhs_diag's finish, same order)
-        cfma(D, el_g[r], yl[e]);
+        cfma(D, el_g[r], yl[e]);  // damping (as k_rhs_diag's finish, same order)
+        Dp[r] = D;
+      }
+      // the other CTAs' stage input: wait for their stage s - 1 (stage 1 reads
+      // the state copy, complete before the attempt)
+      if (s > 0) {
+        ok = grid_wait(R.bar, gen);
+        if (!ok) break;
+      }
+      // the neighbour gathers of all the thread's elements (independent loads)
+      float2 vv[kResidentEpt][kResidentTerms];
+#pragma unroll
+      for (int r = 0; r < kResidentEpt; ++r) {
+        const int le = threadIdx.x + r * blockDim.x;
+#pragma unroll
+        for (int j = 0; j < kResidentTerms; ++j) {
+          const int off = le < E ? Toff[static_cast<size_t>(j) * E + le] : -1;
+          vv[r][j] = off >= 0 ? __ldcg(Xg + off) : make_float2(0.f, 0.f);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kResidentEpt; ++r) {
+        const int le = threadIdx.x + r * blockDim.x;
+        if (le >= E) continue;
+        float2 D = Dp[r];
 #pragma unroll
         for (int j = 0; j < kResidentTerms; ++j) cfma(D, Tcf[static_cast<size_t>(j) * E + le], vv[r][j]);
         // stage epilogue (epi_pre + epi_post, mixed form)
@@ -1309,12 +1330,13 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
           local += static_cast<double>((ex * ex + ey * ey) / (sm * sm));
         }
       }
-      if (s < 6) ok = grid_barrier(R.bar, gen);
+      if (s < 6) grid_arrive(R.bar);
     }
     if (!ok) break;
     const double part = block_sum(local);
     if (threadIdx.x == 0) R.partials[blockIdx.x] = part;
-    ok = grid_barrier(R.bar, gen);
+    grid_arrive(R.bar);
+    ok = grid_wait(R.bar, gen);
     if (!ok) break;
     double v = 0.0;
     for (int i = threadIdx.x; i < static_cast<int>(gridDim.x); i += blockDim.x) v += __ldcg(R.partials + i);

@@ -360,7 +360,7 @@ struct heomgb_qme_solver {
   // resident Dormand-Prince interval (k_dp_resident): one cooperative launch
   // per output interval instead of graph replays of the stage kernels
   bool resident = false;
-  int res_grid = 0, res_apc = 0, res_block = 0;
+  int res_grid = 0, res_apc = 0, res_block = 0, res_ept = 2;
   size_t res_smem = 0;
   unsigned long long* res_bar = nullptr;
   double* res_partials = nullptr;
@@ -1166,9 +1166,10 @@ void autotune(heomgb_qme_solver* qs) {
 // diagonal-coupling path without a terminator, when a co-resident grid holds
 // its state in shared memory.  Fewer ADOs per CTA shorten each stage, more
 // CTAs lengthen each grid barrier, so the grid is tuned: every co-resident
-// shape (1 to 8 CTAs per SM) runs one Dormand-Prince attempt over the
-// solver's zeroed buffers and the fastest is kept.  HEOMGB_RESIDENT=0 keeps
-// the stage kernels; HEOMGB_RESIDENT_PER_SM=<n> pins the shape.
+// shape (1 to 8 CTAs per SM, 1 to 3 elements per thread) runs one
+// Dormand-Prince attempt over the solver's zeroed buffers and the fastest is
+// kept.  HEOMGB_RESIDENT=0 keeps the stage kernels; HEOMGB_RESIDENT_PER_SM
+// and HEOMGB_RESIDENT_EPT pin the shape.
 void plan_resident(heomgb_qme_solver* qs) {
   heomgb_qme* q = qs->q;
   qs->resident = false;
@@ -1183,31 +1184,38 @@ void plan_resident(heomgb_qme_solver* qs) {
   const bool hreal = I.h_real != 0;
   int pin = 0;
   if (const char* env = std::getenv("HEOMGB_RESIDENT_PER_SM")) pin = std::atoi(env);
+  int pin_ept = 0;
+  if (const char* env = std::getenv("HEOMGB_RESIDENT_EPT")) pin_ept = std::atoi(env);
   struct Shape {
-    int grid, apc, block;
+    int grid, apc, block, ept;
     size_t smem;
   };
   std::vector<Shape> shapes;
-  int last_grid = -1;
-  for (int per_sm = 8; per_sm >= 1; --per_sm) {
-    if (pin && per_sm != pin) continue;
-    const int target = per_sm * q->n_sm;
-    const int apc = (I.nh + target - 1) / target;
-    const int grid = (I.nh + apc - 1) / apc;
-    if (grid == last_grid) continue;
-    const size_t smem = resident_smem(I.n2, apc);
-    if (smem > 200 * 1024) continue;
-    const int E = apc * I.n2;  // kResidentEpt elements per thread
-    const int block = std::max(64, ((E + kResidentEpt - 1) / kResidentEpt + 31) / 32 * 32);
-    if (block > kResidentMaxBlock) continue;
-    const int nb = resident_blocks_per_sm(hreal, block, smem);
-    if (nb < 1 || static_cast<long long>(nb) * q->n_sm < grid) continue;
-    shapes.push_back(Shape{grid, apc, block, smem});
-    last_grid = grid;
+  for (int ept = 1; ept <= kResidentMaxEpt; ++ept) {
+    if (pin_ept && ept != pin_ept) continue;
+    int last_grid = -1;
+    for (int per_sm = 8; per_sm >= 1; --per_sm) {
+      if (pin && per_sm != pin) continue;
+      const int target = per_sm * q->n_sm;
+      const int apc = (I.nh + target - 1) / target;
+      const int grid = (I.nh + apc - 1) / apc;
+      if (grid == last_grid) continue;
+      const size_t smem = resident_smem(I.n2, apc);
+      if (smem > 200 * 1024) continue;
+      const int E = apc * I.n2;  // ept elements per thread
+      const int block = std::max(64, ((E + ept - 1) / ept + 31) / 32 * 32);
+      if (block > kResidentMaxBlock) continue;
+      const int nb = resident_blocks_per_sm(hreal, ept, block, smem);
+      if (nb < 1 || static_cast<long long>(nb) * q->n_sm < grid) continue;
+      shapes.push_back(Shape{grid, apc, block, ept, smem});
+      last_grid = grid;
+    }
   }
   if (shapes.empty()) return;
   qs->res_bar = static_cast<unsigned long long*>(qs->arena.alloc(kResidentBarWords * sizeof(unsigned long long)));
-  qs->res_partials = static_cast<double*>(qs->arena.alloc(sizeof(double) * shapes.front().grid));
+  int max_grid = 0;
+  for (const Shape& sh : shapes) max_grid = std::max(max_grid, sh.grid);
+  qs->res_partials = static_cast<double*>(qs->arena.alloc(sizeof(double) * max_grid));
   size_t best = 0;
   if (shapes.size() > 1) {
     const size_t bd = sizeof(double2) * qs->N, bb = sizeof(float2) * qs->N;
@@ -1223,6 +1231,7 @@ void plan_resident(heomgb_qme_solver* qs) {
       qs->res_grid = shapes[i].grid;
       qs->res_apc = shapes[i].apc;
       qs->res_block = shapes[i].block;
+      qs->res_ept = shapes[i].ept;
       qs->res_smem = shapes[i].smem;
       float ms_i = 1e30f;
       for (int r = 0; r < 4; ++r) {  // one warm-up, best of three
@@ -1230,7 +1239,8 @@ void plan_resident(heomgb_qme_solver* qs) {
         ck(launch_ctl_init(qs->ctl, 0.0, 1e-3, 1e-3, 1e-8, 1e-8, 0, qs->stream), "ctl init");
         ck(cudaMemsetAsync(qs->res_bar, 0, kResidentBarWords * sizeof(unsigned long long), qs->stream), "memset");
         ck(cudaEventRecord(e0, qs->stream), "event");
-        ck(launch_dp_resident(resident_args(qs), hreal, qs->res_grid, qs->res_block, qs->res_smem, qs->stream),
+        ck(launch_dp_resident(resident_args(qs), hreal, qs->res_ept, qs->res_grid, qs->res_block, qs->res_smem,
+                              qs->stream),
            "resident tune");
         ck(cudaEventRecord(e1, qs->stream), "event");
         ck(cudaEventSynchronize(e1), "event sync");
@@ -1252,6 +1262,7 @@ void plan_resident(heomgb_qme_solver* qs) {
   qs->res_grid = shapes[best].grid;
   qs->res_apc = shapes[best].apc;
   qs->res_block = shapes[best].block;
+  qs->res_ept = shapes[best].ept;
   qs->res_smem = shapes[best].smem;
   qs->resident = true;
 }
@@ -1447,8 +1458,8 @@ int solve_resident(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwa
   ck(launch_ctl_init(qs->ctl, t0, dt, t1, atol, rtol, cur, qs->stream), "ctl init");
   ck(cudaMemsetAsync(qs->res_bar, 0, kResidentBarWords * sizeof(unsigned long long), qs->stream), "barrier reset");
   busy_begin(qs);
-  ck(launch_dp_resident(resident_args(qs), qs->q->dinst.h_real != 0, qs->res_grid, qs->res_block, qs->res_smem,
-                        qs->stream),
+  ck(launch_dp_resident(resident_args(qs), qs->q->dinst.h_real != 0, qs->res_ept, qs->res_grid, qs->res_block,
+                        qs->res_smem, qs->stream),
      "resident interval");
   busy_end(qs);
   qs->replayed_kernels += 1;

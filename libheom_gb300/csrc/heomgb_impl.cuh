@@ -167,7 +167,7 @@ struct DiagSet {
 // CTAs of at most kResidentMaxBlock threads, CTA b owning ADOs
 // [b*ados_per_cta, ...).
 constexpr int kResidentMaxBlock = 320;
-constexpr int kResidentEpt = 2;            // elements per thread (fixed for the interval)
+constexpr int kResidentMaxEpt = 3;         // elements per thread (1 to 3, fixed for the interval)
 constexpr int kResidentTerms = 8;          // bath-term slots per element: 4 (+1 terms) + 4 (-1 terms)
 constexpr int kResidentBarWords = 32;       // grid-barrier counter and flag (64-bit words)
 struct ResidentArgs {
@@ -184,8 +184,8 @@ struct ResidentArgs {
   int pad_;
 };
 size_t resident_smem(int n2, int ados_per_cta);
-int resident_blocks_per_sm(bool hreal, int block, size_t smem);
-cudaError_t launch_dp_resident(const ResidentArgs& args, bool hreal, int grid, int block, size_t smem,
+int resident_blocks_per_sm(bool hreal, int ept, int block, size_t smem);
+cudaError_t launch_dp_resident(const ResidentArgs& args, bool hreal, int ept, int grid, int block, size_t smem,
                                cudaStream_t s);
 
 // Launchers (kernels.cu).  `mixed` selects FP32 bulk arithmetic; `in_double`

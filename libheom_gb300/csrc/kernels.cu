@@ -1098,7 +1098,7 @@ __device__ bool grid_wait(unsigned long long* bar, unsigned long long& gen) {
   return s_ok != 0;
 }
 
-template <bool HREAL>
+template <bool HREAL, int EPT>
 __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const ResidentArgs R) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ DpCtl c;
@@ -1134,13 +1134,13 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
     }
   }
   // the thread's elements, fixed for the interval: le = threadIdx.x + r * blockDim.x
-  // (r < kResidentEpt; the host sizes the CTA so that they cover E), and
+  // (r < EPT; the host sizes the CTA so that they cover E), and
   // their bath-term table (the host admits models with at most 4 + 4 terms
   // per element)
-  int el_lt[kResidentEpt], el_e[kResidentEpt], el_a[kResidentEpt], el_b[kResidentEpt];
-  float2 el_g[kResidentEpt];
+  int el_lt[EPT], el_e[EPT], el_a[EPT], el_b[EPT];
+  float2 el_g[EPT];
 #pragma unroll
-  for (int r = 0; r < kResidentEpt; ++r) {
+  for (int r = 0; r < EPT; ++r) {
     const int le = threadIdx.x + r * blockDim.x;
     const int lec = le < E ? le : 0;
     const int lt = lec / n2, e = lec - lt * n2, a = e / n;
@@ -1222,9 +1222,9 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
       float2* Xn = yt + static_cast<size_t>((s + 1) & 1) * E;
       // own part first (commutator and damping): it reads only this CTA's
       // copy of the stage input, published by the last grid_arrive's sync
-      float2 Dp[kResidentEpt];
+      float2 Dp[EPT];
 #pragma unroll
-      for (int r = 0; r < kResidentEpt; ++r) {
+      for (int r = 0; r < EPT; ++r) {
         const int le = threadIdx.x + r * blockDim.x;
         Dp[r] = make_float2(0.f, 0.f);
         if (le >= E) continue;
@@ -1263,9 +1263,9 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
         if (!ok) break;
       }
       // the neighbour gathers of all the thread's elements (independent loads)
-      float2 vv[kResidentEpt][kResidentTerms];
+      float2 vv[EPT][kResidentTerms];
 #pragma unroll
-      for (int r = 0; r < kResidentEpt; ++r) {
+      for (int r = 0; r < EPT; ++r) {
         const int le = threadIdx.x + r * blockDim.x;
 #pragma unroll
         for (int j = 0; j < kResidentTerms; ++j) {
@@ -1274,7 +1274,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
         }
       }
 #pragma unroll
-      for (int r = 0; r < kResidentEpt; ++r) {
+      for (int r = 0; r < EPT; ++r) {
         const int le = threadIdx.x + r * blockDim.x;
         if (le >= E) continue;
         float2 D = Dp[r];
@@ -1365,8 +1365,22 @@ size_t resident_smem(int n2, int ados_per_cta) {
               kResidentTerms * (sizeof(int) + sizeof(float2)));
 }
 
-int resident_blocks_per_sm(bool hreal, int block, size_t smem) {
-  auto kern = hreal ? k_dp_resident<true> : k_dp_resident<false>;
+// the kernel instance for H real or complex and EPT elements per thread
+static const void* resident_kernel(bool hreal, int ept) {
+  switch (ept * 2 + (hreal ? 1 : 0)) {
+    case 2: return reinterpret_cast<const void*>(k_dp_resident<false, 1>);
+    case 3: return reinterpret_cast<const void*>(k_dp_resident<true, 1>);
+    case 4: return reinterpret_cast<const void*>(k_dp_resident<false, 2>);
+    case 5: return reinterpret_cast<const void*>(k_dp_resident<true, 2>);
+    case 6: return reinterpret_cast<const void*>(k_dp_resident<false, 3>);
+    case 7: return reinterpret_cast<const void*>(k_dp_resident<true, 3>);
+    default: return nullptr;
+  }
+}
+
+int resident_blocks_per_sm(bool hreal, int ept, int block, size_t smem) {
+  const void* kern = resident_kernel(hreal, ept);
+  if (!kern) return 0;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
     return 0;
   int nb = 0;
@@ -1374,14 +1388,15 @@ int resident_blocks_per_sm(bool hreal, int block, size_t smem) {
   return nb;
 }
 
-cudaError_t launch_dp_resident(const ResidentArgs& args, bool hreal, int grid, int block, size_t smem,
+cudaError_t launch_dp_resident(const ResidentArgs& args, bool hreal, int ept, int grid, int block, size_t smem,
                                cudaStream_t s) {
-  auto kern = hreal ? k_dp_resident<true> : k_dp_resident<false>;
+  const void* kern = resident_kernel(hreal, ept);
+  if (!kern) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return e;
   ResidentArgs a = args;
   void* params[] = {&a};
-  e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(grid), dim3(block), params, smem, s);
+  e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(block), params, smem, s);
   ++g_launches;
   return e;
 }

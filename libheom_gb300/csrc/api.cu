@@ -1166,7 +1166,7 @@ void autotune(heomgb_qme_solver* qs) {
 // diagonal-coupling path without a terminator, when a co-resident grid holds
 // its state in shared memory.  Fewer ADOs per CTA shorten each stage, more
 // CTAs lengthen each grid barrier, so the grid is tuned: every co-resident
-// shape (1 to 8 CTAs per SM, 1 to 3 elements per thread) runs one
+// shape (1 to 8 CTAs per SM, 1 or 2 elements per thread) runs one
 // Dormand-Prince attempt over the solver's zeroed buffers and the fastest is
 // kept.  HEOMGB_RESIDENT=0 keeps the stage kernels; HEOMGB_RESIDENT_PER_SM
 // and HEOMGB_RESIDENT_EPT pin the shape.

@@ -167,7 +167,7 @@ struct DiagSet {
 // CTAs of at most kResidentMaxBlock threads, CTA b owning ADOs
 // [b*ados_per_cta, ...).
 constexpr int kResidentMaxBlock = 320;
-constexpr int kResidentMaxEpt = 3;         // elements per thread (1 to 3, fixed for the interval)
+constexpr int kResidentMaxEpt = 2;         // elements per thread (1 or 2, fixed for the interval)
 constexpr int kResidentTerms = 8;          // bath-term slots per element: 4 (+1 terms) + 4 (-1 terms)
 constexpr int kResidentBarWords = 32;       // grid-barrier counter and flag (64-bit words)
 struct ResidentArgs {

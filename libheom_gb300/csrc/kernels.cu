@@ -1217,7 +1217,10 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
     double local = 0.0;
     for (int s = 0; s < 7 && ok; ++s) {
       // stage input: own ADOs from shared memory, neighbours from global memory
-      const float2* __restrict__ Xg = s == 0 ? R.Yb[cur] : (s < 6 ? R.Ytmp[(s - 1) & 1] : R.Yb[1 - cur]);
+      // (not __restrict__: other CTAs write it until grid_wait returns, and a
+      // restrict-qualified read-only pointer would let the compiler hoist the
+      // gathers above the wait)
+      const float2* Xg = s == 0 ? R.Yb[cur] : (s < 6 ? R.Ytmp[(s - 1) & 1] : R.Yb[1 - cur]);
       const float2* Xs = yt + static_cast<size_t>(s & 1) * E;
       float2* Xn = yt + static_cast<size_t>((s + 1) & 1) * E;
       // own part first (commutator and damping): it reads only this CTA's
@@ -1372,8 +1375,6 @@ static const void* resident_kernel(bool hreal, int ept) {
     case 3: return reinterpret_cast<const void*>(k_dp_resident<true, 1>);
     case 4: return reinterpret_cast<const void*>(k_dp_resident<false, 2>);
     case 5: return reinterpret_cast<const void*>(k_dp_resident<true, 2>);
-    case 6: return reinterpret_cast<const void*>(k_dp_resident<false, 3>);
-    case 7: return reinterpret_cast<const void*>(k_dp_resident<true, 3>);
     default: return nullptr;
   }
 }

@@ -69,6 +69,23 @@ def test_resident_spin_boson(monkeypatch):
     compare(p, [0.0, 2.0, 4.0], monkeypatch, kw=dict(dt=0.01, atol=1e-9, rtol=1e-9))
 
 
+@pytest.mark.parametrize("ept", ["1", "2"])
+def test_resident_first_attempt_bit_identical(ept, monkeypatch):
+    """One accepted attempt: the per-element arithmetic is the stage kernels',
+    so the state agrees bit for bit; the step size may differ in the last bit
+    (the error norm's sum runs in another order)."""
+    p = configs.spin_boson(depth=8)
+    kw = dict(dt=0.01, atol=1e-9, rtol=1e-9)
+    monkeypatch.setenv("HEOMGB_RESIDENT_EPT", ept)
+    res, st_r, tune = run(p, [0.0, 0.01], monkeypatch, True, kw=kw)
+    monkeypatch.delenv("HEOMGB_RESIDENT_EPT")
+    stg, st_s, _ = run(p, [0.0, 0.01], monkeypatch, False, kw=kw)
+    assert tune["resident"]
+    assert st_r["attempts"] == st_s["attempts"] == 1
+    assert np.array_equal(res, stg)
+    assert abs(st_r["dt_save"] - st_s["dt_save"]) <= 1e-12 * abs(st_s["dt_save"])
+
+
 def test_resident_only_where_it_applies(monkeypatch):
     p = configs.exciton_7site(depth=2)
     _, _, tune = run(p, [0.0, 1.0], monkeypatch, True, precision="fp64")

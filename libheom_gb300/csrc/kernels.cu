@@ -1049,17 +1049,18 @@ __global__ void __launch_bounds__(256, MINB) k_rhs_diag_tc(const DiagSet ds, con
 // The whole output interval of the mixed form's Dormand-Prince solver in one
 // cooperative launch, for models small enough that the CTAs together hold
 // the state in shared memory.  A CTA owns a contiguous range of ADOs and
-// keeps their FP64 state and candidate state, the six FP32 stage vectors and
-// two FP32 stage-input copies in shared memory; of each stage only the stage
-// input goes through global memory (written for the neighbour gathers of the
-// other CTAs and read back with L1-bypassing loads after a grid barrier).
-// The arithmetic per element is that of k_rhs_diag with the mixed form's
-// Dormand-Prince epilogues (epi_pre/epi_post: EPI_DP, EPI_DP7), in the same
-// operation order.  The error norm is summed per CTA and published; after
-// one more barrier every CTA adds the partial sums in index order and runs
-// the step controller on its own copy of the controller state, so all CTAs
-// take the same decisions without a further exchange.  Grid barriers are
-// bounded spins: one that runs out sets the failure flag and the CTAs leave.
+// keeps their FP64 state and candidate state with FP32 copies, the six FP32
+// stage vectors, two FP32 stage-input copies and the ADOs' bath-term table in
+// shared memory; of each stage only the stage input goes through global
+// memory (written for the neighbour gathers of the other CTAs and read back
+// with L1-bypassing loads after a grid barrier).  The arithmetic per element
+// is that of k_rhs_diag with the mixed form's Dormand-Prince epilogues
+// (epi_pre/epi_post: EPI_DP, EPI_DP7), in the same operation order.  The
+// error norm is summed per CTA and published; after one more barrier every
+// CTA adds the partial sums in index order and runs the step controller on
+// its own copy of the controller state, so all CTAs take the same decisions
+// without a further exchange.  Grid barriers are bounded spins: one that runs
+// out sets the failure flag and the CTAs leave.
 // Grid barrier of a cooperative launch (every CTA resident), in the
 // arrive/wait pattern of CUTLASS's GenericBarrier, split in two so that a
 // CTA can work on its own data between them.  grid_arrive: the CTA syncs,
@@ -1115,7 +1116,10 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
   // bath terms of every element, fixed for the interval (slot-major): the
   // neighbour element's offset in the state (-1: none) and its coefficient;
   // slots 0-3 hold the +1 terms, 4-7 the -1 terms, in k_rhs_diag's order
-  int* Toff = reinterpret_cast<int*>(yt + 2 * static_cast<size_t>(E));
+  // FP32 copies of both states (Yf[i] = float(S[i]) element-wise, kept with
+  // the states so that no stage converts from FP64)
+  float2* Yf = yt + 2 * static_cast<size_t>(E);
+  int* Toff = reinterpret_cast<int*>(Yf + 2 * static_cast<size_t>(E));
   float2* Tcf = reinterpret_cast<float2*>(Toff + kResidentTerms * static_cast<size_t>(E));
   const float2* __restrict__ ngd = I.ngd_f;
   const float2* __restrict__ cpl = I.c_plus_f;
@@ -1130,7 +1134,9 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
     for (int le = threadIdx.x; le < E; le += blockDim.x) {
       const double2 v = R.S[cur][gb + le];
       Sv[static_cast<size_t>(cur) * E + le] = v;
-      yt[le] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+      const float2 f = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+      Yf[static_cast<size_t>(cur) * E + le] = f;
+      yt[le] = f;
     }
   }
   // the thread's elements, fixed for the interval: le = threadIdx.x + r * blockDim.x
@@ -1214,6 +1220,8 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
     const int cur = c.cur;
     const double2* Sc = Sv + static_cast<size_t>(cur) * E;
     double2* Sn = Sv + static_cast<size_t>(1 - cur) * E;
+    const float2* Yc = Yf + static_cast<size_t>(cur) * E;
+    float2* Yn = Yf + static_cast<size_t>(1 - cur) * E;
     double local = 0.0;
     for (int s = 0; s < 7 && ok; ++s) {
       // stage input: own ADOs from shared memory, neighbours from global memory
@@ -1288,8 +1296,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
         const size_t g = gb + le;
         if (s < 5) {  // k_s; next stage input Yb + sum_j A[s+1][j] k_j in FP32
           Kv[static_cast<size_t>(s) * E + le] = k;
-          const double2 sc = Sc[le];
-          float2 y = make_float2(static_cast<float>(sc.x), static_cast<float>(sc.y));
+          float2 y = Yc[le];
           for (int j = 0; j < s; ++j) {
             const float cj = static_cast<float>(c_dpA[s + 1][j]);
             const float2 kj = Kv[static_cast<size_t>(j) * E + le];
@@ -1313,6 +1320,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
           y.y = fma(c_dpA[6][5], static_cast<double>(k.y), y.y);
           Sn[le] = y;
           const float2 yb = make_float2(static_cast<float>(y.x), static_cast<float>(y.y));
+          Yn[le] = yb;
           Xn[le] = yb;
           R.Yb[1 - cur][g] = yb;
         } else {  // stage 7: e = sum_j E_j k_j in FP32, scaled squared error
@@ -1326,8 +1334,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
           const float c6 = static_cast<float>(c_dpE[6]);
           const float ex = fmaf(c6, k.x, ee.x), ey = fmaf(c6, k.y, ee.y);
           const float2 x1 = Xs[le];
-          const double2 sc = Sc[le];
-          const float2 x2 = make_float2(static_cast<float>(sc.x), static_cast<float>(sc.y));
+          const float2 x2 = Yc[le];
           const double m = static_cast<double>(fmaxf(x1.x * x1.x + x1.y * x1.y, x2.x * x2.x + x2.y * x2.y));
           const float sm = static_cast<float>(c.atol) + static_cast<float>(c.rtol) * sqrtf(static_cast<float>(m));
           local += static_cast<double>((ex * ex + ey * ey) / (sm * sm));
@@ -1347,11 +1354,8 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
     if (threadIdx.x == 0) dp_control(&c, v, R.n_total);
     __syncthreads();
     // the next attempt's stage-1 input (own part): the FP32 copy of the current state
-    const double2* Snow = Sv + static_cast<size_t>(c.cur) * E;
-    for (int le = threadIdx.x; le < E; le += blockDim.x) {
-      const double2 x = Snow[le];
-      yt[le] = make_float2(static_cast<float>(x.x), static_cast<float>(x.y));
-    }
+    const float2* Ynow = Yf + static_cast<size_t>(c.cur) * E;
+    for (int le = threadIdx.x; le < E; le += blockDim.x) yt[le] = Ynow[le];
     __syncthreads();
   }
   if (ok) {
@@ -1364,7 +1368,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
 size_t resident_smem(int n2, int ados_per_cta) {
   const size_t E = static_cast<size_t>(ados_per_cta) * n2;
   return ((sizeof(float2) * n2 + 15) & ~static_cast<size_t>(15)) +
-         E * (2 * sizeof(double2) + 6 * sizeof(float2) + 2 * sizeof(float2) +
+         E * (2 * sizeof(double2) + 6 * sizeof(float2) + 4 * sizeof(float2) +
               kResidentTerms * (sizeof(int) + sizeof(float2)));
 }
 

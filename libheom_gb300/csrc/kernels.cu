@@ -104,6 +104,38 @@ __constant__ double c_dpA[7][6] = {
 __constant__ double c_dpE[7] = {-71.0 / 57600, 0, 71.0 / 16695, -71.0 / 1920, 17253.0 / 339200, -22.0 / 525,
                                 1.0 / 40};
 
+// The mixed form's candidate state rho + sum_j B_j k_j (B = the last row of
+// the tableau, k_j FP32) takes the sum as an unevaluated float pair hi + lo:
+// each B_j is split into two floats (B_j = Bh_j + Bl_j to about 2^-48), each
+// product's rounding error is recovered with an FMA and the additions use
+// Knuth's TwoSum, so the pair carries the sum to about 2^-48 of sum |B_j k_j|;
+// the FP64 state then takes hi and lo in two FP64 additions.  This replaces
+// twelve FP64 FMAs and conversions per element, slow on this part, with FP32
+// work of the same accuracy class.
+#define HEOMGB_DP_B(j) (j == 0 ? 35.0 / 384 : j == 1 ? 0.0 : j == 2 ? 500.0 / 1113 : j == 3 ? 125.0 / 192 \
+                        : j == 4 ? -2187.0 / 6784 : 11.0 / 84)
+#define HEOMGB_SPLIT_LO(v) static_cast<float>((v) - static_cast<double>(static_cast<float>(v)))
+__constant__ float c_dpBh[6] = {static_cast<float>(HEOMGB_DP_B(0)), static_cast<float>(HEOMGB_DP_B(1)),
+                                static_cast<float>(HEOMGB_DP_B(2)), static_cast<float>(HEOMGB_DP_B(3)),
+                                static_cast<float>(HEOMGB_DP_B(4)), static_cast<float>(HEOMGB_DP_B(5))};
+__constant__ float c_dpBl[6] = {HEOMGB_SPLIT_LO(HEOMGB_DP_B(0)), HEOMGB_SPLIT_LO(HEOMGB_DP_B(1)),
+                                HEOMGB_SPLIT_LO(HEOMGB_DP_B(2)), HEOMGB_SPLIT_LO(HEOMGB_DP_B(3)),
+                                HEOMGB_SPLIT_LO(HEOMGB_DP_B(4)), HEOMGB_SPLIT_LO(HEOMGB_DP_B(5))};
+#undef HEOMGB_SPLIT_LO
+#undef HEOMGB_DP_B
+
+// (hi, lo) += (bh + bl) * k; the rounded operations are explicit so that no
+// contraction merges the product into the TwoSum
+__device__ __forceinline__ void ff_add_prod(float& hi, float& lo, float bh, float bl, float k) {
+  const float p = __fmul_rn(bh, k);
+  const float pe = fmaf(bh, k, -p);
+  const float s = __fadd_rn(hi, p);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  hi = s;
+  lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(err, pe), __fmul_rn(bl, k)));
+}
+
 // ------------------------------------------------------------------ step control
 // rkdp.h:150-177 and adaptive_step_size_solver.h:45-55, one thread.
 __device__ void dp_control(DpCtl* c, double sumsq, long long n) {
@@ -148,15 +180,17 @@ __device__ void dp_control(DpCtl* c, double sumsq, long long n) {
 // FP64 form (TC = double): the reference's operation order (rk4.h:40-65,
 // lsrk4.h:32-47, rkdp.h:111-153).  Mixed form (TC = float): stage inputs of
 // the next right-hand side are formed in FP32 from the bulk copy of the
-// state; the state, the RK4 accumulator, the LSRK4 buffer and the
-// Dormand-Prince candidate state rho + sum_j B_j k_j are accumulated in FP64
-// (the k_j themselves are FP32).  The error vector e = sum_j E_j k_j only
+// state; the state, the RK4 accumulator and the LSRK4 buffer are accumulated
+// in FP64, and the Dormand-Prince candidate state rho + sum_j B_j k_j adds
+// the sum of the FP32 k_j, carried as a float pair to about 2^-48
+// (ff_add_prod), to the FP64 state.  The error vector e = sum_j E_j k_j only
 // steers the step size: it is combined from the FP32 k_j in FP32, while the
 // error norm's sum over elements and the step controller are FP64.
 struct EpiPre {
   double2 a;   // FP64 partial result (accumulator, base state, partial sum)
   double2 b;   // FP64 base state (RK4 in FP64 form, LSRK4)
-  float2 f;    // FP32 partial result (mixed-form stage inputs)
+  float2 f;    // FP32 partial result (mixed-form stage inputs; high part of the candidate's sum)
+  float2 g;    // low part of the mixed-form Dormand-Prince candidate's sum
   double m;    // squared error scale (EPI_DP7)
 };
 
@@ -167,6 +201,7 @@ __device__ __forceinline__ EpiPre epi_pre(const Stage& st, size_t g, int cur) {
   p.a = make_double2(0.0, 0.0);
   p.b = make_double2(0.0, 0.0);
   p.f = make_float2(0.f, 0.f);
+  p.g = make_float2(0.f, 0.f);
   p.m = 0.0;
   switch (st.kind) {
     case EPI_DIFF:
@@ -200,15 +235,16 @@ __device__ __forceinline__ EpiPre epi_pre(const Stage& st, size_t g, int cur) {
             y.y = fmaf(c, kj.y, y.y);
           }
           p.f = y;
-        } else {  // candidate state rho + sum_j B_j k_j, accumulated in FP64
-          double2 y = __ldcs(st.S[cur] + g);
+        } else {  // candidate state rho + sum_j B_j k_j: the sum as a float pair (c_dpBh)
+          p.a = __ldcs(st.S[cur] + g);
+          float2 hi = make_float2(0.f, 0.f), lo = make_float2(0.f, 0.f);
           for (int j = 0; j < 5; ++j) {
-            const double c = c_dpA[6][j];
             const float2 kj = __ldcs(static_cast<const float2*>(st.K[j]) + g);
-            y.x = fma(c, static_cast<double>(kj.x), y.x);
-            y.y = fma(c, static_cast<double>(kj.y), y.y);
+            ff_add_prod(hi.x, lo.x, c_dpBh[j], c_dpBl[j], kj.x);
+            ff_add_prod(hi.y, lo.y, c_dpBh[j], c_dpBl[j], kj.y);
           }
-          p.a = y;
+          p.f = hi;
+          p.g = lo;
         }
       } else {
         double2 y = __ldcs(st.S[cur] + g);
@@ -325,9 +361,11 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
           const float c = static_cast<float>(c_dpA[s_ + 1][s_]);
           static_cast<float2*>(st.Ynext)[g] = make_float2(fmaf(c, k.x, p.f.x), fmaf(c, k.y, p.f.y));
         } else {
-          double2 y = p.a;
-          y.x = fma(c_dpA[6][5], static_cast<double>(k.x), y.x);
-          y.y = fma(c_dpA[6][5], static_cast<double>(k.y), y.y);
+          float2 hi = p.f, lo = p.g;
+          ff_add_prod(hi.x, lo.x, c_dpBh[5], c_dpBl[5], k.x);
+          ff_add_prod(hi.y, lo.y, c_dpBh[5], c_dpBl[5], k.y);
+          const double2 y = make_double2((p.a.x + static_cast<double>(hi.x)) + static_cast<double>(lo.x),
+                                         (p.a.y + static_cast<double>(hi.y)) + static_cast<double>(lo.y));
           __stcs(st.S[1 - cur] + g, y);
           static_cast<float2*>(st.Yb[1 - cur])[g] = make_float2(static_cast<float>(y.x), static_cast<float>(y.y));
         }
@@ -1309,15 +1347,17 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
           R.Ytmp[s & 1][g] = y;
         } else if (s == 5) {  // candidate state rho + sum_j B_j k_j in FP64
           Kv[5 * static_cast<size_t>(E) + le] = k;
-          double2 y = Sc[le];
+          float2 hi = make_float2(0.f, 0.f), lo = make_float2(0.f, 0.f);
           for (int j = 0; j < 5; ++j) {
-            const double cj = c_dpA[6][j];
             const float2 kj = Kv[static_cast<size_t>(j) * E + le];
-            y.x = fma(cj, static_cast<double>(kj.x), y.x);
-            y.y = fma(cj, static_cast<double>(kj.y), y.y);
+            ff_add_prod(hi.x, lo.x, c_dpBh[j], c_dpBl[j], kj.x);
+            ff_add_prod(hi.y, lo.y, c_dpBh[j], c_dpBl[j], kj.y);
           }
-          y.x = fma(c_dpA[6][5], static_cast<double>(k.x), y.x);
-          y.y = fma(c_dpA[6][5], static_cast<double>(k.y), y.y);
+          ff_add_prod(hi.x, lo.x, c_dpBh[5], c_dpBl[5], k.x);
+          ff_add_prod(hi.y, lo.y, c_dpBh[5], c_dpBl[5], k.y);
+          const double2 sc = Sc[le];
+          const double2 y = make_double2((sc.x + static_cast<double>(hi.x)) + static_cast<double>(lo.x),
+                                         (sc.y + static_cast<double>(hi.y)) + static_cast<double>(lo.y));
           Sn[le] = y;
           const float2 yb = make_float2(static_cast<float>(y.x), static_cast<float>(y.y));
           Yn[le] = yb;
@@ -1335,8 +1375,8 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
           const float ex = fmaf(c6, k.x, ee.x), ey = fmaf(c6, k.y, ee.y);
           const float2 x1 = Xs[le];
           const float2 x2 = Yc[le];
-          const double m = static_cast<double>(fmaxf(x1.x * x1.x + x1.y * x1.y, x2.x * x2.x + x2.y * x2.y));
-          const float sm = static_cast<float>(c.atol) + static_cast<float>(c.rtol) * sqrtf(static_cast<float>(m));
+          const float m = fmaxf(x1.x * x1.x + x1.y * x1.y, x2.x * x2.x + x2.y * x2.y);
+          const float sm = static_cast<float>(c.atol) + static_cast<float>(c.rtol) * sqrtf(m);
           local += static_cast<double>((ex * ex + ey * ey) / (sm * sm));
         }
       }

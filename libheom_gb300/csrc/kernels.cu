@@ -180,7 +180,8 @@ __device__ void dp_control(DpCtl* c, double sumsq, long long n) {
 // FP64 form (TC = double): the reference's operation order (rk4.h:40-65,
 // lsrk4.h:32-47, rkdp.h:111-153).  Mixed form (TC = float): stage inputs of
 // the next right-hand side are formed in FP32 from the bulk copy of the
-// state; the state, the RK4 accumulator and the LSRK4 buffer are accumulated
+// state; the state and the RK4 accumulator are accumulated in FP64, the LSRK4
+// buffer (a +-1 combination of FP32 k's) is FP32 and added to the FP64 state
 // in FP64, and the Dormand-Prince candidate state rho + sum_j B_j k_j adds
 // the sum of the FP32 k_j, carried as a float pair to about 2^-48
 // (ff_add_prod), to the FP64 state.  The error vector e = sum_j E_j k_j only
@@ -220,7 +221,11 @@ __device__ __forceinline__ EpiPre epi_pre(const Stage& st, size_t g, int cur) {
       p.a = __ldcs(st.acc + g);
       break;
     case EPI_LS:
-      if (!st.ls_first) p.a = __ldcs(st.acc + g);
+      if constexpr (MIX) {  // FP32 buffer (the first half of the buffer allocation)
+        if (!st.ls_first) p.f = __ldcs(reinterpret_cast<const float2*>(st.acc) + g);
+      } else {
+        if (!st.ls_first) p.a = __ldcs(st.acc + g);
+      }
       p.b = __ldcs(st.S[st.ls_in] + g);
       break;
     case EPI_DP: {
@@ -343,12 +348,23 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
       return 0.0;
     }
     case EPI_LS: {  // buff = -buff + k (beta=-1) or k (beta=0); rho += B*buff
-      const double2 k = make_double2(-dt * D.x, -dt * D.y);
-      const double2 b = st.ls_first ? k : make_double2(-p.a.x + k.x, -p.a.y + k.y);
-      __stcs(st.acc + g, b);
-      const double2 v = make_double2(p.b.x + st.coef * b.x, p.b.y + st.coef * b.y);
-      __stcs(st.S[1 - st.ls_in] + g, v);
-      if (st.bulk_separate) st_bulk<TC>(st.Yb[1 - st.ls_in], g, v);
+      if constexpr (MIX) {  // the buffer combines FP32 k's: kept in FP32; the state update is FP64
+        const float fdt = static_cast<float>(dt);
+        const float2 k = make_float2(-fdt * Dc.x, -fdt * Dc.y);
+        const float2 b = st.ls_first ? k : make_float2(-p.f.x + k.x, -p.f.y + k.y);
+        __stcs(reinterpret_cast<float2*>(st.acc) + g, b);
+        const double2 v = make_double2(fma(st.coef, static_cast<double>(b.x), p.b.x),
+                                       fma(st.coef, static_cast<double>(b.y), p.b.y));
+        __stcs(st.S[1 - st.ls_in] + g, v);
+        if (st.bulk_separate) st_bulk<TC>(st.Yb[1 - st.ls_in], g, v);
+      } else {
+        const double2 k = make_double2(-dt * D.x, -dt * D.y);
+        const double2 b = st.ls_first ? k : make_double2(-p.a.x + k.x, -p.a.y + k.y);
+        __stcs(st.acc + g, b);
+        const double2 v = make_double2(p.b.x + st.coef * b.x, p.b.y + st.coef * b.y);
+        __stcs(st.S[1 - st.ls_in] + g, v);
+        if (st.bulk_separate) st_bulk<TC>(st.Yb[1 - st.ls_in], g, v);
+      }
       return 0.0;
     }
     case EPI_DP: {  // store k_s; next stage input rho + sum_j A[s+1][j] k_j

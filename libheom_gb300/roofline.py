@@ -6,9 +6,9 @@ hits; buffers that alias in FP64 mode count once).  State vectors are FP64
 complex (16 B); bulk vectors are 8 B in mixed precision and 16 B in FP64.
 
   rk4   s1: Y1 S | Y2 acc          s2,s3: Y S acc | Y' acc      s4: Y4 acc | S (Y1)
-  lsrk4 s:  Y S (buff) | buff S' (Y')
+  lsrk4 s:  Y S (buff) | buff S' (Y')        (buff is a bulk vector: FP32 in mixed)
   rkdp  s1..s6: Y S K_1..K_{s-1} | K_s Y'  (s6 writes S' and Y' instead of Y')
-        s7: Y7 K_1..K_6 S' S | -
+        s7: Y7 K_1..K_6 S' S | -           (mixed: the FP32 copies of S' and S)
 Flops: real floating-point operations per element of the right-hand side as
 evaluated by the diagonal-coupling kernel: the commutator (4 real FMA per term
 for real H, 8 for complex H), the damping term, and 8 (+2 for the n_k scale)
@@ -42,8 +42,9 @@ def _units(solver: str, mixed: bool):
         for s in range(4):
             i, o = s & 1, 1 - (s & 1)
             Yi = vec("B", f"Yb{i}") if sep else vec("S", f"S{i}")
-            reads = [Yi, vec("S", f"S{i}")] + ([vec("S", "buff")] if s else [])
-            writes = [vec("S", "buff"), vec("S", f"S{o}")] + ([vec("B", f"Yb{o}")] if sep else [])
+            buff = vec("B" if sep else "S", "buff")  # FP32 in mixed precision
+            reads = [Yi, vec("S", f"S{i}")] + ([buff] if s else [])
+            writes = [buff, vec("S", f"S{o}")] + ([vec("B", f"Yb{o}")] if sep else [])
             stages.append((reads, writes))
     elif solver == "rkdp":
         stages = []
@@ -55,7 +56,9 @@ def _units(solver: str, mixed: bool):
             writes += [vec("B", f"Y{s + 1}")] if s < 5 else ([vec("S", "So")] + ([vec("B", "Ybo")] if sep else []))
             stages.append((reads, writes))
         Y7 = vec("B", "Ybo") if sep else vec("S", "So")
-        stages.append(([Y7] + [vec("B", f"K{j}") for j in range(6)] + [vec("S", "So"), vec("S", "Sc")], []))
+        # the error scale reads both states: their FP32 copies in mixed precision
+        scale = [vec("B", "Ybo"), vec("B", "Ybc")] if sep else [vec("S", "So"), vec("S", "Sc")]
+        stages.append(([Y7] + [vec("B", f"K{j}") for j in range(6)] + scale, []))
     else:
         raise ValueError(solver)
     out = []

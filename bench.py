@@ -35,7 +35,7 @@ sys.path.insert(0, ROOT)
 
 WORKLOADS = {
     "exciton7": dict(maker="exciton_7site", solver="rkdp", t_final=1000.0, kw=dict(dt=0.1, atol=1e-8, rtol=1e-8),
-                     cpu_sample_t=1000.0),
+                     cpu_sample_t=1000.0, default_steps=20),
     "spin_boson": dict(maker="spin_boson", solver="rk4", t_final=10.0, kw=dict(dt=0.005), cpu_sample_t=10.0),
     "batched": dict(maker="batched_sweep", solver="rk4", t_final=20.0, kw=dict(dt=0.005), cpu_sample_t=1.0,
                     cpu_sample_instances=24),
@@ -51,7 +51,8 @@ L2_FLUSH_BYTES = 512 << 20
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 20 for the 7-site workload, whose step is short, else 5)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="exciton7")
@@ -60,7 +61,10 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 comparison run (profiling)")
     ap.add_argument("--t-final", type=float, default=None,
                     help="propagate to this time instead of the workload's (short profiling runs)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.steps is None:
+        args.steps = WORKLOADS[args.workload].get("default_steps", 5)
+    return args
 
 
 def dist_env():
@@ -86,7 +90,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (FileNotFoundError, OSError):
             self.proc = None

@@ -137,13 +137,18 @@ __device__ __forceinline__ void ff_add_prod(float& hi, float& lo, float bh, floa
 }
 
 // ------------------------------------------------------------------ step control
-// rkdp.h:150-177 and adaptive_step_size_solver.h:45-55, one thread.
-__device__ void dp_control(DpCtl* c, double sumsq, long long n) {
+// rkdp.h:150-177 and adaptive_step_size_solver.h:45-55, one thread.  The
+// mixed form takes the step-size factor err^-0.2 in FP32 (`fast`): it only
+// scales the next step, FP32 resolves it far below the form's own rounding,
+// and an FP64 pow is thousands of cycles on this part's FP64 pipe, on the
+// critical path between two attempts.  The FP64 form keeps the reference's
+// FP64 pow, so its step sequence follows the reference's.
+__device__ void dp_control(DpCtl* c, double sumsq, long long n, bool fast) {
   const double err = sqrt(sumsq) / sqrt(static_cast<double>(n));
   c->err = err;
   c->attempts += 1;
   c->count += 1;
-  const double fac = pow(err, -0.2);
+  const double fac = fast ? static_cast<double>(powf(static_cast<float>(err), -0.2f)) : pow(err, -0.2);
   if (err < 1.0) {
     c->t += c->dt;
     c->dt *= 0.9 * ((fac < 10.0) ? fac : 10.0);
@@ -466,7 +471,7 @@ __device__ void dp7_finish(const Stage& st, double local, long long n_total) {
   v = block_sum(v);
   if (threadIdx.x == 0) {
     st.ctl->arrive = 0;
-    dp_control(st.ctl, v, n_total);
+    dp_control(st.ctl, v, n_total, st.bulk_separate != 0);
   }
 }
 
@@ -1407,7 +1412,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
     double v = 0.0;
     for (int i = threadIdx.x; i < static_cast<int>(gridDim.x); i += blockDim.x) v += __ldcg(R.partials + i);
     v = block_sum(v);
-    if (threadIdx.x == 0) dp_control(&c, v, R.n_total);
+    if (threadIdx.x == 0) dp_control(&c, v, R.n_total, true);
     __syncthreads();
     // the next attempt's stage-1 input (own part): the FP32 copy of the current state
     const float2* Ynow = Yf + static_cast<size_t>(c.cur) * E;

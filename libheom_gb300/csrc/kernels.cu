@@ -1276,12 +1276,13 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
     }
     const double dt = c.dt;
     const float fdt = static_cast<float>(dt);
+    const float atol_f = static_cast<float>(c.atol), rtol_f = static_cast<float>(c.rtol);
     const int cur = c.cur;
     const double2* Sc = Sv + static_cast<size_t>(cur) * E;
     double2* Sn = Sv + static_cast<size_t>(1 - cur) * E;
     const float2* Yc = Yf + static_cast<size_t>(cur) * E;
     float2* Yn = Yf + static_cast<size_t>(1 - cur) * E;
-    double local = 0.0;
+    float local_f = 0.f;
     for (int s = 0; s < 7 && ok; ++s) {
       // stage input: own ADOs from shared memory, neighbours from global memory
       // (not __restrict__: other CTAs write it until grid_wait returns, and a
@@ -1397,14 +1398,14 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
           const float2 x1 = Xs[le];
           const float2 x2 = Yc[le];
           const float m = fmaxf(x1.x * x1.x + x1.y * x1.y, x2.x * x2.x + x2.y * x2.y);
-          const float sm = static_cast<float>(c.atol) + static_cast<float>(c.rtol) * sqrtf(m);
-          local += static_cast<double>((ex * ex + ey * ey) / (sm * sm));
+          const float sm = atol_f + rtol_f * sqrtf(m);
+          local_f += (ex * ex + ey * ey) / (sm * sm);  // the thread's terms in FP32, then FP64
         }
       }
       if (s < 6) grid_arrive(R.bar);
     }
     if (!ok) break;
-    const double part = block_sum(local);
+    const double part = block_sum(static_cast<double>(local_f));
     if (threadIdx.x == 0) R.partials[blockIdx.x] = part;
     grid_arrive(R.bar);
     ok = grid_wait(R.bar, gen);

@@ -1449,6 +1449,8 @@ void solve_fixed(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwarg
 
 // adaptive_step_size_solver::solve_1 + rkdp::solve_adaptive_step as one
 // resident launch (k_dp_resident).
+int solve_adaptive(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwargs* kw, int cur);
+
 int solve_resident(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwargs* kw, int cur) {
   if (qs->dt_save == -1.0) qs->dt_save = need_kw(kw, kw ? kw->has_dt : 0, kw ? kw->dt : 0, "dt");
   const double atol = need_kw(kw, kw ? kw->has_atol : 0, kw ? kw->atol : 0, "atol");
@@ -1458,9 +1460,19 @@ int solve_resident(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwa
   ck(launch_ctl_init(qs->ctl, t0, dt, t1, atol, rtol, cur, qs->stream), "ctl init");
   ck(cudaMemsetAsync(qs->res_bar, 0, kResidentBarWords * sizeof(unsigned long long), qs->stream), "barrier reset");
   busy_begin(qs);
-  ck(launch_dp_resident(resident_args(qs), qs->q->dinst.h_real != 0, qs->res_ept, qs->res_grid, qs->res_block,
-                        qs->res_smem, qs->stream),
-     "resident interval");
+  const cudaError_t le = launch_dp_resident(resident_args(qs), qs->q->dinst.h_real != 0, qs->res_ept, qs->res_grid,
+                                            qs->res_block, qs->res_smem, qs->stream);
+  if (le == cudaErrorCooperativeLaunchTooLarge) {
+    // the device cannot hold the grid now (another context holds SMs or
+    // shared memory): this and later intervals take the stage kernels
+    cudaGetLastError();
+    busy_end(qs);
+    ck(cudaStreamSynchronize(qs->stream), "solve sync");
+    busy_collect(qs);
+    qs->resident = false;
+    return solve_adaptive(qs, t0, t1, kw, cur);
+  }
+  ck(le, "resident interval");
   busy_end(qs);
   qs->replayed_kernels += 1;
   unsigned long long flag = 0;

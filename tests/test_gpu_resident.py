@@ -64,6 +64,19 @@ def test_resident_complex_hamiltonian_sqrt_normalisation(monkeypatch):
     compare(p, [0.0, 4.0, 8.0], monkeypatch)
 
 
+def test_resident_filtered_hierarchy_col_major(monkeypatch):
+    """A filtered hierarchy (missing neighbours are sentinels in the term
+    table) with column-major ADOs at the boundary."""
+    p = configs.exciton_7site(depth=4)
+
+    def keep(idx, depth):  # drop the Matsubara modes' second excitations
+        return all(idx[k] <= 1 for k in range(1, len(idx), 2))
+
+    p = dataclasses.replace(p, hrchy_filter=keep, order="col_major")
+    assert p.n_hrchy() < configs.exciton_7site(depth=4).n_hrchy()
+    compare(p, [0.0, 5.0, 10.0], monkeypatch)
+
+
 def test_resident_spin_boson(monkeypatch):
     p = configs.spin_boson(depth=8)
     compare(p, [0.0, 2.0, 4.0], monkeypatch, kw=dict(dt=0.01, atol=1e-9, rtol=1e-9))

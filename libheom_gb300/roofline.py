@@ -6,6 +6,7 @@ hits; buffers that alias in FP64 mode count once).  State vectors are FP64
 complex (16 B); bulk vectors are 8 B in mixed precision and 16 B in FP64.
 
   rk4   s1: Y1 S | Y2 acc          s2,s3: Y S acc | Y' acc      s4: Y4 acc | S (Y1)
+        (mixed: s2,s3 read the state's bulk copy Y1 instead of S)
   lsrk4 s:  Y S (buff) | buff S' (Y')        (buff is a bulk vector: FP32 in mixed)
   rkdp  s1..s6: Y S K_1..K_{s-1} | K_s Y'  (s6 writes S' and Y' instead of Y')
         s7: Y7 K_1..K_6 S' S | -           (mixed: the FP32 copies of S' and S)
@@ -31,10 +32,11 @@ def _units(solver: str, mixed: bool):
 
     if solver == "rk4":
         Y1 = vec("B", "Yb0") if sep else vec("S", "S")
+        base = Y1 if sep else vec("S", "S")  # the stage input's base: the state's bulk copy in mixed
         stages = [
             ([Y1, vec("S", "S")], [vec("B", "Y2"), vec("S", "acc")]),
-            ([vec("B", "Y2"), vec("S", "S"), vec("S", "acc")], [vec("B", "Y3"), vec("S", "acc")]),
-            ([vec("B", "Y3"), vec("S", "S"), vec("S", "acc")], [vec("B", "Y4"), vec("S", "acc")]),
+            ([vec("B", "Y2"), base, vec("S", "acc")], [vec("B", "Y3"), vec("S", "acc")]),
+            ([vec("B", "Y3"), base, vec("S", "acc")], [vec("B", "Y4"), vec("S", "acc")]),
             ([vec("B", "Y4"), vec("S", "acc")], [vec("S", "S")] + ([vec("B", "Yb0")] if sep else [])),
         ]
     elif solver == "lsrk4":

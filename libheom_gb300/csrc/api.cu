@@ -356,6 +356,7 @@ struct heomgb_qme_solver {
   // the solver stream around every replay batch), and the kernels replayed
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double busy_ms = 0.0;
+  bool busy_open = false;  // events of a replay batch recorded, not yet collected
   long long replayed_kernels = 0;
   // resident Dormand-Prince interval (k_dp_resident): one cooperative launch
   // per output interval instead of graph replays of the stage kernels
@@ -364,12 +365,18 @@ struct heomgb_qme_solver {
   size_t res_smem = 0;
   unsigned long long* res_bar = nullptr;
   double* res_partials = nullptr;
+  // batch solvers run on a stream of their own (sub-batches of one batch run
+  // concurrently), ordered after the model stream's pending work at each solve
+  cudaStream_t own_stream = nullptr;
+  cudaEvent_t user_ready = nullptr;
   ~heomgb_qme_solver() {
     if (g_small) cudaGraphExecDestroy(g_small);
     if (g_big) cudaGraphExecDestroy(g_big);
     if (ctl_host) cudaFreeHost(ctl_host);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    if (user_ready) cudaEventDestroy(user_ready);
+    if (own_stream) cudaStreamDestroy(own_stream);
   }
 };
 
@@ -1349,7 +1356,7 @@ cudaGraphExec_t capture_units(heomgb_qme_solver* qs, int units, int* nodes) {
   cudaGraph_t g = nullptr;
   ck(cudaStreamBeginCapture(qs->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
   int launched = 0;
-  const long long before = g_launches;
+  const long long before = LaunchCounter::mine();
   try {
     for (int i = 0; i < units; ++i) enqueue_unit(qs);
   } catch (...) {
@@ -1357,8 +1364,8 @@ cudaGraphExec_t capture_units(heomgb_qme_solver* qs, int units, int* nodes) {
     if (g) cudaGraphDestroy(g);
     throw;
   }
-  launched = static_cast<int>(g_launches - before);  // kernels per replay, terminator included
-  g_launches = before;  // captured launches are counted when the graph replays
+  launched = static_cast<int>(LaunchCounter::mine() - before);  // kernels per replay, terminator included
+  g_launches += -static_cast<long long>(launched);  // captured launches are counted when the graph replays
   ck(cudaStreamEndCapture(qs->stream, &g), "end capture");
   cudaGraphExec_t ex = nullptr;
   cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
@@ -1389,18 +1396,17 @@ void replay(heomgb_qme_solver* qs, bool big) {
 }
 
 // Busy-time bracket around a batch of replays; collected after a stream sync.
-bool g_busy_open = false;
 void busy_begin(heomgb_qme_solver* qs) { ck(cudaEventRecord(qs->ev0, qs->stream), "event record"); }
 void busy_end(heomgb_qme_solver* qs) {
   ck(cudaEventRecord(qs->ev1, qs->stream), "event record");
-  g_busy_open = true;
+  qs->busy_open = true;
 }
 void busy_collect(heomgb_qme_solver* qs) {
-  if (!g_busy_open) return;
+  if (!qs->busy_open) return;
   float ms = 0.f;
   ck(cudaEventElapsedTime(&ms, qs->ev0, qs->ev1), "event elapsed");
   qs->busy_ms += ms;
-  g_busy_open = false;
+  qs->busy_open = false;
 }
 
 void state_to_bulk(heomgb_qme_solver* qs, int idx) {
@@ -1541,10 +1547,14 @@ void solve_impl(heomgb_qme_solver* qs, void* rho, bool host, const double* t_lis
   if (!rho) throw arg_error("null rho");
   if (n_t < 1 || !t_list) throw arg_error("t_list must hold at least one time");
   ck(cudaSetDevice(qs->q->device), "cudaSetDevice");
+  if (qs->own_stream) {  // after the work the caller queued on the model stream (e.g. filling rho)
+    ck(cudaEventRecord(qs->user_ready, qs->q->stream()), "event record");
+    ck(cudaStreamWaitEvent(qs->stream, qs->user_ready, 0), "stream wait");
+  }
   qs->n_rhs = qs->n_attempts = qs->n_accepted = 0;
   qs->busy_ms = 0.0;
   qs->replayed_kernels = 0;
-  g_busy_open = false;
+  qs->busy_open = false;
   const size_t bytes = sizeof(double2) * qs->N;
   const cudaMemcpyKind in_kind = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
   const cudaMemcpyKind out_kind = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
@@ -1591,7 +1601,7 @@ extern "C" {
 const char* heomgb_last_error(void) { return g_err.c_str(); }
 const char* heomgb_version(void) { return "0.1.0"; }
 int heomgb_abi_version(void) { return 1; }
-long long heomgb_launch_count(void) { return g_launches; }
+long long heomgb_launch_count(void) { return g_launches.total.load(); }
 
 heomgb_status heomgb_qme_create(heomgb_form form, int max_depth, int n_inner_threads, int n_outer_threads,
                                 heomgb_qme** out) {
@@ -1898,7 +1908,10 @@ heomgb_status heomgb_batch_solver_create(heomgb_qme* const* qmes, int count, heo
     qs->q = q0;
     qs->qmes.assign(qmes, qmes + count);
     qs->kind = s->kind;
-    qs->stream = q0->stream();
+    ck(cudaStreamSynchronize(q0->stream()), "model stream sync");
+    ck(cudaStreamCreateWithFlags(&qs->own_stream, cudaStreamNonBlocking), "stream create");
+    ck(cudaEventCreateWithFlags(&qs->user_ready, cudaEventDisableTiming), "event create");
+    qs->stream = qs->own_stream;
     alloc_solver(qs.get());
     ck(cudaStreamSynchronize(qs->stream), "solver init sync");
     for (heomgb_qme* m : qs->qmes) m->live_solvers += 1;

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <atomic>
 
 #include <cstddef>
 #include <cstdint>
@@ -251,6 +252,24 @@ cudaError_t term_enqueue(heomgb_mlp* M, const TermBuffers& tb, const TermModel& 
                          bool y_float, cudaStream_t s);
 void mlp_dims(const heomgb_mlp* M, int* din, int* h, int* dout);
 
-extern long long g_launches;  // kernels launched (incremented by the launchers / graph replays)
+// Kernels launched (incremented by the launchers and graph replays), safe for
+// solvers driven from several host threads: an atomic total plus a per-thread
+// count (graph capture measures the kernels of one unit on its own thread).
+struct LaunchCounter {
+  std::atomic<long long> total{0};
+  static long long& mine() {
+    thread_local long long c = 0;
+    return c;
+  }
+  void operator++() {
+    total.fetch_add(1, std::memory_order_relaxed);
+    ++mine();
+  }
+  void operator+=(long long k) {
+    total.fetch_add(k, std::memory_order_relaxed);
+    mine() += k;
+  }
+};
+extern LaunchCounter g_launches;
 
 }  // namespace heomgb

@@ -14,7 +14,7 @@
 
 namespace heomgb {
 
-long long g_launches = 0;
+LaunchCounter g_launches;
 
 // ------------------------------------------------------------------ complex helpers
 template <typename T> struct CT;

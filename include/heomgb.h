@@ -179,7 +179,12 @@ heomgb_status heomgb_qme_solver_destroy(heomgb_qme_solver* qs);
  * allowed) that share a precision; every stage of every instance runs in the
  * same kernel launch.  The state passed to solve is the concatenation of the
  * models' states in the given order (heomgb_qme_solver_main_size elements).
- * rk4 / lsrk4 only (one dt for all instances). */
+ * rk4 / lsrk4 only (one dt for all instances).  A batch solver runs on a CUDA
+ * stream of its own; each solve first waits for the work already queued on
+ * the first model's stream.  Solves of different batch solvers may be issued
+ * from different host threads and then run concurrently (the Python batch
+ * solver does so for its mixed and FP64 sub-batches); calls on one solver
+ * must not overlap. */
 heomgb_status heomgb_batch_solver_create(heomgb_qme* const* qmes, int count, heomgb_solver* s,
                                          heomgb_qme_solver** out);
 /* Elements of the state a solve of qs expects (main_size(), summed over a batch). */

@@ -1158,64 +1158,36 @@ __device__ bool grid_wait(unsigned long long* bar, unsigned long long& gen) {
   return s_ok != 0;
 }
 
-template <bool HREAL, int EPT>
-__global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const ResidentArgs R) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ DpCtl c;
-  const DiagInst& I = R.inst;
+// Per-thread element data of a resident kernel (fixed for the launch): the
+// thread's elements le = threadIdx.x + r * blockDim.x, r < EPT.
+template <int EPT>
+struct ResElems {
+  int lt[EPT], e[EPT], a[EPT], b[EPT];
+  float2 g[EPT];  // damping coefficient sum_k n_k gamma_k + the element's s_delta term
+};
+
+// Builds the thread's element data and, for its elements, the bath-term table
+// (slot-major: Toff[j * E + le] the neighbour element's offset in the state,
+// -1 for none, Tcf the coefficient; slots 0-3 hold the +1 terms, 4-7 the -1
+// terms, in k_rhs_diag's order; the host admits models with at most 4 + 4
+// terms per element).
+template <int EPT>
+__device__ __forceinline__ void res_build(const DiagInst& I, int l0, int E, int* Toff, float2* Tcf,
+                                          ResElems<EPT>& el) {
   const int n = I.n, n2 = I.n2, K = I.K, void_idx = I.nh;
-  const int l0 = min(I.nh, static_cast<int>(blockIdx.x) * R.ados_per_cta);
-  const int l1 = min(I.nh, l0 + R.ados_per_cta);
-  const int E = (l1 - l0) * n2;
-  const size_t gb = static_cast<size_t>(l0) * n2;
-  float2* Hs = reinterpret_cast<float2*>(smem_raw);
-  double2* Sv = reinterpret_cast<double2*>(smem_raw + ((sizeof(float2) * n2 + 15) & ~static_cast<size_t>(15)));
-  float2* Kv = reinterpret_cast<float2*>(Sv + 2 * static_cast<size_t>(E));  // k_1..k_6
-  float2* yt = Kv + 6 * static_cast<size_t>(E);                             // stage inputs (two copies)
-  // bath terms of every element, fixed for the interval (slot-major): the
-  // neighbour element's offset in the state (-1: none) and its coefficient;
-  // slots 0-3 hold the +1 terms, 4-7 the -1 terms, in k_rhs_diag's order
-  // FP32 copies of both states (Yf[i] = float(S[i]) element-wise, kept with
-  // the states so that no stage converts from FP64)
-  float2* Yf = yt + 2 * static_cast<size_t>(E);
-  int* Toff = reinterpret_cast<int*>(Yf + 2 * static_cast<size_t>(E));
-  float2* Tcf = reinterpret_cast<float2*>(Toff + kResidentTerms * static_cast<size_t>(E));
-  const float2* __restrict__ ngd = I.ngd_f;
-  const float2* __restrict__ cpl = I.c_plus_f;
-  const float2* __restrict__ cmi = I.c_minus_f;
-  const float2* __restrict__ csd = I.c_sd_f;
   const bool sqn = I.sqrt_norm != 0;
-  for (int i = threadIdx.x; i < n2; i += blockDim.x) Hs[i] = I.H_f[i];
-  if (threadIdx.x == 0) c = *R.ctl;
-  __syncthreads();
-  {
-    const int cur = c.cur;
-    for (int le = threadIdx.x; le < E; le += blockDim.x) {
-      const double2 v = R.S[cur][gb + le];
-      Sv[static_cast<size_t>(cur) * E + le] = v;
-      const float2 f = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
-      Yf[static_cast<size_t>(cur) * E + le] = f;
-      yt[le] = f;
-    }
-  }
-  // the thread's elements, fixed for the interval: le = threadIdx.x + r * blockDim.x
-  // (r < EPT; the host sizes the CTA so that they cover E), and
-  // their bath-term table (the host admits models with at most 4 + 4 terms
-  // per element)
-  int el_lt[EPT], el_e[EPT], el_a[EPT], el_b[EPT];
-  float2 el_g[EPT];
 #pragma unroll
   for (int r = 0; r < EPT; ++r) {
     const int le = threadIdx.x + r * blockDim.x;
     const int lec = le < E ? le : 0;
     const int lt = lec / n2, e = lec - lt * n2, a = e / n;
-    el_lt[r] = lt;
-    el_e[r] = e;
-    el_a[r] = a;
-    el_b[r] = e - a * n;
+    el.lt[r] = lt;
+    el.e[r] = e;
+    el.a[r] = a;
+    el.b[r] = e - a * n;
     const int l = min(l0 + lt, I.nh - 1);
-    const float2 g0 = ngd[l], g1 = csd[e];
-    el_g[r] = make_float2(g0.x + g1.x, g0.y + g1.y);
+    const float2 g0 = I.ngd_f[l], g1 = I.c_sd_f[e];
+    el.g[r] = make_float2(g0.x + g1.x, g0.y + g1.y);
     if (le < E) {
       const int* __restrict__ p1row = I.p1 + static_cast<size_t>(l) * K;
       const int* __restrict__ m1row = I.m1 + static_cast<size_t>(l) * K;
@@ -1231,7 +1203,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
           const int lp = __ldg(p1row + k);
           if (lp != void_idx) {
             off = lp * n2 + e;
-            cf = cpl[p];
+            cf = I.c_plus_f[p];
             if (sqn) {
               const float f = sqrtf(static_cast<float>(__ldg(nrow + k) + 1));
               cf = make_float2(f * cf.x, f * cf.y);
@@ -1251,7 +1223,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
           if (lm != void_idx) {
             const int nk_i = __ldg(nrow + k);
             const float nk = sqn ? sqrtf(static_cast<float>(nk_i)) : static_cast<float>(nk_i);
-            const float2 cm = cmi[p];
+            const float2 cm = I.c_minus_f[p];
             off = lm * n2 + e;
             cf = make_float2(nk * cm.x, nk * cm.y);
           }
@@ -1261,6 +1233,107 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
       }
     }
   }
+}
+
+// Own part of a stage (commutator and damping) for the thread's elements: it
+// reads only this CTA's copy Xs of the stage input (k_rhs_diag's order).
+template <bool HREAL, int EPT>
+__device__ __forceinline__ void res_own(const float2* Hs, const float2* Xs, int n, int n2, int E,
+                                        const ResElems<EPT>& el, float2 (&Dp)[EPT]) {
+#pragma unroll
+  for (int r = 0; r < EPT; ++r) {
+    const int le = threadIdx.x + r * blockDim.x;
+    Dp[r] = make_float2(0.f, 0.f);
+    if (le >= E) continue;
+    const int lt = el.lt[r], e = el.e[r], a = el.a[r], b = el.b[r];
+    const float2* yl = Xs + static_cast<size_t>(lt) * n2;
+    float2 acc = make_float2(0.f, 0.f);  // [H, rho]
+    if (HREAL) {
+#pragma unroll 4
+      for (int cc = 0; cc < n; ++cc) {
+        const float hac = Hs[a * n + cc].x, hcb = Hs[cc * n + b].x;
+        const float2 ycb = yl[cc * n + b], yac = yl[a * n + cc];
+        acc.x = fmaf(hac, ycb.x, acc.x);
+        acc.x = fmaf(-hcb, yac.x, acc.x);
+        acc.y = fmaf(hac, ycb.y, acc.y);
+        acc.y = fmaf(-hcb, yac.y, acc.y);
+      }
+    } else {
+      float2 neg = make_float2(0.f, 0.f);
+#pragma unroll 4
+      for (int cc = 0; cc < n; ++cc) {
+        cfma(acc, Hs[a * n + cc], yl[cc * n + b]);
+        cfma(neg, yl[a * n + cc], Hs[cc * n + b]);
+      }
+      acc.x -= neg.x;
+      acc.y -= neg.y;
+    }
+    float2 D = make_float2(-acc.y, acc.x);
+    cfma(D, el.g[r], yl[e]);
+    Dp[r] = D;
+  }
+}
+
+// Bath terms of the thread's elements added to D: all neighbour gathers are
+// issued first (L1-bypassing loads of the other CTAs' stage input Xg, which
+// must not be restrict-qualified: it is written until the grid wait returns).
+template <int EPT>
+__device__ __forceinline__ void res_bath(const float2* Xg, const int* Toff, const float2* Tcf, int E,
+                                         float2 (&D)[EPT]) {
+  float2 vv[EPT][kResidentTerms];
+#pragma unroll
+  for (int r = 0; r < EPT; ++r) {
+    const int le = threadIdx.x + r * blockDim.x;
+#pragma unroll
+    for (int j = 0; j < kResidentTerms; ++j) {
+      const int off = le < E ? Toff[static_cast<size_t>(j) * E + le] : -1;
+      vv[r][j] = off >= 0 ? __ldcg(Xg + off) : make_float2(0.f, 0.f);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < EPT; ++r) {
+    const int le = threadIdx.x + r * blockDim.x;
+    if (le >= E) continue;
+#pragma unroll
+    for (int j = 0; j < kResidentTerms; ++j) cfma(D[r], Tcf[static_cast<size_t>(j) * E + le], vv[r][j]);
+  }
+}
+
+template <bool HREAL, int EPT>
+__global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const ResidentArgs R) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ DpCtl c;
+  const DiagInst& I = R.inst;
+  const int n = I.n, n2 = I.n2;
+  const int l0 = min(I.nh, static_cast<int>(blockIdx.x) * R.ados_per_cta);
+  const int l1 = min(I.nh, l0 + R.ados_per_cta);
+  const int E = (l1 - l0) * n2;
+  const size_t gb = static_cast<size_t>(l0) * n2;
+  // shared memory: H | both states (FP64) | k_1..k_6 | two stage-input copies |
+  // FP32 copies of both states (Yf[i] = float(S[i]), kept with the states so
+  // that no stage converts from FP64) | the bath-term table
+  float2* Hs = reinterpret_cast<float2*>(smem_raw);
+  double2* Sv = reinterpret_cast<double2*>(smem_raw + ((sizeof(float2) * n2 + 15) & ~static_cast<size_t>(15)));
+  float2* Kv = reinterpret_cast<float2*>(Sv + 2 * static_cast<size_t>(E));
+  float2* yt = Kv + 6 * static_cast<size_t>(E);
+  float2* Yf = yt + 2 * static_cast<size_t>(E);
+  int* Toff = reinterpret_cast<int*>(Yf + 2 * static_cast<size_t>(E));
+  float2* Tcf = reinterpret_cast<float2*>(Toff + kResidentTerms * static_cast<size_t>(E));
+  for (int i = threadIdx.x; i < n2; i += blockDim.x) Hs[i] = I.H_f[i];
+  if (threadIdx.x == 0) c = *R.ctl;
+  __syncthreads();
+  {
+    const int cur = c.cur;
+    for (int le = threadIdx.x; le < E; le += blockDim.x) {
+      const double2 v = R.S[cur][gb + le];
+      Sv[static_cast<size_t>(cur) * E + le] = v;
+      const float2 f = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+      Yf[static_cast<size_t>(cur) * E + le] = f;
+      yt[le] = f;
+    }
+  }
+  ResElems<EPT> el;
+  res_build<EPT>(I, l0, E, Toff, Tcf, el);
   unsigned long long gen = 0;
   bool ok = true;
   long long attempts = 0;
@@ -1285,74 +1358,24 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
     float local_f = 0.f;
     for (int s = 0; s < 7 && ok; ++s) {
       // stage input: own ADOs from shared memory, neighbours from global memory
-      // (not __restrict__: other CTAs write it until grid_wait returns, and a
-      // restrict-qualified read-only pointer would let the compiler hoist the
-      // gathers above the wait)
       const float2* Xg = s == 0 ? R.Yb[cur] : (s < 6 ? R.Ytmp[(s - 1) & 1] : R.Yb[1 - cur]);
       const float2* Xs = yt + static_cast<size_t>(s & 1) * E;
       float2* Xn = yt + static_cast<size_t>((s + 1) & 1) * E;
-      // own part first (commutator and damping): it reads only this CTA's
-      // copy of the stage input, published by the last grid_arrive's sync
-      float2 Dp[EPT];
-#pragma unroll
-      for (int r = 0; r < EPT; ++r) {
-        const int le = threadIdx.x + r * blockDim.x;
-        Dp[r] = make_float2(0.f, 0.f);
-        if (le >= E) continue;
-        const int lt = el_lt[r], e = el_e[r], a = el_a[r], b = el_b[r];
-        const float2* yl = Xs + static_cast<size_t>(lt) * n2;
-        // i[H, rho]
-        float2 acc = make_float2(0.f, 0.f);
-        if (HREAL) {
-#pragma unroll 4
-          for (int cc = 0; cc < n; ++cc) {
-            const float hac = Hs[a * n + cc].x, hcb = Hs[cc * n + b].x;
-            const float2 ycb = yl[cc * n + b], yac = yl[a * n + cc];
-            acc.x = fmaf(hac, ycb.x, acc.x);
-            acc.x = fmaf(-hcb, yac.x, acc.x);
-            acc.y = fmaf(hac, ycb.y, acc.y);
-            acc.y = fmaf(-hcb, yac.y, acc.y);
-          }
-        } else {
-          float2 neg = make_float2(0.f, 0.f);
-#pragma unroll 4
-          for (int cc = 0; cc < n; ++cc) {
-            cfma(acc, Hs[a * n + cc], yl[cc * n + b]);
-            cfma(neg, yl[a * n + cc], Hs[cc * n + b]);
-          }
-          acc.x -= neg.x;
-          acc.y -= neg.y;
-        }
-        float2 D = make_float2(-acc.y, acc.x);
-        cfma(D, el_g[r], yl[e]);  // damping (as k_rhs_diag's finish, same order)
-        Dp[r] = D;
-      }
+      float2 D[EPT];
+      res_own<HREAL, EPT>(Hs, Xs, n, n2, E, el, D);
       // the other CTAs' stage input: wait for their stage s - 1 (stage 1 reads
       // the state copy, complete before the attempt)
       if (s > 0) {
         ok = grid_wait(R.bar, gen);
         if (!ok) break;
       }
-      // the neighbour gathers of all the thread's elements (independent loads)
-      float2 vv[EPT][kResidentTerms];
-#pragma unroll
-      for (int r = 0; r < EPT; ++r) {
-        const int le = threadIdx.x + r * blockDim.x;
-#pragma unroll
-        for (int j = 0; j < kResidentTerms; ++j) {
-          const int off = le < E ? Toff[static_cast<size_t>(j) * E + le] : -1;
-          vv[r][j] = off >= 0 ? __ldcg(Xg + off) : make_float2(0.f, 0.f);
-        }
-      }
+      res_bath<EPT>(Xg, Toff, Tcf, E, D);
 #pragma unroll
       for (int r = 0; r < EPT; ++r) {
         const int le = threadIdx.x + r * blockDim.x;
         if (le >= E) continue;
-        float2 D = Dp[r];
-#pragma unroll
-        for (int j = 0; j < kResidentTerms; ++j) cfma(D, Tcf[static_cast<size_t>(j) * E + le], vv[r][j]);
         // stage epilogue (epi_pre + epi_post, mixed form)
-        const float2 k = make_float2(-fdt * D.x, -fdt * D.y);
+        const float2 k = make_float2(-fdt * D[r].x, -fdt * D[r].y);
         const size_t g = gb + le;
         if (s < 5) {  // k_s; next stage input Yb + sum_j A[s+1][j] k_j in FP32
           Kv[static_cast<size_t>(s) * E + le] = k;
@@ -1367,7 +1390,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
           y = make_float2(fmaf(cs, k.x, y.x), fmaf(cs, k.y, y.y));
           Xn[le] = y;
           R.Ytmp[s & 1][g] = y;
-        } else if (s == 5) {  // candidate state rho + sum_j B_j k_j in FP64
+        } else if (s == 5) {  // candidate state rho + sum_j B_j k_j (float-pair sum, FP64 state)
           Kv[5 * static_cast<size_t>(E) + le] = k;
           float2 hi = make_float2(0.f, 0.f), lo = make_float2(0.f, 0.f);
           for (int j = 0; j < 5; ++j) {
@@ -1427,26 +1450,118 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
   }
 }
 
-size_t resident_smem(int n2, int ados_per_cta) {
-  const size_t E = static_cast<size_t>(ados_per_cta) * n2;
-  return ((sizeof(float2) * n2 + 15) & ~static_cast<size_t>(15)) +
-         E * (2 * sizeof(double2) + 6 * sizeof(float2) + 4 * sizeof(float2) +
-              kResidentTerms * (sizeof(int) + sizeof(float2)));
+// The fixed-step RK4 interval of the mixed form in one cooperative launch:
+// n_steps steps of dt_step, then one of dt_last (fixed_step_size_solver's
+// clamped last step), every stage separated by a grid barrier.  A CTA keeps
+// its ADOs' FP64 state and RK4 accumulator, the state's FP32 copy, two
+// stage-input copies and the bath-term table in shared memory; the stage
+// inputs Y2, Y3, Y4 and the new state's FP32 copy go through global memory
+// for the neighbour gathers.  Per element the arithmetic is k_rhs_diag's with
+// the mixed form's RK4 epilogues (EPI_RK4_1..4), in the same order.
+template <bool HREAL, int EPT>
+__global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const ResidentArgs R) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const DiagInst& I = R.inst;
+  const int n = I.n, n2 = I.n2;
+  const int l0 = min(I.nh, static_cast<int>(blockIdx.x) * R.ados_per_cta);
+  const int l1 = min(I.nh, l0 + R.ados_per_cta);
+  const int E = (l1 - l0) * n2;
+  const size_t gb = static_cast<size_t>(l0) * n2;
+  // shared memory: H | state, accumulator (FP64) | two stage-input copies |
+  // the state's FP32 copy | the bath-term table
+  float2* Hs = reinterpret_cast<float2*>(smem_raw);
+  double2* Sv = reinterpret_cast<double2*>(smem_raw + ((sizeof(float2) * n2 + 15) & ~static_cast<size_t>(15)));
+  double2* Av = Sv + E;
+  float2* yt = reinterpret_cast<float2*>(Av + E);
+  float2* Yf = yt + 2 * static_cast<size_t>(E);
+  int* Toff = reinterpret_cast<int*>(Yf + E);
+  float2* Tcf = reinterpret_cast<float2*>(Toff + kResidentTerms * static_cast<size_t>(E));
+  for (int i = threadIdx.x; i < n2; i += blockDim.x) Hs[i] = I.H_f[i];
+  for (int le = threadIdx.x; le < E; le += blockDim.x) {
+    const double2 v = R.S[0][gb + le];
+    Sv[le] = v;
+    const float2 f = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+    Yf[le] = f;
+    yt[le] = f;
+  }
+  __syncthreads();
+  ResElems<EPT> el;
+  res_build<EPT>(I, l0, E, Toff, Tcf, el);
+  unsigned long long gen = 0;
+  bool ok = true;
+  for (long long step = 0; step <= R.n_steps && ok; ++step) {
+    const float fdt = static_cast<float>(step < R.n_steps ? R.dt_step : R.dt_last);
+    for (int s = 0; s < 4 && ok; ++s) {
+      const float2* Xg = s == 0 ? R.Yb[0] : R.Ytmp[(s - 1) & 1];
+      const float2* Xs = yt + static_cast<size_t>(s & 1) * E;
+      float2* Xn = yt + static_cast<size_t>((s + 1) & 1) * E;
+      float2 D[EPT];
+      res_own<HREAL, EPT>(Hs, Xs, n, n2, E, el, D);
+      if (step > 0 || s > 0) {  // the other CTAs' stage input (or new state) of the last stage
+        ok = grid_wait(R.bar, gen);
+        if (!ok) break;
+      }
+      res_bath<EPT>(Xg, Toff, Tcf, E, D);
+#pragma unroll
+      for (int r = 0; r < EPT; ++r) {
+        const int le = threadIdx.x + r * blockDim.x;
+        if (le >= E) continue;
+        const float2 k = make_float2(-fdt * D[r].x, -fdt * D[r].y);
+        const size_t g = gb + le;
+        if (s < 3) {  // rho_n = rho + c*k (FP32 from the state's copy); acc = rho + k/6 or acc += k/3
+          const float cs = static_cast<float>(s == 2 ? 1.0 : 0.5);
+          const float w = static_cast<float>(s == 0 ? (1.0 / 6.0) : (2.0 / 6.0));
+          const float2 yf = Yf[le];
+          const float2 y = make_float2(yf.x + cs * k.x, yf.y + cs * k.y);
+          Xn[le] = y;
+          R.Ytmp[s & 1][g] = y;
+          double2 a = s == 0 ? Sv[le] : Av[le];
+          a.x += static_cast<double>(w * k.x);
+          a.y += static_cast<double>(w * k.y);
+          Av[le] = a;
+        } else {  // rho = acc + k4/6
+          const double2 a = Av[le];
+          const double2 v = make_double2(a.x + static_cast<double>((1.0f / 6.0f) * k.x),
+                                         a.y + static_cast<double>((1.0f / 6.0f) * k.y));
+          Sv[le] = v;
+          const float2 f = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+          Yf[le] = f;
+          Xn[le] = f;  // the next step's stage-1 input (yt[0])
+          R.Yb[0][g] = f;
+        }
+      }
+      grid_arrive(R.bar);
+    }
+  }
+  if (ok)
+    for (int le = threadIdx.x; le < E; le += blockDim.x) R.S[0][gb + le] = Sv[le];
 }
 
-// the kernel instance for H real or complex and EPT elements per thread
-static const void* resident_kernel(bool hreal, int ept) {
-  switch (ept * 2 + (hreal ? 1 : 0)) {
+size_t resident_smem(int n2, int ados_per_cta, bool rk4) {
+  const size_t E = static_cast<size_t>(ados_per_cta) * n2;
+  const size_t per = rk4 ? 2 * sizeof(double2) + 3 * sizeof(float2)
+                         : 2 * sizeof(double2) + 6 * sizeof(float2) + 4 * sizeof(float2);
+  return ((sizeof(float2) * n2 + 15) & ~static_cast<size_t>(15)) +
+         E * (per + kResidentTerms * (sizeof(int) + sizeof(float2)));
+}
+
+// the kernel instance for the scheme, H real or complex and EPT elements per thread
+static const void* resident_kernel(bool rk4, bool hreal, int ept) {
+  switch ((rk4 ? 8 : 0) + ept * 2 + (hreal ? 1 : 0)) {
     case 2: return reinterpret_cast<const void*>(k_dp_resident<false, 1>);
     case 3: return reinterpret_cast<const void*>(k_dp_resident<true, 1>);
     case 4: return reinterpret_cast<const void*>(k_dp_resident<false, 2>);
     case 5: return reinterpret_cast<const void*>(k_dp_resident<true, 2>);
+    case 10: return reinterpret_cast<const void*>(k_rk4_resident<false, 1>);
+    case 11: return reinterpret_cast<const void*>(k_rk4_resident<true, 1>);
+    case 12: return reinterpret_cast<const void*>(k_rk4_resident<false, 2>);
+    case 13: return reinterpret_cast<const void*>(k_rk4_resident<true, 2>);
     default: return nullptr;
   }
 }
 
-int resident_blocks_per_sm(bool hreal, int ept, int block, size_t smem) {
-  const void* kern = resident_kernel(hreal, ept);
+int resident_blocks_per_sm(bool rk4, bool hreal, int ept, int block, size_t smem) {
+  const void* kern = resident_kernel(rk4, hreal, ept);
   if (!kern) return 0;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
     return 0;
@@ -1455,9 +1570,9 @@ int resident_blocks_per_sm(bool hreal, int ept, int block, size_t smem) {
   return nb;
 }
 
-cudaError_t launch_dp_resident(const ResidentArgs& args, bool hreal, int ept, int grid, int block, size_t smem,
-                               cudaStream_t s) {
-  const void* kern = resident_kernel(hreal, ept);
+cudaError_t launch_resident(const ResidentArgs& args, bool rk4, bool hreal, int ept, int grid, int block,
+                            size_t smem, cudaStream_t s) {
+  const void* kern = resident_kernel(rk4, hreal, ept);
   if (!kern) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return e;

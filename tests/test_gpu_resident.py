@@ -104,5 +104,31 @@ def test_resident_only_where_it_applies(monkeypatch):
     _, _, tune = run(p, [0.0, 1.0], monkeypatch, True, precision="fp64")
     assert not tune["resident"]  # the FP64 form keeps the stage kernels
     monkeypatch.setenv("HEOMGB_RESIDENT", "1")
-    qs = lh.qme_solver(lh.from_params(p, precision="mixed"), lh.rk4())
-    assert not qs.tuning()["resident"]  # fixed-step solvers keep the stage kernels
+    qs = lh.qme_solver(lh.from_params(p, precision="mixed"), lh.lsrk4())
+    assert not qs.tuning()["resident"]  # LSRK4 keeps the stage kernels
+
+
+@pytest.mark.parametrize("ept", ["1", "2"])
+@pytest.mark.parametrize("maker", ["spin_boson", "exciton"])
+def test_resident_rk4_bit_identical(maker, ept, monkeypatch):
+    """Fixed-step RK4 in one resident launch per interval: the same
+    per-element arithmetic as the stage kernels and no step control, so every
+    ADO agrees bit for bit after many steps, the clamped last step included."""
+    p = configs.spin_boson(depth=10) if maker == "spin_boson" else configs.exciton_7site(depth=3)
+    dt = 0.005 if maker == "spin_boson" else 0.5
+    t = [0.0, 37 * dt + 0.3 * dt, 60 * dt]  # the first interval ends with a shorter step
+
+    def go(resident):
+        monkeypatch.setenv("HEOMGB_RESIDENT", "1" if resident else "0")
+        monkeypatch.setenv("HEOMGB_RESIDENT_EPT", ept)
+        q = lh.from_params(p, precision="mixed")
+        qs = lh.qme_solver(q, lh.rk4())
+        rho = p.rho0_ground()
+        qs.solve(rho, t, None, {"dt": dt})
+        return rho, qs.stats(), qs.tuning()
+
+    res, st_r, tune = go(True)
+    stg, st_s, _ = go(False)
+    assert tune["resident"]
+    assert st_r["rhs"] == st_s["rhs"]
+    assert np.array_equal(res, stg)

@@ -959,7 +959,12 @@ void run_diff_rm(heomgb_qme* q, double2* drho, const double2* rho, const double*
 void autotune(heomgb_qme_solver* qs);
 void plan_resident(heomgb_qme_solver* qs);
 
-// Arguments of k_dp_resident for the solver's buffers and its tuned shape.
+// The resident kernel of the solver's scheme.
+int resident_scheme(const heomgb_qme_solver* qs) {
+  return qs->kind == HEOMGB_RK4 ? kResidentRk4 : qs->kind == HEOMGB_LSRK4 ? kResidentLs : kResidentDp;
+}
+
+// Arguments of the resident kernels for the solver's buffers and its tuned shape.
 ResidentArgs resident_args(heomgb_qme_solver* qs) {
   ResidentArgs a{};
   a.inst = qs->q->dinst;
@@ -1171,21 +1176,19 @@ void autotune(heomgb_qme_solver* qs) {
     build_plan(qs->plan, insts, best_b, best_e, best_m, qs->mixed, q->n_sm, qs->stream);
 }
 
-// The resident interval (Dormand-Prince or fixed-step RK4) applies to one
+// The resident interval (Dormand-Prince, fixed-step RK4 or LSRK4) applies to one
 // mixed-form model on the diagonal-coupling path without a terminator, when a
 // co-resident grid holds its state in shared memory.  Fewer ADOs per CTA shorten each stage, more
 // CTAs lengthen each grid barrier, so the grid is tuned: every co-resident
 // shape (1 to 8 CTAs per SM, 1 or 2 elements per thread) runs one
-// Dormand-Prince attempt or RK4 step over the solver's zeroed buffers and the fastest is
+// Dormand-Prince attempt or one fixed step over the solver's zeroed buffers and the fastest is
 // kept.  HEOMGB_RESIDENT=0 keeps the stage kernels; HEOMGB_RESIDENT_PER_SM
 // and HEOMGB_RESIDENT_EPT pin the shape.
 void plan_resident(heomgb_qme_solver* qs) {
   heomgb_qme* q = qs->q;
   qs->resident = false;
-  if ((qs->kind != HEOMGB_RKDP && qs->kind != HEOMGB_RK4) || !qs->mixed || q->path != PATH_DIAG ||
-      qs->qmes.size() != 1 || qs->term)
-    return;
-  const bool rk4 = qs->kind == HEOMGB_RK4;
+  if (!qs->mixed || q->path != PATH_DIAG || qs->qmes.size() != 1 || qs->term) return;
+  const int scheme = resident_scheme(qs);
   if (q->dinst.max_terms > kResidentTerms / 2) return;  // the per-element term table holds 4 + 4
   if (const char* env = std::getenv("HEOMGB_RESIDENT"))
     if (std::string(env) == "0") return;
@@ -1212,12 +1215,12 @@ void plan_resident(heomgb_qme_solver* qs) {
       const int apc = (I.nh + target - 1) / target;
       const int grid = (I.nh + apc - 1) / apc;
       if (grid == last_grid) continue;
-      const size_t smem = resident_smem(I.n2, apc, rk4);
+      const size_t smem = resident_smem(I.n2, apc, scheme);
       if (smem > 200 * 1024) continue;
       const int E = apc * I.n2;  // ept elements per thread
       const int block = std::max(64, ((E + ept - 1) / ept + 31) / 32 * 32);
       if (block > kResidentMaxBlock) continue;
-      const int nb = resident_blocks_per_sm(rk4, hreal, ept, block, smem);
+      const int nb = resident_blocks_per_sm(scheme, hreal, ept, block, smem);
       if (nb < 1 || static_cast<long long>(nb) * q->n_sm < grid) continue;
       shapes.push_back(Shape{grid, apc, block, ept, smem});
       last_grid = grid;
@@ -1254,7 +1257,7 @@ void plan_resident(heomgb_qme_solver* qs) {
         a.n_steps = 0;
         a.dt_step = a.dt_last = 1e-3;
         ck(cudaEventRecord(e0, qs->stream), "event");
-        ck(launch_resident(a, rk4, hreal, qs->res_ept, qs->res_grid, qs->res_block, qs->res_smem, qs->stream),
+        ck(launch_resident(a, scheme, hreal, qs->res_ept, qs->res_grid, qs->res_block, qs->res_smem, qs->stream),
            "resident tune");
         ck(cudaEventRecord(e1, qs->stream), "event");
         ck(cudaEventSynchronize(e1), "event sync");
@@ -1442,15 +1445,15 @@ void solve_fixed(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwarg
     t += d;
     if (++m > cap) throw numeric_error("fixed-step loop does not terminate");
   }
-  if (qs->resident) {  // the whole interval as one resident launch (k_rk4_resident)
+  if (qs->resident) {  // the whole interval as one resident launch (k_rk4_resident / k_ls_resident)
     ck(cudaMemsetAsync(qs->res_bar, 0, kResidentBarWords * sizeof(unsigned long long), qs->stream), "barrier reset");
     ResidentArgs a = resident_args(qs);
     a.n_steps = m;
     a.dt_step = dt;
     a.dt_last = last;
     busy_begin(qs);
-    const cudaError_t le = launch_resident(a, true, qs->q->dinst.h_real != 0, qs->res_ept, qs->res_grid,
-                                           qs->res_block, qs->res_smem, qs->stream);
+    const cudaError_t le = launch_resident(a, resident_scheme(qs), qs->q->dinst.h_real != 0, qs->res_ept,
+                                           qs->res_grid, qs->res_block, qs->res_smem, qs->stream);
     if (le != cudaErrorCooperativeLaunchTooLarge) {
       ck(le, "resident interval");
       busy_end(qs);
@@ -1460,7 +1463,7 @@ void solve_fixed(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwarg
          "barrier read");
       ck(cudaStreamSynchronize(qs->stream), "solve sync");
       busy_collect(qs);
-      if (flag) throw cuda_error("resident RK4 interval: a grid barrier wait ran out");
+      if (flag) throw cuda_error("resident fixed-step interval: a grid barrier wait ran out");
       qs->n_rhs += 4 * (m + 1);
       qs->n_attempts += m + 1;
       qs->n_accepted += m + 1;
@@ -1504,7 +1507,7 @@ int solve_resident(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwa
   ck(launch_ctl_init(qs->ctl, t0, dt, t1, atol, rtol, cur, qs->stream), "ctl init");
   ck(cudaMemsetAsync(qs->res_bar, 0, kResidentBarWords * sizeof(unsigned long long), qs->stream), "barrier reset");
   busy_begin(qs);
-  const cudaError_t le = launch_resident(resident_args(qs), false, qs->q->dinst.h_real != 0, qs->res_ept,
+  const cudaError_t le = launch_resident(resident_args(qs), kResidentDp, qs->q->dinst.h_real != 0, qs->res_ept,
                                          qs->res_grid, qs->res_block, qs->res_smem, qs->stream);
   if (le == cudaErrorCooperativeLaunchTooLarge) {
     // the device cannot hold the grid now (another context holds SMs or

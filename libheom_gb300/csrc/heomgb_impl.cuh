@@ -164,8 +164,8 @@ struct DiagSet {
   int tmem_cols;            // tensor-memory columns a CTA of k_rhs_diag_tc allocates
 };
 
-// Resident intervals (k_dp_resident: Dormand-Prince; k_rk4_resident: fixed
-// RK4 steps): one cooperative launch of CTAs of at most kResidentMaxBlock
+// Resident intervals (k_dp_resident: Dormand-Prince; k_rk4_resident and
+// k_ls_resident: fixed RK4 / LSRK4 steps): one cooperative launch of CTAs of at most kResidentMaxBlock
 // threads, CTA b owning ADOs [b*ados_per_cta, ...).
 constexpr int kResidentMaxBlock = 320;
 constexpr int kResidentMaxEpt = 2;         // elements per thread (1 or 2, fixed for the interval)
@@ -181,16 +181,17 @@ struct ResidentArgs {
   unsigned long long* bar;  // grid barrier: kResidentBarWords words, zero at launch (grid_barrier)
   long long n_total;        // elements of the state
   long long max_attempts;   // attempts before the interval gives up (status 3)
-  long long n_steps;        // RK4: steps of dt_step before the last step of dt_last
+  long long n_steps;        // RK4, LSRK4: steps of dt_step before the last step of dt_last
   double dt_step, dt_last;
   int ados_per_cta;
   int pad_;
 };
-// smem of a CTA owning ados_per_cta ADOs (rk4: the fixed-step RK4 kernel,
-// else the Dormand-Prince one)
-size_t resident_smem(int n2, int ados_per_cta, bool rk4);
-int resident_blocks_per_sm(bool rk4, bool hreal, int ept, int block, size_t smem);
-cudaError_t launch_resident(const ResidentArgs& args, bool rk4, bool hreal, int ept, int grid, int block,
+// the resident kernels: Dormand-Prince, fixed-step RK4, fixed-step LSRK4
+constexpr int kResidentDp = 0, kResidentRk4 = 1, kResidentLs = 2;
+// smem of a CTA owning ados_per_cta ADOs in the given scheme's kernel
+size_t resident_smem(int n2, int ados_per_cta, int scheme);
+int resident_blocks_per_sm(int scheme, bool hreal, int ept, int block, size_t smem);
+cudaError_t launch_resident(const ResidentArgs& args, int scheme, bool hreal, int ept, int grid, int block,
                             size_t smem, cudaStream_t s);
 
 // Launchers (kernels.cu).  `mixed` selects FP32 bulk arithmetic; `in_double`

@@ -323,12 +323,13 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
       const double w = st.kind == EPI_RK4_1 ? (1.0 / 6.0) : (2.0 / 6.0);
       double2 a = p.a;
       if constexpr (MIX) {
+        // explicit roundings (no contraction), shared with k_rk4_resident
         const float fdt = static_cast<float>(dt);
-        const float2 k = make_float2(-fdt * Dc.x, -fdt * Dc.y);
-        static_cast<float2*>(st.Ynext)[g] = make_float2(p.f.x + static_cast<float>(c) * k.x,
-                                                        p.f.y + static_cast<float>(c) * k.y);
-        a.x += static_cast<double>(static_cast<float>(w) * k.x);
-        a.y += static_cast<double>(static_cast<float>(w) * k.y);
+        const float2 k = make_float2(__fmul_rn(-fdt, Dc.x), __fmul_rn(-fdt, Dc.y));
+        static_cast<float2*>(st.Ynext)[g] = make_float2(fmaf(static_cast<float>(c), k.x, p.f.x),
+                                                        fmaf(static_cast<float>(c), k.y, p.f.y));
+        a.x += static_cast<double>(__fmul_rn(static_cast<float>(w), k.x));
+        a.y += static_cast<double>(__fmul_rn(static_cast<float>(w), k.y));
       } else {
         const double2 k = make_double2(-dt * D.x, -dt * D.y);
         st_bulk<TC>(st.Ynext, g, make_double2(p.b.x + c * k.x, p.b.y + c * k.y));
@@ -342,8 +343,8 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
       double2 v;
       if constexpr (MIX) {
         const float fdt = static_cast<float>(dt);
-        v = make_double2(p.a.x + static_cast<double>((1.0f / 6.0f) * (-fdt * Dc.x)),
-                         p.a.y + static_cast<double>((1.0f / 6.0f) * (-fdt * Dc.y)));
+        v = make_double2(p.a.x + static_cast<double>(__fmul_rn(1.0f / 6.0f, __fmul_rn(-fdt, Dc.x))),
+                         p.a.y + static_cast<double>(__fmul_rn(1.0f / 6.0f, __fmul_rn(-fdt, Dc.y))));
       } else {
         const double2 k = make_double2(-dt * D.x, -dt * D.y);
         v = make_double2(p.a.x + (1.0 / 6.0) * k.x, p.a.y + (1.0 / 6.0) * k.y);
@@ -354,9 +355,10 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
     }
     case EPI_LS: {  // buff = -buff + k (beta=-1) or k (beta=0); rho += B*buff
       if constexpr (MIX) {  // the buffer combines FP32 k's: kept in FP32; the state update is FP64
+        // explicit roundings (no contraction), shared with k_ls_resident
         const float fdt = static_cast<float>(dt);
-        const float2 k = make_float2(-fdt * Dc.x, -fdt * Dc.y);
-        const float2 b = st.ls_first ? k : make_float2(-p.f.x + k.x, -p.f.y + k.y);
+        const float2 b = st.ls_first ? make_float2(__fmul_rn(-fdt, Dc.x), __fmul_rn(-fdt, Dc.y))
+                                     : make_float2(fmaf(-fdt, Dc.x, -p.f.x), fmaf(-fdt, Dc.y, -p.f.y));
         __stcs(reinterpret_cast<float2*>(st.acc) + g, b);
         const double2 v = make_double2(fma(st.coef, static_cast<double>(b.x), p.b.x),
                                        fma(st.coef, static_cast<double>(b.y), p.b.y));
@@ -1506,23 +1508,23 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
       for (int r = 0; r < EPT; ++r) {
         const int le = threadIdx.x + r * blockDim.x;
         if (le >= E) continue;
-        const float2 k = make_float2(-fdt * D[r].x, -fdt * D[r].y);
+        const float2 k = make_float2(__fmul_rn(-fdt, D[r].x), __fmul_rn(-fdt, D[r].y));
         const size_t g = gb + le;
         if (s < 3) {  // rho_n = rho + c*k (FP32 from the state's copy); acc = rho + k/6 or acc += k/3
           const float cs = static_cast<float>(s == 2 ? 1.0 : 0.5);
           const float w = static_cast<float>(s == 0 ? (1.0 / 6.0) : (2.0 / 6.0));
           const float2 yf = Yf[le];
-          const float2 y = make_float2(yf.x + cs * k.x, yf.y + cs * k.y);
+          const float2 y = make_float2(fmaf(cs, k.x, yf.x), fmaf(cs, k.y, yf.y));
           Xn[le] = y;
           R.Ytmp[s & 1][g] = y;
           double2 a = s == 0 ? Sv[le] : Av[le];
-          a.x += static_cast<double>(w * k.x);
-          a.y += static_cast<double>(w * k.y);
+          a.x += static_cast<double>(__fmul_rn(w, k.x));
+          a.y += static_cast<double>(__fmul_rn(w, k.y));
           Av[le] = a;
         } else {  // rho = acc + k4/6
           const double2 a = Av[le];
-          const double2 v = make_double2(a.x + static_cast<double>((1.0f / 6.0f) * k.x),
-                                         a.y + static_cast<double>((1.0f / 6.0f) * k.y));
+          const double2 v = make_double2(a.x + static_cast<double>(__fmul_rn(1.0f / 6.0f, k.x)),
+                                         a.y + static_cast<double>(__fmul_rn(1.0f / 6.0f, k.y)));
           Sv[le] = v;
           const float2 f = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
           Yf[le] = f;
@@ -1537,17 +1539,91 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
     for (int le = threadIdx.x; le < E; le += blockDim.x) R.S[0][gb + le] = Sv[le];
 }
 
-size_t resident_smem(int n2, int ados_per_cta, bool rk4) {
+// The fixed-step LSRK4 interval of the mixed form in one cooperative launch
+// (2N-storage RK4, lsrk4.h:32-47: buff = -buff + k or k, rho += B_s buff): a
+// CTA keeps its ADOs' FP64 state (updated in place), the FP32 buffer, the
+// state's FP32 copy (the stage input) and the bath-term table in shared
+// memory; the new state's FP32 copy goes through global memory (alternating
+// two buffers) for the neighbour gathers.  Same per-element arithmetic as
+// k_rhs_diag with the mixed form's EPI_LS epilogue.
+template <bool HREAL, int EPT>
+__global__ void __launch_bounds__(kResidentMaxBlock, 2) k_ls_resident(const ResidentArgs R) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const DiagInst& I = R.inst;
+  const int n = I.n, n2 = I.n2;
+  const int l0 = min(I.nh, static_cast<int>(blockIdx.x) * R.ados_per_cta);
+  const int l1 = min(I.nh, l0 + R.ados_per_cta);
+  const int E = (l1 - l0) * n2;
+  const size_t gb = static_cast<size_t>(l0) * n2;
+  // shared memory: H | state (FP64) | buffer | the state's FP32 copy | the bath-term table
+  float2* Hs = reinterpret_cast<float2*>(smem_raw);
+  double2* Sv = reinterpret_cast<double2*>(smem_raw + ((sizeof(float2) * n2 + 15) & ~static_cast<size_t>(15)));
+  float2* Bv = reinterpret_cast<float2*>(Sv + E);
+  float2* Yf = Bv + E;
+  int* Toff = reinterpret_cast<int*>(Yf + E);
+  float2* Tcf = reinterpret_cast<float2*>(Toff + kResidentTerms * static_cast<size_t>(E));
+  for (int i = threadIdx.x; i < n2; i += blockDim.x) Hs[i] = I.H_f[i];
+  for (int le = threadIdx.x; le < E; le += blockDim.x) {
+    const double2 v = R.S[0][gb + le];
+    Sv[le] = v;
+    Yf[le] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+  }
+  __syncthreads();
+  ResElems<EPT> el;
+  res_build<EPT>(I, l0, E, Toff, Tcf, el);
+  const double B[4] = {1.0 / 3.0, 3.0 / 4.0, 2.0 / 3.0, 1.0 / 4.0};  // lsrk4.h:39-46
+  unsigned long long gen = 0;
+  bool ok = true;
+  for (long long step = 0; step <= R.n_steps && ok; ++step) {
+    const float fdt = static_cast<float>(step < R.n_steps ? R.dt_step : R.dt_last);
+    for (int s = 0; s < 4 && ok; ++s) {
+      const float2* Xg = R.Yb[s & 1];
+      float2 D[EPT];
+      res_own<HREAL, EPT>(Hs, Yf, n, n2, E, el, D);  // all reads of Yf end before the wait's sync
+      if (step > 0 || s > 0) {
+        ok = grid_wait(R.bar, gen);
+        if (!ok) break;
+      }
+      res_bath<EPT>(Xg, Toff, Tcf, E, D);
+#pragma unroll
+      for (int r = 0; r < EPT; ++r) {
+        const int le = threadIdx.x + r * blockDim.x;
+        if (le >= E) continue;
+        float2 b;
+        if (s == 0) {
+          b = make_float2(__fmul_rn(-fdt, D[r].x), __fmul_rn(-fdt, D[r].y));
+        } else {
+          const float2 pb = Bv[le];
+          b = make_float2(fmaf(-fdt, D[r].x, -pb.x), fmaf(-fdt, D[r].y, -pb.y));
+        }
+        Bv[le] = b;
+        const double2 sp = Sv[le];
+        const double2 v = make_double2(fma(B[s], static_cast<double>(b.x), sp.x),
+                                       fma(B[s], static_cast<double>(b.y), sp.y));
+        Sv[le] = v;
+        const float2 f = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+        Yf[le] = f;
+        R.Yb[1 - (s & 1)][gb + le] = f;
+      }
+      grid_arrive(R.bar);
+    }
+  }
+  if (ok)
+    for (int le = threadIdx.x; le < E; le += blockDim.x) R.S[0][gb + le] = Sv[le];
+}
+
+size_t resident_smem(int n2, int ados_per_cta, int scheme) {
   const size_t E = static_cast<size_t>(ados_per_cta) * n2;
-  const size_t per = rk4 ? 2 * sizeof(double2) + 3 * sizeof(float2)
-                         : 2 * sizeof(double2) + 6 * sizeof(float2) + 4 * sizeof(float2);
+  const size_t per = scheme == kResidentRk4   ? 2 * sizeof(double2) + 3 * sizeof(float2)
+                     : scheme == kResidentLs  ? sizeof(double2) + 2 * sizeof(float2)
+                                              : 2 * sizeof(double2) + 6 * sizeof(float2) + 4 * sizeof(float2);
   return ((sizeof(float2) * n2 + 15) & ~static_cast<size_t>(15)) +
          E * (per + kResidentTerms * (sizeof(int) + sizeof(float2)));
 }
 
 // the kernel instance for the scheme, H real or complex and EPT elements per thread
-static const void* resident_kernel(bool rk4, bool hreal, int ept) {
-  switch ((rk4 ? 8 : 0) + ept * 2 + (hreal ? 1 : 0)) {
+static const void* resident_kernel(int scheme, bool hreal, int ept) {
+  switch (scheme * 8 + ept * 2 + (hreal ? 1 : 0)) {
     case 2: return reinterpret_cast<const void*>(k_dp_resident<false, 1>);
     case 3: return reinterpret_cast<const void*>(k_dp_resident<true, 1>);
     case 4: return reinterpret_cast<const void*>(k_dp_resident<false, 2>);
@@ -1556,12 +1632,16 @@ static const void* resident_kernel(bool rk4, bool hreal, int ept) {
     case 11: return reinterpret_cast<const void*>(k_rk4_resident<true, 1>);
     case 12: return reinterpret_cast<const void*>(k_rk4_resident<false, 2>);
     case 13: return reinterpret_cast<const void*>(k_rk4_resident<true, 2>);
+    case 18: return reinterpret_cast<const void*>(k_ls_resident<false, 1>);
+    case 19: return reinterpret_cast<const void*>(k_ls_resident<true, 1>);
+    case 20: return reinterpret_cast<const void*>(k_ls_resident<false, 2>);
+    case 21: return reinterpret_cast<const void*>(k_ls_resident<true, 2>);
     default: return nullptr;
   }
 }
 
-int resident_blocks_per_sm(bool rk4, bool hreal, int ept, int block, size_t smem) {
-  const void* kern = resident_kernel(rk4, hreal, ept);
+int resident_blocks_per_sm(int scheme, bool hreal, int ept, int block, size_t smem) {
+  const void* kern = resident_kernel(scheme, hreal, ept);
   if (!kern) return 0;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
     return 0;
@@ -1570,9 +1650,9 @@ int resident_blocks_per_sm(bool rk4, bool hreal, int ept, int block, size_t smem
   return nb;
 }
 
-cudaError_t launch_resident(const ResidentArgs& args, bool rk4, bool hreal, int ept, int grid, int block,
+cudaError_t launch_resident(const ResidentArgs& args, int scheme, bool hreal, int ept, int grid, int block,
                             size_t smem, cudaStream_t s) {
-  const void* kern = resident_kernel(rk4, hreal, ept);
+  const void* kern = resident_kernel(scheme, hreal, ept);
   if (!kern) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return e;

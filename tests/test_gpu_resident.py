@@ -104,14 +104,15 @@ def test_resident_only_where_it_applies(monkeypatch):
     _, _, tune = run(p, [0.0, 1.0], monkeypatch, True, precision="fp64")
     assert not tune["resident"]  # the FP64 form keeps the stage kernels
     monkeypatch.setenv("HEOMGB_RESIDENT", "1")
-    qs = lh.qme_solver(lh.from_params(p, precision="mixed"), lh.lsrk4())
-    assert not qs.tuning()["resident"]  # LSRK4 keeps the stage kernels
+    qs = lh.qme_solver(lh.from_params(p, precision="fp64"), lh.rk4())
+    assert not qs.tuning()["resident"]  # the FP64 form keeps the stage kernels for fixed steps too
 
 
+@pytest.mark.parametrize("solver", ["rk4", "lsrk4"])
 @pytest.mark.parametrize("ept", ["1", "2"])
 @pytest.mark.parametrize("maker", ["spin_boson", "exciton"])
-def test_resident_rk4_bit_identical(maker, ept, monkeypatch):
-    """Fixed-step RK4 in one resident launch per interval: the same
+def test_resident_fixed_step_bit_identical(maker, ept, solver, monkeypatch):
+    """Fixed-step RK4 / LSRK4 in one resident launch per interval: the same
     per-element arithmetic as the stage kernels and no step control, so every
     ADO agrees bit for bit after many steps, the clamped last step included."""
     p = configs.spin_boson(depth=10) if maker == "spin_boson" else configs.exciton_7site(depth=3)
@@ -122,7 +123,7 @@ def test_resident_rk4_bit_identical(maker, ept, monkeypatch):
         monkeypatch.setenv("HEOMGB_RESIDENT", "1" if resident else "0")
         monkeypatch.setenv("HEOMGB_RESIDENT_EPT", ept)
         q = lh.from_params(p, precision="mixed")
-        qs = lh.qme_solver(q, lh.rk4())
+        qs = lh.qme_solver(q, lh.SOLVERS[solver]())
         rho = p.rho0_ground()
         qs.solve(rho, t, None, {"dt": dt})
         return rho, qs.stats(), qs.tuning()

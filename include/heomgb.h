@@ -203,13 +203,14 @@ heomgb_status heomgb_qme_solver_tuning(const heomgb_qme_solver* qs, int* block, 
  * that variant, HEOMGB_TCORE=0 keeps it out of the search.  No reference
  * counterpart: the reference evaluates every term on CUDA cores. */
 heomgb_status heomgb_qme_solver_tensor_cores(const heomgb_qme_solver* qs, int* on);
-/* 1 when the solver runs each output interval (rkdp or rk4) as one resident
+/* 1 when the solver runs each output interval (rkdp, rk4, lsrk4) as one resident
  * cooperative launch (mixed form, one model on the diagonal-coupling path,
  * state held in the CTAs' shared memory between stages), else 0; grid and
  * ados_per_cta (may be NULL) receive its CTAs and the ADOs each owns.
  * HEOMGB_RESIDENT=0 keeps the per-stage kernels.  No reference counterpart:
- * rkdp::solve_adaptive_step (rkdp.h:81-179) and rk4::solve_fixed_step
- * (rk4.h:40-65) issue every stage's BLAS calls from the host. */
+ * rkdp::solve_adaptive_step (rkdp.h:81-179), rk4::solve_fixed_step
+ * (rk4.h:40-65) and lsrk4::solve_fixed_step (lsrk4.h:32-47) issue every
+ * stage's BLAS calls from the host. */
 heomgb_status heomgb_qme_solver_resident(const heomgb_qme_solver* qs, int* on, int* grid, int* ados_per_cta);
 
 /* qme_solver::solve(rho, t_list, n_t, callback, kwargs) -- qme_solver.h:44-52,

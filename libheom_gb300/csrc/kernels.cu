@@ -1062,7 +1062,7 @@ __device__ __forceinline__ double diag_tile_tc(const DiagInst* __restrict__ I, c
 // (128 or 80) the autotuner picks between.
 template <typename TB, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_rhs_diag_tc(const DiagSet ds, const Stage st) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];  // operands are rounded up to 128 bytes below
   double dt;
   int cur;
   // one verdict per CTA: another CTA of this launch may flag the controller

@@ -327,7 +327,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         ms64 = e0.elapsed_time(e1)
         tm64 = qs64.timing()
-        avg64 = 1e-3 * tm64["busy_ms"] / max(tm64["kernels"], 1)
+        avg64 = 1e-3 * tm64["busy_ms"] / max(st64["rhs"], 1)  # per stage evaluated (an interval launch runs many)
         fl64 = w.flops_per_launch() / avg64 / 1e12
         plain = {"value": st64["ado_updates"] / (ms64 / 1e3), "ms_per_step": ms64,
                  "attempts": st64["attempts"], "avg_stage_kernel_us": 1e6 * avg64, "tuning": qs64.tuning(),
@@ -406,18 +406,31 @@ def run_ours(args):
     achieved = alg_bytes_per_launch / avg_launch_s / 1e9
     flops = w.flops_per_launch()
     tuning = qs.tuning()
-    resident = isinstance(tuning, dict) and tuning.get("resident", False)
+    part_tunings = tuning.get("parts", [tuning]) if isinstance(tuning, dict) else []
+    resident = any(t.get("resident", False) for t in part_tunings)
+    local = any(t.get("local", False) for t in part_tunings)
+    if resident:
+        kernel = {"rkdp": "k_dp_resident", "rk4": "k_rk4_resident", "lsrk4": "k_ls_resident"}[wl["solver"]] + (
+            " (one cooperative launch per output interval: fused RHS and stage epilogues"
+            + (", error norm and step control" if wl["solver"] == "rkdp" else "") + "; state in shared memory)")
+    elif local:
+        kernel = ("k_rk4_local (one launch per output interval; every instance inside one CTA with its stage "
+                  "inputs in shared memory, no grid-wide synchronisation)"
+                  + ("" if all(t.get("local", False) for t in part_tunings) else "; k_rhs_diag for the other part"))
+    else:
+        kernel = "k_rhs_diag (fused RHS + stage epilogue)"
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": profile_traffic(args.workload, args.form), "peak_source": peak_kind,
-            "kernel": ("k_dp_resident (one cooperative launch per output interval: fused RHS, stage epilogues, "
-                       "error norm and step control; state in shared memory)") if resident
-            else "k_rhs_diag (fused RHS + stage epilogue)",
+            "kernel": kernel,
             "alg_bytes_per_launch": alg_bytes_per_launch, "avg_launch_us": avg_launch_s * 1e6,
             "alg_flops_per_launch": flops, "achieved_tflops": flops / avg_launch_s / 1e12,
             "fma_peaks_tflops": {"fp64": fma_peaks[0], "fp32": fma_peaks[1]},
             "note": ("per stage: CUDA-event time of the resident launches / stages evaluated (grid barriers "
                      "included); bytes per stage are the algorithmic bytes of one stage over the whole state, "
                      "most of which stay in shared memory and L2") if resident
+            else ("per stage: CUDA-event time of the interval launches (the longest sub-batch; sub-batches run "
+                  "concurrently) / stages evaluated; bytes per stage are the algorithmic bytes of one stage over "
+                  "the whole state, which stay in shared memory and L2") if local
             else ("avg launch time = CUDA-event time of the graph replays / stages evaluated (one stage "
                   "over the whole state; intra-graph gaps and the no-op launches replayed after an interval "
                   "ends are included in the time, not in the count)")}

@@ -73,6 +73,7 @@ SIGNATURES = {
     "heomgb_qme_solver_tuning": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p]),
     "heomgb_qme_solver_tensor_cores": (ctypes.c_int, [ctypes.c_void_p, c_int_p]),
     "heomgb_qme_solver_resident": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p]),
+    "heomgb_qme_solver_local": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p]),
     "heomgb_qme_solver_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                                CALLBACK, ctypes.c_void_p, ctypes.POINTER(Kwargs)]),
     "heomgb_qme_solver_solve_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -365,6 +365,15 @@ struct heomgb_qme_solver {
   size_t res_smem = 0;
   unsigned long long* res_bar = nullptr;
   double* res_partials = nullptr;
+  // instance-resident RK4 intervals of a batch (k_rk4_local): one launch per
+  // output interval, bins of whole instances per CTA, no grid barrier
+  bool local = false;
+  int loc_grid = 0, loc_block = 0;
+  size_t loc_smem = 0;
+  DeviceArena loc_arena;
+  const int* loc_bin_ptr = nullptr;
+  const int* loc_bin_inst = nullptr;
+  float stage_ms = 0.f;  // the autotuned stage kernel's time per launch (0: not timed)
   // batch solvers run on a stream of their own (sub-batches of one batch run
   // concurrently), ordered after the model stream's pending work at each solve
   cudaStream_t own_stream = nullptr;
@@ -958,6 +967,7 @@ void run_diff_rm(heomgb_qme* q, double2* drho, const double2* rho, const double*
 // ------------------------------------------------------------------ solvers
 void autotune(heomgb_qme_solver* qs);
 void plan_resident(heomgb_qme_solver* qs);
+void plan_local(heomgb_qme_solver* qs);
 
 // The resident kernel of the solver's scheme.
 int resident_scheme(const heomgb_qme_solver* qs) {
@@ -1029,6 +1039,7 @@ void alloc_solver(heomgb_qme_solver* qs) {
   }
   qs->partials = static_cast<double*>(A.alloc(sizeof(double) * std::max(qs->grid, 1)));
   plan_resident(qs);
+  plan_local(qs);
 }
 
 // Tile shape search for the diagonal-coupling kernel: CTA size x elements per
@@ -1170,6 +1181,7 @@ void autotune(heomgb_qme_solver* qs) {
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  qs->stage_ms = best < 1e29f ? best / 3.f : 0.f;
   if (best_tc)
     build_plan(qs->plan, insts, best_tc_b, 1, best_tc_m, qs->mixed, q->n_sm, qs->stream, true);
   else
@@ -1282,6 +1294,141 @@ void plan_resident(heomgb_qme_solver* qs) {
   qs->res_ept = shapes[best].ept;
   qs->res_smem = shapes[best].smem;
   qs->resident = true;
+}
+
+// Instance-resident RK4 intervals (k_rk4_local) apply to fixed-step RK4 on the
+// diagonal-coupling path without a terminator, when no cooperative resident
+// interval was planned and every instance fits one CTA's shared memory.
+// Instances are packed into bins (largest first, each into the least-loaded
+// bin with room: at most kLocalMaxInst instances and the shared-memory cap),
+// for 1, 2 or 4 bins per SM and 128, 256 or 512 threads per CTA; every shape runs
+// four steps over the solver's zeroed buffers, the fastest is kept, and it
+// replaces the graphs of stage kernels only where it beats four launches of
+// the autotuned stage kernel.  HEOMGB_LOCAL=0 keeps the stage kernels,
+// HEOMGB_LOCAL=1 takes the fastest shape without the comparison.
+void plan_local(heomgb_qme_solver* qs) {
+  heomgb_qme* q = qs->q;
+  qs->local = false;
+  if (qs->kind != HEOMGB_RK4 || q->path != PATH_DIAG || qs->term || qs->resident || qs->plan.tcore) return;
+  bool force = false;
+  if (const char* env = std::getenv("HEOMGB_LOCAL")) {
+    if (std::string(env) == "0") return;
+    force = std::string(env) == "1";
+  }
+  const std::vector<DiagInst>& insts = qs->plan.inst;
+  if (insts.empty()) return;
+  for (const DiagInst& I : insts)
+    if (I.n2 > kLocalMaxN2 || I.nh > kLocalMaxAdo || I.term_p) return;
+  const bool mixed = qs->mixed;
+  auto inst_smem = [&](const DiagInst& I) { return local_bin_smem(&I.n2, &I.nh, 1, mixed); };
+  std::vector<int> order(insts.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = static_cast<int>(i);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return static_cast<long long>(insts[x].n2) * insts[x].nh > static_cast<long long>(insts[y].n2) * insts[y].nh;
+  });
+  struct Shape {
+    int grid, block;
+    size_t smem;
+    std::vector<int> ptr, list;
+  };
+  std::vector<Shape> shapes;
+  for (int per_sm : {1, 2, 4}) {
+    const size_t cap = (200u * 1024u) / per_sm;
+    const int want = static_cast<int>(std::min<size_t>(insts.size(), static_cast<size_t>(per_sm) * q->n_sm));
+    std::vector<long long> load(want, 0);
+    std::vector<size_t> used(want, 0);
+    std::vector<std::vector<int>> bins(want);
+    bool fits = true;
+    for (int i : order) {
+      const size_t si = inst_smem(insts[i]);
+      if (si > cap) {
+        fits = false;
+        break;
+      }
+      int pick_b = -1;
+      for (size_t b = 0; b < bins.size(); ++b)
+        if (used[b] + si <= cap && static_cast<int>(bins[b].size()) < kLocalMaxInst &&
+            (pick_b < 0 || load[b] < load[pick_b]))
+          pick_b = static_cast<int>(b);
+      if (pick_b < 0) {  // every bin is full: open another (it runs in a later wave)
+        bins.emplace_back();
+        load.push_back(0);
+        used.push_back(0);
+        pick_b = static_cast<int>(bins.size()) - 1;
+      }
+      bins[pick_b].push_back(i);
+      load[pick_b] += static_cast<long long>(insts[i].n2) * insts[i].nh;
+      used[pick_b] += si;
+    }
+    if (!fits) continue;
+    Shape sh;
+    sh.smem = 16;
+    sh.ptr.push_back(0);
+    // the heaviest bins first, so that later waves (if any) hold the light ones
+    std::vector<int> bo(bins.size());
+    for (size_t b = 0; b < bo.size(); ++b) bo[b] = static_cast<int>(b);
+    std::stable_sort(bo.begin(), bo.end(), [&](int x, int y) { return load[x] > load[y]; });
+    for (int b : bo) {
+      if (bins[b].empty()) continue;
+      for (int i : bins[b]) sh.list.push_back(i);
+      sh.ptr.push_back(static_cast<int>(sh.list.size()));
+      sh.smem = std::max(sh.smem, used[b]);
+    }
+    sh.grid = static_cast<int>(sh.ptr.size()) - 1;
+    for (int block : {128, 256, 512}) {
+      if (local_blocks_per_sm(mixed, block, sh.smem) < 1) continue;
+      sh.block = block;
+      shapes.push_back(sh);
+    }
+  }
+  if (shapes.empty()) return;
+  const size_t bd = sizeof(double2) * qs->N;
+  for (double2* p : {qs->S[0], qs->acc})
+    if (p) ck(cudaMemsetAsync(p, 0, bd, qs->stream), "memset");
+  if (mixed) ck(cudaMemsetAsync(qs->Yb[0], 0, sizeof(float2) * qs->N, qs->stream), "memset");
+  cudaEvent_t e0, e1;
+  ck(cudaEventCreate(&e0), "event");
+  ck(cudaEventCreate(&e1), "event");
+  float best_ms = 1e30f;
+  size_t best = 0;
+  for (size_t i = 0; i < shapes.size(); ++i) {
+    DeviceArena tab;
+    LocalArgs a{};
+    a.inst = qs->plan.ds.inst;
+    a.bin_ptr = tab.upload(shapes[i].ptr, qs->stream);
+    a.bin_inst = tab.upload(shapes[i].list, qs->stream);
+    a.S = qs->S[0];
+    a.acc = qs->acc;
+    a.Yf = mixed ? static_cast<float2*>(qs->Yb[0]) : nullptr;
+    a.n_steps = 3;  // four steps
+    a.dt_step = a.dt_last = 1e-3;
+    float ms_i = 1e30f;
+    for (int r = 0; r < 4; ++r) {  // one warm-up, best of three
+      ck(cudaEventRecord(e0, qs->stream), "event");
+      ck(launch_local(a, mixed, shapes[i].grid, shapes[i].block, shapes[i].smem, qs->stream), "local tune");
+      ck(cudaEventRecord(e1, qs->stream), "event");
+      ck(cudaEventSynchronize(e1), "event sync");
+      float ms = 0.f;
+      ck(cudaEventElapsedTime(&ms, e0, e1), "event time");
+      if (r > 0) ms_i = std::min(ms_i, ms);
+    }
+    if (ms_i < best_ms) {
+      best_ms = ms_i;
+      best = i;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (!force && !(best_ms / 4.f < 4.f * qs->stage_ms)) return;
+  const Shape& sh = shapes[best];
+  qs->loc_arena.release();
+  qs->loc_bin_ptr = qs->loc_arena.upload(sh.ptr, qs->stream);
+  qs->loc_bin_inst = qs->loc_arena.upload(sh.list, qs->stream);
+  ck(cudaStreamSynchronize(qs->stream), "local plan upload");
+  qs->loc_grid = sh.grid;
+  qs->loc_block = sh.block;
+  qs->loc_smem = sh.smem;
+  qs->local = true;
 }
 
 Stage solver_stage(heomgb_qme_solver* qs) {
@@ -1444,6 +1591,26 @@ void solve_fixed(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwarg
     }
     t += d;
     if (++m > cap) throw numeric_error("fixed-step loop does not terminate");
+  }
+  if (qs->local) {  // the whole interval as one launch of instance-resident bins (k_rk4_local)
+    LocalArgs a{};
+    a.inst = qs->plan.ds.inst;
+    a.bin_ptr = qs->loc_bin_ptr;
+    a.bin_inst = qs->loc_bin_inst;
+    a.S = qs->S[0];
+    a.acc = qs->acc;
+    a.Yf = qs->mixed ? static_cast<float2*>(qs->Yb[0]) : nullptr;
+    a.n_steps = m;
+    a.dt_step = dt;
+    a.dt_last = last;
+    busy_begin(qs);
+    ck(launch_local(a, qs->mixed, qs->loc_grid, qs->loc_block, qs->loc_smem, qs->stream), "instance-resident interval");
+    busy_end(qs);
+    qs->replayed_kernels += 1;
+    qs->n_rhs += 4 * (m + 1);
+    qs->n_attempts += m + 1;
+    qs->n_accepted += m + 1;
+    return;
   }
   if (qs->resident) {  // the whole interval as one resident launch (k_rk4_resident / k_ls_resident)
     ck(cudaMemsetAsync(qs->res_bar, 0, kResidentBarWords * sizeof(unsigned long long), qs->stream), "barrier reset");
@@ -1994,6 +2161,15 @@ heomgb_status heomgb_qme_solver_resident(const heomgb_qme_solver* qs, int* on, i
     *on = qs->resident ? 1 : 0;
     if (grid) *grid = qs->resident ? qs->res_grid : 0;
     if (ados_per_cta) *ados_per_cta = qs->resident ? qs->res_apc : 0;
+  });
+}
+
+heomgb_status heomgb_qme_solver_local(const heomgb_qme_solver* qs, int* on, int* bins, int* block) {
+  return guard([&] {
+    require(qs != nullptr && on != nullptr, "null argument");
+    *on = qs->local ? 1 : 0;
+    if (bins) *bins = qs->local ? qs->loc_grid : 0;
+    if (block) *block = qs->local ? qs->loc_block : 0;
   });
 }
 

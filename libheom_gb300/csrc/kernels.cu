@@ -11,6 +11,7 @@
 #include <type_traits>
 
 #include "heomgb_impl.cuh"
+#include "fpconv.cuh"
 
 namespace heomgb {
 
@@ -44,8 +45,19 @@ template <typename C> __device__ __forceinline__ void cfma(C& acc, C a, C b) {
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+// A hierarchy occupation 0 <= v < 2^31 as TC.  For double the IEEE-754
+// encoding is assembled with integer operations (exact, like the conversion
+// instruction), which keeps it off this part's narrow FP64 pipe.
+template <typename TC> __device__ __forceinline__ TC occ(int v);
+template <> __device__ __forceinline__ float occ<float>(int v) { return static_cast<float>(v); }
+template <> __device__ __forceinline__ double occ<double>(int v) {
+  if (v <= 0) return 0.0;
+  const int e = 31 - __clz(v);  // the leading bit; it moves to bit 52 of the significand
+  const unsigned long long sig = static_cast<unsigned long long>(v) << (52 - e);
+  return __longlong_as_double((static_cast<unsigned long long>(1023 + e) << 52) | (sig & ((1ull << 52) - 1)));
+}
 __device__ __forceinline__ double2 to_d(double2 v) { return v; }
-__device__ __forceinline__ double2 to_d(float2 v) { return make_double2(v.x, v.y); }
+__device__ __forceinline__ double2 to_d(float2 v) { return make_double2(f2d(v.x), f2d(v.y)); }
 
 template <typename TC> __device__ __forceinline__ const cx_t<TC>* pick(const double2* d, const float2* f);
 template <> __device__ __forceinline__ const double2* pick<double>(const double2* d, const float2*) { return d; }
@@ -56,7 +68,7 @@ template <typename TC> __device__ __forceinline__ void st_bulk(void* base, size_
   if constexpr (std::is_same<TC, double>::value) {
     static_cast<double2*>(base)[g] = v;
   } else {
-    static_cast<float2*>(base)[g] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+    static_cast<float2*>(base)[g] = make_float2(d2f(v.x), d2f(v.y));
   }
 }
 template <typename TC> __device__ __forceinline__ double2 ld_bulk(const void* base, size_t g) {
@@ -73,7 +85,7 @@ template <typename TC> __device__ __forceinline__ void st_bulk_cs(void* base, si
   if constexpr (std::is_same<TC, double>::value) {
     __stcs(static_cast<double2*>(base) + g, v);
   } else {
-    __stcs(static_cast<float2*>(base) + g, make_float2(static_cast<float>(v.x), static_cast<float>(v.y)));
+    __stcs(static_cast<float2*>(base) + g, make_float2(d2f(v.x), d2f(v.y)));
   }
 }
 template <typename TC> __device__ __forceinline__ double2 ld_bulk_cs(const void* base, size_t g) {
@@ -88,7 +100,7 @@ template <typename TC> __device__ __forceinline__ double2 as_bulk(double2 v) {
   if constexpr (std::is_same<TC, double>::value) {
     return v;
   } else {
-    return make_double2(static_cast<float>(v.x), static_cast<float>(v.y));
+    return make_double2(f2d(d2f(v.x)), f2d(d2f(v.y)));
   }
 }
 
@@ -291,7 +303,7 @@ __device__ __forceinline__ EpiPre epi_pre(const Stage& st, size_t g, int cur) {
       if constexpr (MIX) {  // scale from the bulk copies of both states
         const float2 x1 = static_cast<const float2*>(st.Yb[1 - cur])[g];
         const float2 x2 = static_cast<const float2*>(st.Yb[cur])[g];
-        p.m = static_cast<double>(fmaxf(x1.x * x1.x + x1.y * x1.y, x2.x * x2.x + x2.y * x2.y));
+        p.m = f2d(fmaxf(x1.x * x1.x + x1.y * x1.y, x2.x * x2.x + x2.y * x2.y));
       } else {
         const double2 x1 = __ldcs(st.S[1 - cur] + g);
         const double2 x2 = __ldcs(st.S[cur] + g);
@@ -328,13 +340,14 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
         const float2 k = make_float2(__fmul_rn(-fdt, Dc.x), __fmul_rn(-fdt, Dc.y));
         static_cast<float2*>(st.Ynext)[g] = make_float2(fmaf(static_cast<float>(c), k.x, p.f.x),
                                                         fmaf(static_cast<float>(c), k.y, p.f.y));
-        a.x += static_cast<double>(__fmul_rn(static_cast<float>(w), k.x));
-        a.y += static_cast<double>(__fmul_rn(static_cast<float>(w), k.y));
+        a.x += f2d(__fmul_rn(static_cast<float>(w), k.x));
+        a.y += f2d(__fmul_rn(static_cast<float>(w), k.y));
       } else {
+        // explicit FMAs, shared with k_rk4_local
         const double2 k = make_double2(-dt * D.x, -dt * D.y);
-        st_bulk<TC>(st.Ynext, g, make_double2(p.b.x + c * k.x, p.b.y + c * k.y));
-        a.x += w * k.x;
-        a.y += w * k.y;
+        st_bulk<TC>(st.Ynext, g, make_double2(fma(c, k.x, p.b.x), fma(c, k.y, p.b.y)));
+        a.x = fma(w, k.x, a.x);
+        a.y = fma(w, k.y, a.y);
       }
       __stcs(st.acc + g, a);
       return 0.0;
@@ -343,11 +356,11 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
       double2 v;
       if constexpr (MIX) {
         const float fdt = static_cast<float>(dt);
-        v = make_double2(p.a.x + static_cast<double>(__fmul_rn(1.0f / 6.0f, __fmul_rn(-fdt, Dc.x))),
-                         p.a.y + static_cast<double>(__fmul_rn(1.0f / 6.0f, __fmul_rn(-fdt, Dc.y))));
+        v = make_double2(p.a.x + f2d(__fmul_rn(1.0f / 6.0f, __fmul_rn(-fdt, Dc.x))),
+                         p.a.y + f2d(__fmul_rn(1.0f / 6.0f, __fmul_rn(-fdt, Dc.y))));
       } else {
         const double2 k = make_double2(-dt * D.x, -dt * D.y);
-        v = make_double2(p.a.x + (1.0 / 6.0) * k.x, p.a.y + (1.0 / 6.0) * k.y);
+        v = make_double2(fma(1.0 / 6.0, k.x, p.a.x), fma(1.0 / 6.0, k.y, p.a.y));
       }
       __stcs(st.S[0] + g, v);
       if (st.bulk_separate) st_bulk<TC>(st.Yb[0], g, v);
@@ -360,8 +373,7 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
         const float2 b = st.ls_first ? make_float2(__fmul_rn(-fdt, Dc.x), __fmul_rn(-fdt, Dc.y))
                                      : make_float2(fmaf(-fdt, Dc.x, -p.f.x), fmaf(-fdt, Dc.y, -p.f.y));
         __stcs(reinterpret_cast<float2*>(st.acc) + g, b);
-        const double2 v = make_double2(fma(st.coef, static_cast<double>(b.x), p.b.x),
-                                       fma(st.coef, static_cast<double>(b.y), p.b.y));
+        const double2 v = make_double2(fma(st.coef, f2d(b.x), p.b.x), fma(st.coef, f2d(b.y), p.b.y));
         __stcs(st.S[1 - st.ls_in] + g, v);
         if (st.bulk_separate) st_bulk<TC>(st.Yb[1 - st.ls_in], g, v);
       } else {
@@ -387,10 +399,9 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
           float2 hi = p.f, lo = p.g;
           ff_add_prod(hi.x, lo.x, c_dpBh[5], c_dpBl[5], k.x);
           ff_add_prod(hi.y, lo.y, c_dpBh[5], c_dpBl[5], k.y);
-          const double2 y = make_double2((p.a.x + static_cast<double>(hi.x)) + static_cast<double>(lo.x),
-                                         (p.a.y + static_cast<double>(hi.y)) + static_cast<double>(lo.y));
+          const double2 y = make_double2((p.a.x + f2d(hi.x)) + f2d(lo.x), (p.a.y + f2d(hi.y)) + f2d(lo.y));
           __stcs(st.S[1 - cur] + g, y);
-          static_cast<float2*>(st.Yb[1 - cur])[g] = make_float2(static_cast<float>(y.x), static_cast<float>(y.y));
+          static_cast<float2*>(st.Yb[1 - cur])[g] = make_float2(d2f(y.x), d2f(y.y));
         }
       } else {
         const double2 k = make_double2(-dt * D.x, -dt * D.y);
@@ -413,7 +424,7 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
         const float ex = fmaf(c, -fdt * Dc.x, p.f.x), ey = fmaf(c, -fdt * Dc.y, p.f.y);
         const float s = static_cast<float>(st.ctl->atol) +
                         static_cast<float>(st.ctl->rtol) * sqrtf(static_cast<float>(p.m));
-        return static_cast<double>((ex * ex + ey * ey) / (s * s));
+        return f2d((ex * ex + ey * ey) / (s * s));
       } else {
         const double2 k7 = make_double2(-dt * D.x, -dt * D.y);
         double2 e = p.a;
@@ -801,7 +812,7 @@ __device__ __forceinline__ double diag_tile(const DiagInst* __restrict__ I, cons
           const int k = __ldg(minus_mode + p);
           const int lm = m1row[k];
           if (lm != void_idx) {
-            const TC nk = sqn ? sqrt(static_cast<TC>(nrow[k])) : static_cast<TC>(nrow[k]);
+            const TC nk = sqn ? sqrt(static_cast<TC>(nrow[k])) : occ<TC>(nrow[k]);
             const C cm = cmi[p];
             v[4 + j] = ldc<TC>(yi + static_cast<size_t>(lm) * n2 + e);
             cf[4 + j] = cx<TC>(nk * cm.x, nk * cm.y);
@@ -1329,7 +1340,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
     for (int le = threadIdx.x; le < E; le += blockDim.x) {
       const double2 v = R.S[cur][gb + le];
       Sv[static_cast<size_t>(cur) * E + le] = v;
-      const float2 f = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+      const float2 f = make_float2(d2f(v.x), d2f(v.y));
       Yf[static_cast<size_t>(cur) * E + le] = f;
       yt[le] = f;
     }
@@ -1403,10 +1414,9 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
           ff_add_prod(hi.x, lo.x, c_dpBh[5], c_dpBl[5], k.x);
           ff_add_prod(hi.y, lo.y, c_dpBh[5], c_dpBl[5], k.y);
           const double2 sc = Sc[le];
-          const double2 y = make_double2((sc.x + static_cast<double>(hi.x)) + static_cast<double>(lo.x),
-                                         (sc.y + static_cast<double>(hi.y)) + static_cast<double>(lo.y));
+          const double2 y = make_double2((sc.x + f2d(hi.x)) + f2d(lo.x), (sc.y + f2d(hi.y)) + f2d(lo.y));
           Sn[le] = y;
-          const float2 yb = make_float2(static_cast<float>(y.x), static_cast<float>(y.y));
+          const float2 yb = make_float2(d2f(y.x), d2f(y.y));
           Yn[le] = yb;
           Xn[le] = yb;
           R.Yb[1 - cur][g] = yb;
@@ -1430,7 +1440,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
       if (s < 6) grid_arrive(R.bar);
     }
     if (!ok) break;
-    const double part = block_sum(static_cast<double>(local_f));
+    const double part = block_sum(f2d(local_f));
     if (threadIdx.x == 0) R.partials[blockIdx.x] = part;
     grid_arrive(R.bar);
     ok = grid_wait(R.bar, gen);
@@ -1482,7 +1492,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
   for (int le = threadIdx.x; le < E; le += blockDim.x) {
     const double2 v = R.S[0][gb + le];
     Sv[le] = v;
-    const float2 f = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+    const float2 f = make_float2(d2f(v.x), d2f(v.y));
     Yf[le] = f;
     yt[le] = f;
   }
@@ -1518,15 +1528,15 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
           Xn[le] = y;
           R.Ytmp[s & 1][g] = y;
           double2 a = s == 0 ? Sv[le] : Av[le];
-          a.x += static_cast<double>(__fmul_rn(w, k.x));
-          a.y += static_cast<double>(__fmul_rn(w, k.y));
+          a.x += f2d(__fmul_rn(w, k.x));
+          a.y += f2d(__fmul_rn(w, k.y));
           Av[le] = a;
         } else {  // rho = acc + k4/6
           const double2 a = Av[le];
-          const double2 v = make_double2(a.x + static_cast<double>(__fmul_rn(1.0f / 6.0f, k.x)),
-                                         a.y + static_cast<double>(__fmul_rn(1.0f / 6.0f, k.y)));
+          const double2 v = make_double2(a.x + f2d(__fmul_rn(1.0f / 6.0f, k.x)),
+                                         a.y + f2d(__fmul_rn(1.0f / 6.0f, k.y)));
           Sv[le] = v;
-          const float2 f = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+          const float2 f = make_float2(d2f(v.x), d2f(v.y));
           Yf[le] = f;
           Xn[le] = f;  // the next step's stage-1 input (yt[0])
           R.Yb[0][g] = f;
@@ -1566,7 +1576,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_ls_resident(const Resi
   for (int le = threadIdx.x; le < E; le += blockDim.x) {
     const double2 v = R.S[0][gb + le];
     Sv[le] = v;
-    Yf[le] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+    Yf[le] = make_float2(d2f(v.x), d2f(v.y));
   }
   __syncthreads();
   ResElems<EPT> el;
@@ -1598,10 +1608,9 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_ls_resident(const Resi
         }
         Bv[le] = b;
         const double2 sp = Sv[le];
-        const double2 v = make_double2(fma(B[s], static_cast<double>(b.x), sp.x),
-                                       fma(B[s], static_cast<double>(b.y), sp.y));
+        const double2 v = make_double2(fma(B[s], f2d(b.x), sp.x), fma(B[s], f2d(b.y), sp.y));
         Sv[le] = v;
-        const float2 f = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+        const float2 f = make_float2(d2f(v.x), d2f(v.y));
         Yf[le] = f;
         R.Yb[1 - (s & 1)][gb + le] = f;
       }
@@ -1659,6 +1668,231 @@ cudaError_t launch_resident(const ResidentArgs& args, int scheme, bool hreal, in
   ResidentArgs a = args;
   void* params[] = {&a};
   e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(block), params, smem, s);
+  ++g_launches;
+  return e;
+}
+
+// ------------------------------------------------------------------ instance-resident RK4 (batches)
+// The right-hand side D of one element (e of ADO lt), k_rhs_diag's arithmetic
+// in its order (commutator, damping, then the +1 and -1 terms in groups of
+// four), with every ADO read from the bin's shared-memory copy Xi of the
+// instance's stage input.  Slots without a term are skipped (k_rhs_diag adds
+// them as 0*0, which leaves D unchanged).
+template <typename TC>
+__device__ __forceinline__ cx_t<TC> local_rhs(const DiagInst& I, const cx_t<TC>* Hi, const cx_t<TC>* Xi, int lt,
+                                              int e) {
+  using C = cx_t<TC>;
+  const int n = I.n, n2 = I.n2, K = I.K, void_idx = I.nh;
+  const int a = e / n, b = e - a * n;
+  const C* yl = Xi + lt * n2;
+  C acc = cx<TC>(0, 0);  // [H, rho]
+  if (I.h_real) {
+#pragma unroll 4
+    for (int c = 0; c < n; ++c) {
+      const TC hac = Hi[a * n + c].x, hcb = Hi[c * n + b].x;
+      const C ycb = yl[c * n + b], yac = yl[a * n + c];
+      acc.x = fma(hac, ycb.x, acc.x);
+      acc.x = fma(-hcb, yac.x, acc.x);
+      acc.y = fma(hac, ycb.y, acc.y);
+      acc.y = fma(-hcb, yac.y, acc.y);
+    }
+  } else {
+    C neg = cx<TC>(0, 0);
+#pragma unroll 4
+    for (int c = 0; c < n; ++c) {
+      cfma(acc, Hi[a * n + c], yl[c * n + b]);
+      cfma(neg, yl[a * n + c], Hi[c * n + b]);
+    }
+    acc.x -= neg.x;
+    acc.y -= neg.y;
+  }
+  C D = cx<TC>(-acc.y, acc.x);
+  const C g0 = pick<TC>(I.ngd, I.ngd_f)[lt], g1 = pick<TC>(I.c_sd, I.c_sd_f)[e];
+  cfma(D, cx<TC>(g0.x + g1.x, g0.y + g1.y), yl[e]);
+  const bool sqn = I.sqrt_norm != 0;
+  const int* __restrict__ p1row = I.p1 + static_cast<size_t>(lt) * K;
+  const int* __restrict__ m1row = I.m1 + static_cast<size_t>(lt) * K;
+  const int* __restrict__ nrow = I.nidx + static_cast<size_t>(lt) * K;
+  const C* __restrict__ cpl = pick<TC>(I.c_plus, I.c_plus_f);
+  const C* __restrict__ cmi = pick<TC>(I.c_minus, I.c_minus_f);
+  const int pb = __ldg(I.plus_ptr + e), pe = __ldg(I.plus_ptr + e + 1);
+  const int mb = __ldg(I.minus_ptr + e), me = __ldg(I.minus_ptr + e + 1);
+  for (int pp = pb, mp = mb; pp < pe || mp < me; pp += 4, mp += 4) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int p = pp + j;
+      if (p < pe) {
+        const int k = __ldg(I.plus_mode + p);
+        const int lp = __ldg(p1row + k);
+        if (lp != void_idx) {
+          C cf = cpl[p];
+          if (sqn) {
+            const TC f = sqrt(static_cast<TC>(__ldg(nrow + k) + 1));
+            cf = cx<TC>(f * cf.x, f * cf.y);
+          }
+          cfma(D, cf, Xi[lp * n2 + e]);
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int p = mp + j;
+      if (p < me) {
+        const int k = __ldg(I.minus_mode + p);
+        const int lm = __ldg(m1row + k);
+        if (lm != void_idx) {
+          const int nk_i = __ldg(nrow + k);
+          const TC nk = sqn ? sqrt(static_cast<TC>(nk_i)) : occ<TC>(nk_i);
+          const C cm = cmi[p];
+          cfma(D, cx<TC>(nk * cm.x, nk * cm.y), Xi[lm * n2 + e]);
+        }
+      }
+    }
+  }
+  return D;
+}
+
+// A fixed-step RK4 interval (n_steps steps of dt_step, then one of dt_last)
+// of the instances of bin blockIdx.x, every stage separated by a CTA barrier
+// only: no instance's ADOs leave the CTA.  Shared memory holds H of every
+// instance, two stage-input copies (FP64 form: double2; mixed form: float2)
+// and a packed descriptor per element (instance slot in bits 0-7, element of
+// the ADO in bits 8-15, ADO in bits 16-31); the FP64 state, the RK4
+// accumulator and the state's FP32 copy (mixed form) are read and written in
+// global memory by the element's owning thread only.  Per element the
+// arithmetic is k_rhs_diag's with the RK4 epilogues (EPI_RK4_1..4) of the
+// form, in the same order, so both paths give the same bits.
+template <typename TC>
+__global__ void __launch_bounds__(512, 1) k_rk4_local(const LocalArgs A) {
+  using C = cx_t<TC>;
+  constexpr bool MIX = std::is_same<TC, float>::value;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ DiagInst s_inst[kLocalMaxInst];
+  __shared__ int s_ebase[kLocalMaxInst + 1], s_hbase[kLocalMaxInst + 1];
+  const int i0 = A.bin_ptr[blockIdx.x];
+  const int ni = min(kLocalMaxInst, A.bin_ptr[blockIdx.x + 1] - i0);
+  if (static_cast<int>(threadIdx.x) < ni) s_inst[threadIdx.x] = A.inst[A.bin_inst[i0 + threadIdx.x]];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int e = 0, h = 0;
+    for (int ii = 0; ii < ni; ++ii) {
+      s_ebase[ii] = e;
+      s_hbase[ii] = h;
+      e += s_inst[ii].nh * s_inst[ii].n2;
+      h += (s_inst[ii].n2 * static_cast<int>(sizeof(C)) + 15) / 16 * (16 / static_cast<int>(sizeof(C)));
+    }
+    s_ebase[ni] = e;
+    s_hbase[ni] = h;
+  }
+  __syncthreads();
+  const int E = s_ebase[ni];
+  C* Hs = reinterpret_cast<C*>(smem_raw);
+  C* X0 = Hs + s_hbase[ni];
+  C* X1 = X0 + E;
+  unsigned* desc = reinterpret_cast<unsigned*>(X1 + E);
+  for (int ii = 0; ii < ni; ++ii) {
+    const C* Hg = pick<TC>(s_inst[ii].H, s_inst[ii].H_f);
+    for (int i = threadIdx.x; i < s_inst[ii].n2; i += blockDim.x) Hs[s_hbase[ii] + i] = Hg[i];
+  }
+  for (int le = threadIdx.x; le < E; le += blockDim.x) {
+    int ii = 0;
+    while (s_ebase[ii + 1] <= le) ++ii;
+    const DiagInst& I = s_inst[ii];
+    const int loc = le - s_ebase[ii];
+    const int lt = loc / I.n2, e = loc - lt * I.n2;
+    desc[le] = static_cast<unsigned>(ii) | (static_cast<unsigned>(e) << 8) | (static_cast<unsigned>(lt) << 16);
+    const size_t g = static_cast<size_t>(I.elem_off) + loc;
+    if constexpr (MIX)
+      X0[le] = A.Yf[g];
+    else
+      X0[le] = A.S[g];
+  }
+  __syncthreads();
+  for (long long step = 0; step <= A.n_steps; ++step) {
+    const double dt = step < A.n_steps ? A.dt_step : A.dt_last;
+    for (int s = 0; s < 4; ++s) {
+      const C* Xs = (s & 1) ? X1 : X0;
+      C* Xn = (s & 1) ? X0 : X1;
+      for (int le = threadIdx.x; le < E; le += blockDim.x) {
+        const unsigned d = desc[le];
+        const int ii = static_cast<int>(d & 0xffu), e = static_cast<int>((d >> 8) & 0xffu),
+                  lt = static_cast<int>(d >> 16);
+        const DiagInst& I = s_inst[ii];
+        const size_t g = static_cast<size_t>(I.elem_off) + static_cast<size_t>(lt) * I.n2 + e;
+        // the epilogue's operands first, so their loads overlap the right-hand side
+        const double2 pa = s == 0 ? A.S[g] : A.acc[g];
+        if constexpr (MIX) {
+          const float2 pf = s < 3 ? A.Yf[g] : make_float2(0.f, 0.f);
+          const float2 D = local_rhs<TC>(I, Hs + s_hbase[ii], Xs + s_ebase[ii], lt, e);
+          const float fdt = static_cast<float>(dt);
+          const float2 k = make_float2(__fmul_rn(-fdt, D.x), __fmul_rn(-fdt, D.y));
+          if (s < 3) {  // rho_n = rho + c*k (FP32 from the state's copy); acc = rho + k/6 or acc += k/3
+            const float c = static_cast<float>(s == 2 ? 1.0 : 0.5);
+            const float w = static_cast<float>(s == 0 ? (1.0 / 6.0) : (2.0 / 6.0));
+            Xn[le] = make_float2(fmaf(c, k.x, pf.x), fmaf(c, k.y, pf.y));
+            double2 acc = pa;
+            acc.x += f2d(__fmul_rn(w, k.x));
+            acc.y += f2d(__fmul_rn(w, k.y));
+            A.acc[g] = acc;
+          } else {  // rho = acc + k4/6
+            const double2 v = make_double2(pa.x + f2d(__fmul_rn(1.0f / 6.0f, k.x)),
+                                           pa.y + f2d(__fmul_rn(1.0f / 6.0f, k.y)));
+            A.S[g] = v;
+            const float2 f = make_float2(d2f(v.x), d2f(v.y));
+            A.Yf[g] = f;
+            Xn[le] = f;
+          }
+        } else {
+          const double2 pb = (s == 1 || s == 2) ? A.S[g] : pa;
+          const double2 D = local_rhs<TC>(I, Hs + s_hbase[ii], Xs + s_ebase[ii], lt, e);
+          const double2 k = make_double2(-dt * D.x, -dt * D.y);
+          if (s < 3) {
+            const double c = s == 2 ? 1.0 : 0.5;
+            const double w = s == 0 ? (1.0 / 6.0) : (2.0 / 6.0);
+            Xn[le] = make_double2(fma(c, k.x, pb.x), fma(c, k.y, pb.y));
+            A.acc[g] = make_double2(fma(w, k.x, pa.x), fma(w, k.y, pa.y));
+          } else {
+            const double2 v = make_double2(fma(1.0 / 6.0, k.x, pa.x), fma(1.0 / 6.0, k.y, pa.y));
+            A.S[g] = v;
+            Xn[le] = v;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+size_t local_bin_smem(const int* n2, const int* nh, int count, bool mixed) {
+  const size_t c = mixed ? sizeof(float2) : sizeof(double2);
+  size_t h = 0, e = 0;
+  for (int i = 0; i < count; ++i) {
+    h += (static_cast<size_t>(n2[i]) * c + 15) / 16 * 16;
+    e += static_cast<size_t>(n2[i]) * nh[i];
+  }
+  return h + e * (2 * c + sizeof(unsigned));
+}
+
+static const void* local_kernel(bool mixed) {
+  return mixed ? reinterpret_cast<const void*>(k_rk4_local<float>) : reinterpret_cast<const void*>(k_rk4_local<double>);
+}
+
+int local_blocks_per_sm(bool mixed, int block, size_t smem) {
+  const void* kern = local_kernel(mixed);
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
+    return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, block, smem) != cudaSuccess) return 0;
+  return nb;
+}
+
+cudaError_t launch_local(const LocalArgs& args, bool mixed, int grid, int block, size_t smem, cudaStream_t s) {
+  const void* kern = local_kernel(mixed);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  LocalArgs a = args;
+  void* params[] = {&a};
+  e = cudaLaunchKernel(kern, dim3(grid), dim3(block), params, smem, s);
   ++g_launches;
   return e;
 }
@@ -2140,7 +2374,7 @@ __global__ void k_to_bulk(const double2* src, float2* dst, long long n) {
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * blockDim.x) {
     const double2 v = src[i];
-    dst[i] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+    dst[i] = make_float2(d2f(v.x), d2f(v.y));
   }
 }
 

@@ -327,10 +327,14 @@ class qme_solver:
         tc, rs, rg, ra = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         check(self._lib.heomgb_qme_solver_tensor_cores(self._h, ctypes.byref(tc)))
         check(self._lib.heomgb_qme_solver_resident(self._h, ctypes.byref(rs), ctypes.byref(rg), ctypes.byref(ra)))
+        lo, lb, lk = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(self._lib.heomgb_qme_solver_local(self._h, ctypes.byref(lo), ctypes.byref(lb), ctypes.byref(lk)))
         out = dict(block=b.value, elems_per_thread=e.value, n_tiles=t.value, min_blocks=m.value,
-                   tensor_cores=bool(tc.value), resident=bool(rs.value))
+                   tensor_cores=bool(tc.value), resident=bool(rs.value), local=bool(lo.value))
         if rs.value:
             out.update(resident_grid=rg.value, resident_ados_per_cta=ra.value)
+        if lo.value:
+            out.update(local_bins=lb.value, local_block=lk.value)
         return out
 
     def stats(self) -> dict:
@@ -432,6 +436,7 @@ class batch_solver:
             self._parts[0][0].solve(flat, t_list, callback, kwargs)
             return
         t = [float(x) for x in t_list]
+        self._counts = [dict(rhs=0, attempts=0, accepted=0) for _ in self._parts]
         with ThreadPoolExecutor(len(self._parts)) as pool:  # sub-batches run concurrently (own streams)
             for i in range(len(t) - 1):
                 if callback:
@@ -443,8 +448,16 @@ class batch_solver:
                     f.result()
                 for (_, _, ranges, _), sub in zip(self._parts, subs):
                     self._scatter(flat, ranges, sub)
+                self._count_interval()
         if callback and t:
             callback(t[-1])
+
+    def _count_interval(self):
+        # each sub-batch solve covers one interval: its counters restart every interval
+        for c, (part, _, _, _) in zip(self._counts, self._parts):
+            st = part.stats()
+            for k in c:
+                c[k] += st[k]
 
     def solve_device(self, rho_ptr: int, t_list, callback=None, kwargs=None) -> None:
         """rho_ptr: device pointer to the concatenated state (complex128)."""
@@ -455,6 +468,7 @@ class batch_solver:
             raise ValueError("sub-batches must be contiguous in the state for device solves; order the models "
                              "by effective precision")
         t = [float(x) for x in t_list]
+        self._counts = [dict(rhs=0, attempts=0, accepted=0) for _ in self._parts]
         with ThreadPoolExecutor(len(self._parts)) as pool:  # sub-batches run concurrently (own streams)
             for i in range(len(t) - 1):
                 if callback:
@@ -463,13 +477,15 @@ class batch_solver:
                                     kwargs) for part, _, ranges, _ in self._parts]
                 for f in futs:
                     f.result()
+                self._count_interval()
         if callback and t:
             callback(t[-1])
 
     def stats(self) -> dict:
         out = dict(rhs=0, attempts=0, accepted=0, ado_updates=0, dt_save=-1.0)
-        for part, idx, _, _ in self._parts:
-            st = part.stats()
+        counts = getattr(self, "_counts", None) if len(self._parts) > 1 else None
+        for j, (part, idx, _, _) in enumerate(self._parts):
+            st = counts[j] if counts else part.stats()
             nh = sum(self.qmes[i].get_n_hrchy() for i in idx)
             out["rhs"] = max(out["rhs"], st["rhs"])
             out["attempts"] = max(out["attempts"], st["attempts"])

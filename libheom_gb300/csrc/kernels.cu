@@ -1763,7 +1763,7 @@ __device__ __forceinline__ cx_t<TC> local_rhs(const DiagInst& I, const cx_t<TC>*
 // arithmetic is k_rhs_diag's with the RK4 epilogues (EPI_RK4_1..4) of the
 // form, in the same order, so both paths give the same bits.
 template <typename TC>
-__global__ void __launch_bounds__(512, 1) k_rk4_local(const LocalArgs A) {
+__global__ void __launch_bounds__(512, 2) k_rk4_local(const LocalArgs A) {
   using C = cx_t<TC>;
   constexpr bool MIX = std::is_same<TC, float>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];

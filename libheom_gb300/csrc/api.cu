@@ -373,7 +373,8 @@ struct heomgb_qme_solver {
   DeviceArena loc_arena;
   const int* loc_bin_ptr = nullptr;
   const int* loc_bin_inst = nullptr;
-  float stage_ms = 0.f;  // the autotuned stage kernel's time per launch (0: not timed)
+  float stage_ms = 0.f;     // the autotuned stage kernel's time per launch (0: not timed)
+  float res_step_ms = 0.f;  // the resident fixed-step plan's time per step (0: not timed)
   // batch solvers run on a stream of their own (sub-batches of one batch run
   // concurrently), ordered after the model stream's pending work at each solve
   cudaStream_t own_stream = nullptr;
@@ -1266,7 +1267,7 @@ void plan_resident(heomgb_qme_solver* qs) {
         ck(launch_ctl_init(qs->ctl, 0.0, 1e-3, 1e-3, 1e-8, 1e-8, 0, qs->stream), "ctl init");
         ck(cudaMemsetAsync(qs->res_bar, 0, kResidentBarWords * sizeof(unsigned long long), qs->stream), "memset");
         ResidentArgs a = resident_args(qs);
-        a.n_steps = 0;
+        a.n_steps = scheme == kResidentDp ? 0 : 3;  // fixed steps: four, as the instance-resident plan times
         a.dt_step = a.dt_last = 1e-3;
         ck(cudaEventRecord(e0, qs->stream), "event");
         ck(launch_resident(a, scheme, hreal, qs->res_ept, qs->res_grid, qs->res_block, qs->res_smem, qs->stream),
@@ -1287,6 +1288,7 @@ void plan_resident(heomgb_qme_solver* qs) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    qs->res_step_ms = scheme == kResidentDp ? 0.f : best_ms / 4.f;
   }
   qs->res_grid = shapes[best].grid;
   qs->res_apc = shapes[best].apc;
@@ -1297,19 +1299,21 @@ void plan_resident(heomgb_qme_solver* qs) {
 }
 
 // Instance-resident RK4 intervals (k_rk4_local) apply to fixed-step RK4 on the
-// diagonal-coupling path without a terminator, when no cooperative resident
-// interval was planned and every instance fits one CTA's shared memory.
-// Instances are packed into bins (largest first, each into the least-loaded
-// bin with room: at most kLocalMaxInst instances and the shared-memory cap),
-// for 1, 2 or 4 bins per SM and 128, 256 or 512 threads per CTA; every shape runs
-// four steps over the solver's zeroed buffers, the fastest is kept, and it
-// replaces the graphs of stage kernels only where it beats four launches of
-// the autotuned stage kernel.  HEOMGB_LOCAL=0 keeps the stage kernels,
-// HEOMGB_LOCAL=1 takes the fastest shape without the comparison.
+// diagonal-coupling path without a terminator when every instance fits one
+// CTA's shared memory.  Instances are packed into bins (largest first, each
+// into the least-loaded bin with room: at most kLocalMaxInst instances and
+// the shared-memory cap), for 1, 2 or 4 bins per SM and 128, 256 or 512
+// threads per CTA; every shape runs four steps over the solver's zeroed
+// buffers and the fastest is kept.  It replaces the cooperative resident
+// plan (timed the same way) or, without one, the graphs of stage kernels
+// (four launches of the autotuned stage kernel) only where it is faster.
+// HEOMGB_LOCAL=0 keeps the other paths, HEOMGB_LOCAL=1 takes the fastest
+// shape without the comparison.
 void plan_local(heomgb_qme_solver* qs) {
   heomgb_qme* q = qs->q;
   qs->local = false;
-  if (qs->kind != HEOMGB_RK4 || q->path != PATH_DIAG || qs->term || qs->resident || qs->plan.tcore) return;
+  if (qs->kind != HEOMGB_RK4 || q->path != PATH_DIAG || qs->term || qs->plan.tcore) return;
+  if (qs->resident && qs->res_step_ms <= 0.f) return;  // an untimed (pinned) resident plan stays
   bool force = false;
   if (const char* env = std::getenv("HEOMGB_LOCAL")) {
     if (std::string(env) == "0") return;
@@ -1419,7 +1423,10 @@ void plan_local(heomgb_qme_solver* qs) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (!force && !(best_ms / 4.f < 4.f * qs->stage_ms)) return;
+  // against the cooperative resident plan where there is one, else the stage kernels
+  const float rival = qs->resident ? qs->res_step_ms : 4.f * qs->stage_ms;
+  if (!force && !(best_ms / 4.f < rival)) return;
+  qs->resident = false;
   const Shape& sh = shapes[best];
   qs->loc_arena.release();
   qs->loc_bin_ptr = qs->loc_arena.upload(sh.ptr, qs->stream);

@@ -122,6 +122,7 @@ def test_resident_fixed_step_bit_identical(maker, ept, solver, monkeypatch):
     def go(resident):
         monkeypatch.setenv("HEOMGB_RESIDENT", "1" if resident else "0")
         monkeypatch.setenv("HEOMGB_RESIDENT_EPT", ept)
+        monkeypatch.setenv("HEOMGB_LOCAL", "0")  # the cooperative kernel under test, not the one-CTA plan
         q = lh.from_params(p, precision="mixed")
         qs = lh.qme_solver(q, lh.SOLVERS[solver]())
         rho = p.rho0_ground()

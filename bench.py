@@ -414,7 +414,7 @@ def run_ours(args):
             " (one cooperative launch per output interval: fused RHS and stage epilogues"
             + (", error norm and step control" if wl["solver"] == "rkdp" else "") + "; state in shared memory)")
     elif local:
-        kernel = ("k_rk4_local (one launch per output interval; every instance inside one CTA with its stage "
+        kernel = ("k_fixed_local (one launch per output interval; every instance inside one CTA with its stage "
                   "inputs in shared memory, no grid-wide synchronisation)"
                   + ("" if all(t.get("local", False) for t in part_tunings) else "; k_rhs_diag for the other part"))
     else:

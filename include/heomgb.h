@@ -212,13 +212,14 @@ heomgb_status heomgb_qme_solver_tensor_cores(const heomgb_qme_solver* qs, int* o
  * (rk4.h:40-65) and lsrk4::solve_fixed_step (lsrk4.h:32-47) issue every
  * stage's BLAS calls from the host. */
 heomgb_status heomgb_qme_solver_resident(const heomgb_qme_solver* qs, int* on, int* grid, int* ados_per_cta);
-/* 1 when the solver runs each fixed-step RK4 output interval as one launch of
+/* 1 when the solver runs each fixed-step (rk4, lsrk4) output interval as one launch of
  * instance-resident bins (diagonal-coupling path, every instance inside one
  * CTA: its stage inputs in shared memory, no grid-wide synchronisation), else
  * 0; bins and block (may be NULL) receive the CTAs and their threads.  Chosen
  * where it beats the per-stage kernels; HEOMGB_LOCAL=0 keeps them,
  * HEOMGB_LOCAL=1 takes it wherever it applies.  No reference counterpart:
- * rk4::solve_fixed_step (rk4.h:40-65) steps one model at a time. */
+ * rk4::solve_fixed_step (rk4.h:40-65) and lsrk4::solve_fixed_step
+ * (lsrk4.h:32-47) step one model at a time. */
 heomgb_status heomgb_qme_solver_local(const heomgb_qme_solver* qs, int* on, int* bins, int* block);
 
 /* qme_solver::solve(rho, t_list, n_t, callback, kwargs) -- qme_solver.h:44-52,

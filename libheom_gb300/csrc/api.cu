@@ -365,7 +365,7 @@ struct heomgb_qme_solver {
   size_t res_smem = 0;
   unsigned long long* res_bar = nullptr;
   double* res_partials = nullptr;
-  // instance-resident RK4 intervals of a batch (k_rk4_local): one launch per
+  // instance-resident fixed-step intervals of a batch (k_fixed_local): one launch per
   // output interval, bins of whole instances per CTA, no grid barrier
   bool local = false;
   int loc_grid = 0, loc_block = 0;
@@ -1298,8 +1298,8 @@ void plan_resident(heomgb_qme_solver* qs) {
   qs->resident = true;
 }
 
-// Instance-resident RK4 intervals (k_rk4_local) apply to fixed-step RK4 on the
-// diagonal-coupling path without a terminator when every instance fits one
+// Instance-resident fixed-step intervals (k_fixed_local) apply to RK4 and
+// LSRK4 on the diagonal-coupling path without a terminator when every instance fits one
 // CTA's shared memory.  Instances are packed into bins (largest first, each
 // into the least-loaded bin with room: at most kLocalMaxInst instances and
 // the shared-memory cap), for 1, 2 or 4 bins per SM and 128, 256 or 512
@@ -1312,7 +1312,9 @@ void plan_resident(heomgb_qme_solver* qs) {
 void plan_local(heomgb_qme_solver* qs) {
   heomgb_qme* q = qs->q;
   qs->local = false;
-  if (qs->kind != HEOMGB_RK4 || q->path != PATH_DIAG || qs->term || qs->plan.tcore) return;
+  if ((qs->kind != HEOMGB_RK4 && qs->kind != HEOMGB_LSRK4) || q->path != PATH_DIAG || qs->term || qs->plan.tcore)
+    return;
+  const int scheme = resident_scheme(qs);
   if (qs->resident && qs->res_step_ms <= 0.f) return;  // an untimed (pinned) resident plan stays
   bool force = false;
   if (const char* env = std::getenv("HEOMGB_LOCAL")) {
@@ -1380,7 +1382,7 @@ void plan_local(heomgb_qme_solver* qs) {
     }
     sh.grid = static_cast<int>(sh.ptr.size()) - 1;
     for (int block : {128, 256, 512}) {
-      if (local_blocks_per_sm(mixed, block, sh.smem) < 1) continue;
+      if (local_blocks_per_sm(mixed, scheme, block, sh.smem) < 1) continue;
       sh.block = block;
       shapes.push_back(sh);
     }
@@ -1409,7 +1411,7 @@ void plan_local(heomgb_qme_solver* qs) {
     float ms_i = 1e30f;
     for (int r = 0; r < 4; ++r) {  // one warm-up, best of three
       ck(cudaEventRecord(e0, qs->stream), "event");
-      ck(launch_local(a, mixed, shapes[i].grid, shapes[i].block, shapes[i].smem, qs->stream), "local tune");
+      ck(launch_local(a, mixed, scheme, shapes[i].grid, shapes[i].block, shapes[i].smem, qs->stream), "local tune");
       ck(cudaEventRecord(e1, qs->stream), "event");
       ck(cudaEventSynchronize(e1), "event sync");
       float ms = 0.f;
@@ -1599,7 +1601,7 @@ void solve_fixed(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwarg
     t += d;
     if (++m > cap) throw numeric_error("fixed-step loop does not terminate");
   }
-  if (qs->local) {  // the whole interval as one launch of instance-resident bins (k_rk4_local)
+  if (qs->local) {  // the whole interval as one launch of instance-resident bins (k_fixed_local)
     LocalArgs a{};
     a.inst = qs->plan.ds.inst;
     a.bin_ptr = qs->loc_bin_ptr;
@@ -1611,7 +1613,8 @@ void solve_fixed(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwarg
     a.dt_step = dt;
     a.dt_last = last;
     busy_begin(qs);
-    ck(launch_local(a, qs->mixed, qs->loc_grid, qs->loc_block, qs->loc_smem, qs->stream), "instance-resident interval");
+    ck(launch_local(a, qs->mixed, resident_scheme(qs), qs->loc_grid, qs->loc_block, qs->loc_smem, qs->stream),
+       "instance-resident interval");
     busy_end(qs);
     qs->replayed_kernels += 1;
     qs->n_rhs += 4 * (m + 1);

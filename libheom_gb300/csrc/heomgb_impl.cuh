@@ -194,12 +194,13 @@ int resident_blocks_per_sm(int scheme, bool hreal, int ept, int block, size_t sm
 cudaError_t launch_resident(const ResidentArgs& args, int scheme, bool hreal, int ept, int grid, int block,
                             size_t smem, cudaStream_t s);
 
-// Instance-resident fixed-step RK4 intervals of a batch (k_rk4_local): CTA b
+// Instance-resident fixed-step RK4 / LSRK4 intervals of a batch (k_fixed_local): CTA b
 // holds the whole instances of bin b and runs every step of the interval with
 // no grid barrier (its instances' neighbour gathers never leave the CTA): the
 // two stage-input copies live in its shared memory, the FP64 state, the RK4
 // accumulator and (mixed form) the state's FP32 copy stay in global memory,
-// each element touched only by the thread that owns it.
+// each element touched only by the thread that owns it.  The scheme is
+// kResidentRk4 or kResidentLs (the resident kernels' scheme numbers).
 constexpr int kLocalMaxInst = 32;   // instances per bin
 constexpr int kLocalMaxN2 = 256;    // n_state <= 16 (an element index packs into 8 bits)
 constexpr int kLocalMaxAdo = 65535; // ADOs per instance (16 bits)
@@ -208,7 +209,7 @@ struct LocalArgs {
   const int* bin_ptr;       // bin b holds instances bin_inst[bin_ptr[b] .. bin_ptr[b+1])
   const int* bin_inst;
   double2* S;               // FP64 state (updated in place every step)
-  double2* acc;             // RK4 accumulator
+  double2* acc;             // RK4 accumulator / LSRK4 buffer (mixed: FP32, the first half)
   float2* Yf;               // mixed form: the state's FP32 copy (the stage-1 input); null in FP64 form
   long long n_steps;        // steps of dt_step before the last step of dt_last
   double dt_step, dt_last;
@@ -216,8 +217,9 @@ struct LocalArgs {
 // shared memory of a bin: H of every instance (16-byte rounded), two
 // stage-input copies and one packed element descriptor per element
 size_t local_bin_smem(const int* n2, const int* nh, int count, bool mixed);
-int local_blocks_per_sm(bool mixed, int block, size_t smem);
-cudaError_t launch_local(const LocalArgs& args, bool mixed, int grid, int block, size_t smem, cudaStream_t s);
+int local_blocks_per_sm(bool mixed, int scheme, int block, size_t smem);
+cudaError_t launch_local(const LocalArgs& args, bool mixed, int scheme, int grid, int block, size_t smem,
+                         cudaStream_t s);
 
 // Launchers (kernels.cu).  `mixed` selects FP32 bulk arithmetic; `in_double`
 // says the RHS input is a double2 array even in mixed mode.  `ds` describes

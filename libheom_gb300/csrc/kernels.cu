@@ -343,7 +343,7 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
         a.x += f2d(__fmul_rn(static_cast<float>(w), k.x));
         a.y += f2d(__fmul_rn(static_cast<float>(w), k.y));
       } else {
-        // explicit FMAs, shared with k_rk4_local
+        // explicit FMAs, shared with k_fixed_local
         const double2 k = make_double2(-dt * D.x, -dt * D.y);
         st_bulk<TC>(st.Ynext, g, make_double2(fma(c, k.x, p.b.x), fma(c, k.y, p.b.y)));
         a.x = fma(w, k.x, a.x);
@@ -380,7 +380,7 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
         const double2 k = make_double2(-dt * D.x, -dt * D.y);
         const double2 b = st.ls_first ? k : make_double2(-p.a.x + k.x, -p.a.y + k.y);
         __stcs(st.acc + g, b);
-        const double2 v = make_double2(p.b.x + st.coef * b.x, p.b.y + st.coef * b.y);
+        const double2 v = make_double2(fma(st.coef, b.x, p.b.x), fma(st.coef, b.y, p.b.y));  // as k_fixed_local
         __stcs(st.S[1 - st.ls_in] + g, v);
         if (st.bulk_separate) st_bulk<TC>(st.Yb[1 - st.ls_in], g, v);
       }
@@ -1672,7 +1672,7 @@ cudaError_t launch_resident(const ResidentArgs& args, int scheme, bool hreal, in
   return e;
 }
 
-// ------------------------------------------------------------------ instance-resident RK4 (batches)
+// ------------------------------------------------------------------ instance-resident fixed steps (batches)
 // The right-hand side D of one element (e of ADO lt), k_rhs_diag's arithmetic
 // in its order (commutator, damping, then the +1 and -1 terms in groups of
 // four), with every ADO read from the bin's shared-memory copy Xi of the
@@ -1752,18 +1752,19 @@ __device__ __forceinline__ cx_t<TC> local_rhs(const DiagInst& I, const cx_t<TC>*
   return D;
 }
 
-// A fixed-step RK4 interval (n_steps steps of dt_step, then one of dt_last)
-// of the instances of bin blockIdx.x, every stage separated by a CTA barrier
-// only: no instance's ADOs leave the CTA.  Shared memory holds H of every
-// instance, two stage-input copies (FP64 form: double2; mixed form: float2)
-// and a packed descriptor per element (instance slot in bits 0-7, element of
-// the ADO in bits 8-15, ADO in bits 16-31); the FP64 state, the RK4
-// accumulator and the state's FP32 copy (mixed form) are read and written in
-// global memory by the element's owning thread only.  Per element the
-// arithmetic is k_rhs_diag's with the RK4 epilogues (EPI_RK4_1..4) of the
-// form, in the same order, so both paths give the same bits.
-template <typename TC>
-__global__ void __launch_bounds__(512, 2) k_rk4_local(const LocalArgs A) {
+// A fixed-step interval (n_steps steps of dt_step, then one of dt_last) of
+// the instances of bin blockIdx.x, RK4 or LSRK4 (SCHEME), every stage
+// separated by a CTA barrier only: no instance's ADOs leave the CTA.  Shared
+// memory holds H of every instance, two stage-input copies (FP64 form:
+// double2; mixed form: float2) and a packed descriptor per element (instance
+// slot in bits 0-7, element of the ADO in bits 8-15, ADO in bits 16-31); the
+// FP64 state (updated in place), the RK4 accumulator or LSRK4 buffer and the
+// state's FP32 copy (mixed form) are read and written in global memory by the
+// element's owning thread only.  Per element the arithmetic is k_rhs_diag's
+// with the form's RK4 (EPI_RK4_1..4) or LSRK4 (EPI_LS) epilogues, in the same
+// order, so both paths give the same bits.
+template <typename TC, int SCHEME>
+__global__ void __launch_bounds__(512, 2) k_fixed_local(const LocalArgs A) {
   using C = cx_t<TC>;
   constexpr bool MIX = std::is_same<TC, float>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1819,6 +1820,34 @@ __global__ void __launch_bounds__(512, 2) k_rk4_local(const LocalArgs A) {
                   lt = static_cast<int>(d >> 16);
         const DiagInst& I = s_inst[ii];
         const size_t g = static_cast<size_t>(I.elem_off) + static_cast<size_t>(lt) * I.n2 + e;
+        if constexpr (SCHEME == kResidentLs) {  // buff = -buff + k (or k); rho += B_s buff (lsrk4.h:32-47)
+          const double Bs = s == 0 ? 1.0 / 3.0 : s == 1 ? 3.0 / 4.0 : s == 2 ? 2.0 / 3.0 : 1.0 / 4.0;
+          const double2 pb = A.S[g];
+          if constexpr (MIX) {  // FP32 buffer (the first half of the buffer allocation), FP64 state
+            float2* buf = reinterpret_cast<float2*>(A.acc);
+            const float2 pf = s == 0 ? make_float2(0.f, 0.f) : buf[g];
+            const float2 D = local_rhs<TC>(I, Hs + s_hbase[ii], Xs + s_ebase[ii], lt, e);
+            const float fdt = static_cast<float>(dt);
+            const float2 b = s == 0 ? make_float2(__fmul_rn(-fdt, D.x), __fmul_rn(-fdt, D.y))
+                                    : make_float2(fmaf(-fdt, D.x, -pf.x), fmaf(-fdt, D.y, -pf.y));
+            buf[g] = b;
+            const double2 v = make_double2(fma(Bs, f2d(b.x), pb.x), fma(Bs, f2d(b.y), pb.y));
+            A.S[g] = v;
+            const float2 f = make_float2(d2f(v.x), d2f(v.y));
+            A.Yf[g] = f;
+            Xn[le] = f;
+          } else {
+            const double2 pa = s == 0 ? make_double2(0.0, 0.0) : A.acc[g];
+            const double2 D = local_rhs<TC>(I, Hs + s_hbase[ii], Xs + s_ebase[ii], lt, e);
+            const double2 k = make_double2(-dt * D.x, -dt * D.y);
+            const double2 b = s == 0 ? k : make_double2(-pa.x + k.x, -pa.y + k.y);
+            A.acc[g] = b;
+            const double2 v = make_double2(fma(Bs, b.x, pb.x), fma(Bs, b.y, pb.y));
+            A.S[g] = v;
+            Xn[le] = v;
+          }
+          continue;
+        }
         // the epilogue's operands first, so their loads overlap the right-hand side
         const double2 pa = s == 0 ? A.S[g] : A.acc[g];
         if constexpr (MIX) {
@@ -1873,12 +1902,16 @@ size_t local_bin_smem(const int* n2, const int* nh, int count, bool mixed) {
   return h + e * (2 * c + sizeof(unsigned));
 }
 
-static const void* local_kernel(bool mixed) {
-  return mixed ? reinterpret_cast<const void*>(k_rk4_local<float>) : reinterpret_cast<const void*>(k_rk4_local<double>);
+static const void* local_kernel(bool mixed, int scheme) {
+  if (scheme == kResidentLs)
+    return mixed ? reinterpret_cast<const void*>(k_fixed_local<float, kResidentLs>)
+                 : reinterpret_cast<const void*>(k_fixed_local<double, kResidentLs>);
+  return mixed ? reinterpret_cast<const void*>(k_fixed_local<float, kResidentRk4>)
+               : reinterpret_cast<const void*>(k_fixed_local<double, kResidentRk4>);
 }
 
-int local_blocks_per_sm(bool mixed, int block, size_t smem) {
-  const void* kern = local_kernel(mixed);
+int local_blocks_per_sm(bool mixed, int scheme, int block, size_t smem) {
+  const void* kern = local_kernel(mixed, scheme);
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
     return 0;
   int nb = 0;
@@ -1886,8 +1919,9 @@ int local_blocks_per_sm(bool mixed, int block, size_t smem) {
   return nb;
 }
 
-cudaError_t launch_local(const LocalArgs& args, bool mixed, int grid, int block, size_t smem, cudaStream_t s) {
-  const void* kern = local_kernel(mixed);
+cudaError_t launch_local(const LocalArgs& args, bool mixed, int scheme, int grid, int block, size_t smem,
+                         cudaStream_t s) {
+  const void* kern = local_kernel(mixed, scheme);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return e;
   LocalArgs a = args;

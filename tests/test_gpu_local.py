@@ -1,4 +1,4 @@
-"""Instance-resident RK4 intervals (k_rk4_local: every instance of a batch
+"""Instance-resident fixed-step intervals (k_fixed_local: every instance of a batch
 inside one CTA, its stage inputs in shared memory, one launch per output
 interval with no grid-wide synchronisation) against the per-stage kernels on
 the same batches.  The per-element arithmetic is the stage kernels', in the
@@ -28,21 +28,22 @@ def parts(tune):
     return tune["parts"] if "parts" in tune else [tune]
 
 
-def go(ps, precision, local, monkeypatch, t=T):
+def go(ps, precision, local, monkeypatch, t=T, solver="rk4"):
     monkeypatch.setenv("HEOMGB_LOCAL", "1" if local else "0")
     qmes = [lh.from_params(p, precision=precision) for p in ps]
-    bs = lh.batch_solver(qmes, lh.rk4())
+    bs = lh.batch_solver(qmes, lh.SOLVERS[solver]())
     rho = np.concatenate([p.rho0_ground().ravel() for p in ps])
     bs.solve(rho, list(t), None, {"dt": DT})
     monkeypatch.delenv("HEOMGB_LOCAL")
     return rho, bs
 
 
+@pytest.mark.parametrize("solver", ["rk4", "lsrk4"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_local_bit_identical_to_stage_kernels(precision, monkeypatch):
+def test_local_bit_identical_to_stage_kernels(precision, solver, monkeypatch):
     ps = instances()
-    loc, bs_l = go(ps, precision, True, monkeypatch)
-    stg, bs_s = go(ps, precision, False, monkeypatch)
+    loc, bs_l = go(ps, precision, True, monkeypatch, solver=solver)
+    stg, bs_s = go(ps, precision, False, monkeypatch, solver=solver)
     assert all(p["local"] and p["local_bins"] >= 1 for p in parts(bs_l.tuning()))
     assert not any(p["local"] for p in parts(bs_s.tuning()))
     assert bs_l.stats()["rhs"] == bs_s.stats()["rhs"] == 4 * 61
@@ -103,8 +104,8 @@ def test_local_single_model(monkeypatch):
     assert np.array_equal(loc, stg)
 
 
-def test_local_not_for_other_solvers(monkeypatch):
+def test_local_not_for_adaptive_steps(monkeypatch):
     monkeypatch.setenv("HEOMGB_LOCAL", "1")
-    ps = instances(3, 1)
-    bs = lh.batch_solver([lh.from_params(p) for p in ps], lh.lsrk4())
-    assert not any(p["local"] for p in parts(bs.tuning()))
+    p = configs.spin_boson(depth=6)
+    qs = lh.qme_solver(lh.from_params(p, precision="fp64"), lh.rkdp())
+    assert not qs.tuning()["local"]

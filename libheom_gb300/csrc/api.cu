@@ -817,6 +817,12 @@ void build_model(heomgb_qme* q) {
     di.c_minus_f = m.c_minus_f;
     di.c_sd = m.c_sd;
     di.c_sd_f = m.c_sd_f;
+    int* plus_any = static_cast<int*>(q->arena.alloc(sizeof(int) * std::max(nh, 1)));
+    if (K > 0)
+      ck(launch_plus_any(K, nh, m.p1, plus_any, s), "plus_any");
+    else
+      ck(cudaMemsetAsync(plus_any, 0, sizeof(int) * std::max(nh, 1), s), "memset");
+    di.plus_any = plus_any;
     build_plan(q->diff_plan, {di}, 128, 4, 1, q->precision_eff == HEOMGB_MIXED, q->n_sm, s);
   } else if (q->path == PATH_GENERAL) {
     if (rhs_smem_bytes(m, PATH_GENERAL, false) > 200 * 1024)

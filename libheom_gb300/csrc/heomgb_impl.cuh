@@ -149,6 +149,7 @@ struct DiagInst {
   int sqrt_norm;            // 1: +1 terms scale by sqrt(n_k+1), -1 terms by sqrt(n_k) (else 1 and n_k)
   int h_sym;                // H real and symmetric (the tensor-core commutator's condition)
   int max_terms;            // max over elements of max(+1 terms, -1 terms)
+  const int* plus_any;      // per ADO: 1 if any ptr_p1 entry is a real ADO (0 on the deepest tier)
 };
 struct DiagTile {
   int inst, l0, nt, pad;
@@ -240,6 +241,7 @@ cudaError_t launch_hrchy_build(int K, int depth, int n_hrchy, const long long* b
 cudaError_t launch_ngd(int K, int n_hrchy, const int* nidx, const double2* gdiag, double2* ngd, float2* ngd_f,
                        cudaStream_t s);
 cudaError_t launch_to_bulk(const double2* src, float2* dst, long long n, cudaStream_t s);
+cudaError_t launch_plus_any(int K, int n_hrchy, const int* p1, int* out, cudaStream_t s);
 cudaError_t launch_transpose_ados(const double2* in, double2* out, int n, long long count, cudaStream_t s);
 cudaError_t launch_ctl_init(DpCtl* c, double t, double dt, double t_bound, double atol, double rtol, int cur,
                             cudaStream_t s);

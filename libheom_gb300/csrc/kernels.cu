@@ -777,7 +777,10 @@ __device__ __forceinline__ double diag_tile(const DiagInst* __restrict__ I, cons
     const int* p1row = p1s + lt * K;
     const int* m1row = m1s + lt * K;
     const int* nrow = nks + lt * K;
-    const int pb = __ldg(plus_ptr + e), pe = __ldg(plus_ptr + e + 1);
+    // an ADO without +1 neighbours (the deepest tier) skips its +1 slots
+    // (they would add 0 * 0) unless the terminator stands in for them
+    const bool plus_on = term_p != nullptr || __ldg(I->plus_any + l0 + lt) != 0;
+    const int pb = __ldg(plus_ptr + e), pe = plus_on ? __ldg(plus_ptr + e + 1) : pb;
     const int mb = __ldg(minus_ptr + e), me = __ldg(minus_ptr + e + 1);
     for (int pp = pb, mp = mb; pp < pe || mp < me; pp += 4, mp += 4) {
       C v[8], cf[8];
@@ -819,8 +822,12 @@ __device__ __forceinline__ double diag_tile(const DiagInst* __restrict__ I, cons
           }
         }
       }
+      if (plus_on) {
 #pragma unroll
-      for (int j = 0; j < 8; ++j) cfma(D, cf[j], v[j]);
+        for (int j = 0; j < 4; ++j) cfma(D, cf[j], v[j]);
+      }
+#pragma unroll
+      for (int j = 4; j < 8; ++j) cfma(D, cf[j], v[j]);
     }
     local += epi_post<TC>(st, static_cast<size_t>(base + static_cast<long long>(l0) * n2 + i), D, dt, cur, pre);
   };
@@ -2400,6 +2407,22 @@ __global__ void k_ngd(int K, int n_hrchy, const int* nidx, const double2* gdiag,
 cudaError_t launch_ngd(int K, int n_hrchy, const int* nidx, const double2* gdiag, double2* ngd, float2* ngd_f,
                        cudaStream_t s) {
   k_ngd<<<(n_hrchy + 127) / 128, 128, 0, s>>>(K, n_hrchy, nidx, gdiag, ngd, ngd_f);
+  ++g_launches;
+  return cudaGetLastError();
+}
+
+// plus_any[l] = 1 if ADO l has any +1 neighbour (ptr_p1 not the sentinel)
+__global__ void k_plus_any(int K, int n_hrchy, const int* p1, int* out) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= n_hrchy) return;
+  int any = 0;
+  for (int k = 0; k < K; ++k) any |= p1[static_cast<size_t>(l) * K + k] != n_hrchy;
+  out[l] = any;
+}
+
+cudaError_t launch_plus_any(int K, int n_hrchy, const int* p1, int* out, cudaStream_t s) {
+  if (n_hrchy <= 0) return cudaSuccess;
+  k_plus_any<<<(n_hrchy + 127) / 128, 128, 0, s>>>(K, n_hrchy, p1, out);
   ++g_launches;
   return cudaGetLastError();
 }

@@ -66,50 +66,63 @@ HEOMGB_HD int fc_msb(uint32_t v) {
 #endif
 }
 
-// float -> double (exact)
-HEOMGB_HD double f2d(float x) {
-  const uint32_t u = fc_f2u(x);
+#if defined(__CUDA_ARCH__)
+#define HEOMGB_COLD static __device__ __noinline__
+#else
+#define HEOMGB_COLD static inline
+#endif
+
+// float -> double (exact).  The common case (a normal float) is a few integer
+// operations; zeros, subnormals, infinities and NaNs take a separate call so
+// that the compiler does not predicate their paths into every conversion.
+HEOMGB_COLD uint64_t f2d_rare(uint32_t u) {
   const uint64_t sign = static_cast<uint64_t>(u >> 31) << 63;
   const uint32_t ex = (u >> 23) & 0xffu, man = u & 0x7fffffu;
-  uint64_t bits;
-  if (ex != 0 && ex != 0xffu) {  // normal: rebias the exponent (1023 - 127), widen the fraction
-    bits = sign | (static_cast<uint64_t>(ex + 896u) << 52) | (static_cast<uint64_t>(man) << 29);
-  } else if (ex == 0xffu) {  // infinity or NaN (quiet bit stays the top fraction bit)
-    bits = sign | (0x7ffull << 52) | (static_cast<uint64_t>(man) << 29);
-  } else if (man == 0) {  // signed zero
-    bits = sign;
-  } else {  // subnormal: man * 2^-149 with its leading bit at position p
-    const int p = fc_msb(man);
-    bits = sign | (static_cast<uint64_t>(p + 874) << 52) |
-           ((static_cast<uint64_t>(man) << (52 - p)) & ((1ull << 52) - 1));
-  }
-  return fc_u2d(bits);
+  if (ex == 0xffu) return sign | (0x7ffull << 52) | (static_cast<uint64_t>(man) << 29);  // infinity or NaN
+  if (man == 0) return sign;                                                           // signed zero
+  const int p = fc_msb(man);  // subnormal: man * 2^-149 with its leading bit at position p
+  return sign | (static_cast<uint64_t>(p + 874) << 52) | ((static_cast<uint64_t>(man) << (52 - p)) & ((1ull << 52) - 1));
+}
+HEOMGB_HD double f2d(float x) {
+  const uint32_t u = fc_f2u(x);
+  const uint32_t ex = (u >> 23) & 0xffu;
+  if (ex - 1u < 0xfeu)  // normal: rebias the exponent (1023 - 127), widen the fraction
+    return fc_u2d((static_cast<uint64_t>(u >> 31) << 63) | (static_cast<uint64_t>(ex + 896u) << 52) |
+                  (static_cast<uint64_t>(u & 0x7fffffu) << 29));
+  return fc_u2d(f2d_rare(u));
 }
 
-// double -> float, round to nearest even
-HEOMGB_HD float d2f(double x) {
-  const uint64_t u = fc_d2u(x);
+// double -> float, round to nearest even.  The common case (a result in the
+// normal float range) drops 29 fraction bits with one rounding increment (a
+// carry may reach the exponent, up to infinity); the rest takes a separate call.
+HEOMGB_COLD uint32_t d2f_rare(uint64_t u) {
   const uint32_t sign = static_cast<uint32_t>(u >> 63) << 31;
   const int ex = static_cast<int>((u >> 52) & 0x7ffu);
   const uint64_t man = u & ((1ull << 52) - 1);
   if (ex == 0x7ff)  // infinity, or a quiet NaN
-    return fc_u2f(sign | 0x7f800000u | (man ? (0x400000u | static_cast<uint32_t>(man >> 29)) : 0u));
-  const int e = ex - 896;  // the biased float exponent
-  if (e >= 255) return fc_u2f(sign | 0x7f800000u);
-  if (e >= 1) {  // normal range: drop 29 fraction bits; a carry may reach the exponent (up to infinity)
-    uint32_t bits = sign | (static_cast<uint32_t>(e) << 23) | static_cast<uint32_t>(man >> 29);
-    const uint64_t rem = man & ((1ull << 29) - 1), half = 1ull << 28;
-    if (rem > half || (rem == half && (bits & 1u))) bits += 1u;
-    return fc_u2f(bits);
-  }
+    return sign | 0x7f800000u | (man ? (0x400000u | static_cast<uint32_t>(man >> 29)) : 0u);
+  if (ex - 896 >= 255) return sign | 0x7f800000u;  // overflow
   // subnormal or zero result: q = round(M / 2^s), M the 53-bit significand
   const int s = 926 - ex;  // >= 30
-  if (s > 54 || ex == 0) return fc_u2f(sign);  // below half the smallest subnormal (FP64 subnormals too)
+  if (s > 54 || ex == 0) return sign;  // below half the smallest subnormal (FP64 subnormals too)
   const uint64_t M = man | (1ull << 52);
   uint32_t q = static_cast<uint32_t>(M >> s);
   const uint64_t rem = M & ((1ull << s) - 1), half = 1ull << (s - 1);
   if (rem > half || (rem == half && (q & 1u))) q += 1u;  // may become the smallest normal: same encoding
-  return fc_u2f(sign | q);
+  return sign | q;
+}
+HEOMGB_HD float d2f(double x) {
+  const uint64_t u = fc_d2u(x);
+  const uint32_t hi = static_cast<uint32_t>(u >> 32);
+  const uint32_t e = ((hi >> 20) & 0x7ffu) - 897u;  // biased float exponent - 1, unsigned
+  if (e < 254u) {  // the float exponent is 1..254
+    // sign | exponent | the top 23 fraction bits, then round on the 29 dropped bits
+    uint32_t bits = (hi & 0x80000000u) | ((e + 1u) << 23) | static_cast<uint32_t>((u >> 29) & 0x7fffffu);
+    const uint32_t rem = static_cast<uint32_t>(u) & 0x1fffffffu;
+    bits += (rem > 0x10000000u || (rem == 0x10000000u && (bits & 1u))) ? 1u : 0u;
+    return fc_u2f(bits);
+  }
+  return fc_u2f(d2f_rare(u));
 }
 
 }  // namespace heomgb

@@ -193,7 +193,7 @@ heomgb_status heomgb_qme_solver_main_size(const heomgb_qme_solver* qs, long long
  * elements per thread, number of tiles and the kernel variant's minimum
  * resident CTAs (1, or 3 for the mixed form's register-capped variant); 0 for
  * the other kernels.  The environment variable
- * HEOMGB_TILE=<64|128|256>x<1..8>[x<1|3>] (e.g. "128x2") pins the shape
+ * HEOMGB_TILE=<64|128|256>x<1..8>[x<1|3|4>] (e.g. "128x2") pins the shape
  * instead of searching, for reproducible profiles. */
 heomgb_status heomgb_qme_solver_tuning(const heomgb_qme_solver* qs, int* block, int* elems_per_thread,
                                        int* n_tiles, int* min_blocks);

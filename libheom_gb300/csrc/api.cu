@@ -1107,8 +1107,8 @@ void autotune(heomgb_qme_solver* qs) {
     } else {
       const int got = std::sscanf(env, "%dx%dx%d", &pin_b, &pin_e, &pin_m);
       if (got < 2 || (pin_b != 64 && pin_b != 128 && pin_b != 256) || pin_e < 1 || pin_e > 8 ||
-          (pin_m != 1 && pin_m != 3))
-        throw arg_error("HEOMGB_TILE must be tc or <64|128|256>x<1..8>[x<1|3>]");
+          (pin_m != 1 && pin_m != 3 && pin_m != 4))
+        throw arg_error("HEOMGB_TILE must be tc or <64|128|256>x<1..8>[x<1|3|4>]");
     }
   }
   // the tensor-core commutator joins the search where every instance is
@@ -1160,7 +1160,7 @@ void autotune(heomgb_qme_solver* qs) {
     }
   }
   const int blocks[3] = {64, 128, 256}, epts[4] = {1, 2, 4, 8};
-  const int n_minb = qs->mixed ? 2 : 1, minbs[2] = {1, 3};
+  const int n_minb = qs->mixed ? 3 : 1, minbs[3] = {1, 3, 4};
   for (int b : blocks)
     for (int e : epts)
       for (int mi = 0; mi < n_minb; ++mi) {

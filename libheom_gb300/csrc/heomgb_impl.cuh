@@ -160,7 +160,7 @@ struct DiagSet {
   int n_tiles;
   long long total;          // elements over all instances
   size_t smem;              // dynamic shared memory of the largest tile
-  int min_blocks;           // 1, or 3: the mixed kernel compiled for 3 resident 256-thread CTAs (<= 80 registers)
+  int min_blocks;           // 1, 3 or 4: the mixed kernel compiled for 3 (<= 80 registers) or 4 (<= 64) resident 256-thread CTAs
   int tcore;                // 1: micro-tiled commutators on the tensor cores (k_rhs_diag_tc)
   int tmem_cols;            // tensor-memory columns a CTA of k_rhs_diag_tc allocates
 };

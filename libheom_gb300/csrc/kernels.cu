@@ -2269,6 +2269,7 @@ static cudaError_t launch_typed(const RhsModel& m, const DiagSet* ds, const Stag
     auto kern = k_rhs_diag<TC, TB, 1>;
     if constexpr (std::is_same<TC, float>::value) {
       if (ds->min_blocks == 3) kern = k_rhs_diag<TC, TB, 3>;
+      if (ds->min_blocks == 4) kern = k_rhs_diag<TC, TB, 4>;  // 64 registers: 32 warps per SM
       if (ds->tcore) kern = ds->min_blocks == 3 ? k_rhs_diag_tc<TB, 3> : k_rhs_diag_tc<TB, 2>;
     }
     if (dsm > 48 * 1024) {

@@ -203,8 +203,9 @@ heomgb_status heomgb_qme_solver_tuning(const heomgb_qme_solver* qs, int* block, 
  * that variant, HEOMGB_TCORE=0 keeps it out of the search.  No reference
  * counterpart: the reference evaluates every term on CUDA cores. */
 heomgb_status heomgb_qme_solver_tensor_cores(const heomgb_qme_solver* qs, int* on);
-/* 1 when the solver runs each output interval (rkdp, rk4, lsrk4) as one resident
- * cooperative launch (mixed form, one model on the diagonal-coupling path,
+/* 1 when the solver runs each output interval (rkdp, rk4, lsrk4 in the mixed
+ * form; rk4 in the FP64 form) as one resident
+ * cooperative launch (one model on the diagonal-coupling path,
  * state held in the CTAs' shared memory between stages), else 0; grid and
  * ados_per_cta (may be NULL) receive its CTAs and the ADOs each owns.
  * HEOMGB_RESIDENT=0 keeps the per-stage kernels.  No reference counterpart:

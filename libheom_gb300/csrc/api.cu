@@ -981,6 +981,14 @@ int resident_scheme(const heomgb_qme_solver* qs) {
   return qs->kind == HEOMGB_RK4 ? kResidentRk4 : qs->kind == HEOMGB_LSRK4 ? kResidentLs : kResidentDp;
 }
 
+// The resident kernel variant of the solver: the scheme in the mixed form,
+// k_rk4_resident64 for fixed-step RK4 in the FP64 form, -1 where none exists.
+int resident_variant(const heomgb_qme_solver* qs) {
+  const int scheme = resident_scheme(qs);
+  if (qs->mixed) return scheme;
+  return scheme == kResidentRk4 ? kResidentRk4F64 : -1;
+}
+
 // Arguments of the resident kernels for the solver's buffers and its tuned shape.
 ResidentArgs resident_args(heomgb_qme_solver* qs) {
   ResidentArgs a{};
@@ -1195,9 +1203,10 @@ void autotune(heomgb_qme_solver* qs) {
     build_plan(qs->plan, insts, best_b, best_e, best_m, qs->mixed, q->n_sm, qs->stream);
 }
 
-// The resident interval (Dormand-Prince, fixed-step RK4 or LSRK4) applies to one
-// mixed-form model on the diagonal-coupling path without a terminator, when a
-// co-resident grid holds its state in shared memory.  Fewer ADOs per CTA shorten each stage, more
+// The resident interval (Dormand-Prince, fixed-step RK4 or LSRK4; fixed-step
+// RK4 also in the FP64 form) applies to one model on the diagonal-coupling
+// path without a terminator, when a co-resident grid holds its state in
+// shared memory.  Fewer ADOs per CTA shorten each stage, more
 // CTAs lengthen each grid barrier, so the grid is tuned: every co-resident
 // shape (1 to 8 CTAs per SM, 1 or 2 elements per thread) runs one
 // Dormand-Prince attempt or one fixed step over the solver's zeroed buffers and the fastest is
@@ -1206,8 +1215,9 @@ void autotune(heomgb_qme_solver* qs) {
 void plan_resident(heomgb_qme_solver* qs) {
   heomgb_qme* q = qs->q;
   qs->resident = false;
-  if (!qs->mixed || q->path != PATH_DIAG || qs->qmes.size() != 1 || qs->term) return;
   const int scheme = resident_scheme(qs);
+  const int variant = resident_variant(qs);
+  if (variant < 0 || q->path != PATH_DIAG || qs->qmes.size() != 1 || qs->term) return;
   if (q->dinst.max_terms > kResidentTerms / 2) return;  // the per-element term table holds 4 + 4
   if (const char* env = std::getenv("HEOMGB_RESIDENT"))
     if (std::string(env) == "0") return;
@@ -1234,12 +1244,12 @@ void plan_resident(heomgb_qme_solver* qs) {
       const int apc = (I.nh + target - 1) / target;
       const int grid = (I.nh + apc - 1) / apc;
       if (grid == last_grid) continue;
-      const size_t smem = resident_smem(I.n2, apc, scheme);
+      const size_t smem = resident_smem(I.n2, apc, variant);
       if (smem > 200 * 1024) continue;
       const int E = apc * I.n2;  // ept elements per thread
       const int block = std::max(64, ((E + ept - 1) / ept + 31) / 32 * 32);
       if (block > kResidentMaxBlock) continue;
-      const int nb = resident_blocks_per_sm(scheme, hreal, ept, block, smem);
+      const int nb = resident_blocks_per_sm(variant, hreal, ept, block, smem);
       if (nb < 1 || static_cast<long long>(nb) * q->n_sm < grid) continue;
       shapes.push_back(Shape{grid, apc, block, ept, smem});
       last_grid = grid;
@@ -1276,7 +1286,7 @@ void plan_resident(heomgb_qme_solver* qs) {
         a.n_steps = scheme == kResidentDp ? 0 : 3;  // fixed steps: four, as the instance-resident plan times
         a.dt_step = a.dt_last = 1e-3;
         ck(cudaEventRecord(e0, qs->stream), "event");
-        ck(launch_resident(a, scheme, hreal, qs->res_ept, qs->res_grid, qs->res_block, qs->res_smem, qs->stream),
+        ck(launch_resident(a, variant, hreal, qs->res_ept, qs->res_grid, qs->res_block, qs->res_smem, qs->stream),
            "resident tune");
         ck(cudaEventRecord(e1, qs->stream), "event");
         ck(cudaEventSynchronize(e1), "event sync");
@@ -1635,7 +1645,7 @@ void solve_fixed(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwarg
     a.dt_step = dt;
     a.dt_last = last;
     busy_begin(qs);
-    const cudaError_t le = launch_resident(a, resident_scheme(qs), qs->q->dinst.h_real != 0, qs->res_ept,
+    const cudaError_t le = launch_resident(a, resident_variant(qs), qs->q->dinst.h_real != 0, qs->res_ept,
                                            qs->res_grid, qs->res_block, qs->res_smem, qs->stream);
     if (le != cudaErrorCooperativeLaunchTooLarge) {
       ck(le, "resident interval");

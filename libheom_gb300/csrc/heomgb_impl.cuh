@@ -189,6 +189,7 @@ struct ResidentArgs {
 };
 // the resident kernels: Dormand-Prince, fixed-step RK4, fixed-step LSRK4
 constexpr int kResidentDp = 0, kResidentRk4 = 1, kResidentLs = 2;
+constexpr int kResidentRk4F64 = 4;  // fixed-step RK4 in the FP64 form (k_rk4_resident64)
 // smem of a CTA owning ados_per_cta ADOs in the given scheme's kernel
 size_t resident_smem(int n2, int ados_per_cta, int scheme);
 int resident_blocks_per_sm(int scheme, bool hreal, int ept, int block, size_t smem);

@@ -1556,6 +1556,192 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
     for (int le = threadIdx.x; le < E; le += blockDim.x) R.S[0][gb + le] = Sv[le];
 }
 
+// The fixed-step RK4 interval of the FP64 form in one cooperative launch (the
+// stage kernels of a small model are launch-bound): as k_rk4_resident, with
+// every vector in FP64 — a CTA keeps its ADOs' state, the RK4 accumulator, two
+// stage-input copies and a bath-term table with FP64 coefficients in shared
+// memory; the stage inputs Y2, Y3, Y4 and the new state go through global
+// memory for the neighbour gathers (the state buffer is the stage-1 input, as
+// in the stage kernels).  Per element the arithmetic is k_rhs_diag's FP64
+// form with the RK4 epilogues (EPI_RK4_1..4, explicit FMAs), in the same
+// order, so the results are the stage kernels' bits.
+template <int EPT>
+__device__ __forceinline__ void res_build64(const DiagInst& I, int l0, int E, int* Toff, double2* Tcf,
+                                            ResElems<EPT>& el, double2 (&g)[EPT]) {
+  const int n = I.n, n2 = I.n2, K = I.K, void_idx = I.nh;
+  const bool sqn = I.sqrt_norm != 0;
+#pragma unroll
+  for (int r = 0; r < EPT; ++r) {
+    const int le = threadIdx.x + r * blockDim.x;
+    const int lec = le < E ? le : 0;
+    const int lt = lec / n2, e = lec - lt * n2, a = e / n;
+    el.lt[r] = lt;
+    el.e[r] = e;
+    el.a[r] = a;
+    el.b[r] = e - a * n;
+    const int l = min(l0 + lt, I.nh - 1);
+    const double2 g0 = I.ngd[l], g1 = I.c_sd[e];
+    g[r] = make_double2(g0.x + g1.x, g0.y + g1.y);
+    if (le < E) {
+      const int* __restrict__ p1row = I.p1 + static_cast<size_t>(l) * K;
+      const int* __restrict__ m1row = I.m1 + static_cast<size_t>(l) * K;
+      const int* __restrict__ nrow = I.nidx + static_cast<size_t>(l) * K;
+      const int pb = __ldg(I.plus_ptr + e), pe = __ldg(I.plus_ptr + e + 1);
+      const int mb = __ldg(I.minus_ptr + e), me = __ldg(I.minus_ptr + e + 1);
+      for (int j = 0; j < 4; ++j) {
+        int off = -1;
+        double2 cf = make_double2(0.0, 0.0);
+        const int p = pb + j;
+        if (p < pe) {
+          const int k = __ldg(I.plus_mode + p);
+          const int lp = __ldg(p1row + k);
+          if (lp != void_idx) {
+            off = lp * n2 + e;
+            cf = I.c_plus[p];
+            if (sqn) {
+              const double f = sqrt(static_cast<double>(__ldg(nrow + k) + 1));
+              cf = make_double2(f * cf.x, f * cf.y);
+            }
+          }
+        }
+        Toff[static_cast<size_t>(j) * E + le] = off;
+        Tcf[static_cast<size_t>(j) * E + le] = cf;
+      }
+      for (int j = 0; j < 4; ++j) {
+        int off = -1;
+        double2 cf = make_double2(0.0, 0.0);
+        const int p = mb + j;
+        if (p < me) {
+          const int k = __ldg(I.minus_mode + p);
+          const int lm = __ldg(m1row + k);
+          if (lm != void_idx) {
+            const int nk_i = __ldg(nrow + k);
+            const double nk = sqn ? sqrt(static_cast<double>(nk_i)) : occ<double>(nk_i);
+            const double2 cm = I.c_minus[p];
+            off = lm * n2 + e;
+            cf = make_double2(nk * cm.x, nk * cm.y);
+          }
+        }
+        Toff[static_cast<size_t>(4 + j) * E + le] = off;
+        Tcf[static_cast<size_t>(4 + j) * E + le] = cf;
+      }
+    }
+  }
+}
+
+template <bool HREAL, int EPT>
+__global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident64(const ResidentArgs R) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const DiagInst& I = R.inst;
+  const int n = I.n, n2 = I.n2;
+  const int l0 = min(I.nh, static_cast<int>(blockIdx.x) * R.ados_per_cta);
+  const int l1 = min(I.nh, l0 + R.ados_per_cta);
+  const int E = (l1 - l0) * n2;
+  const size_t gb = static_cast<size_t>(l0) * n2;
+  double2* S = R.S[0];  // the state: also the stage-1 input the neighbours gather
+  double2* Yt[2] = {reinterpret_cast<double2*>(R.Ytmp[0]), reinterpret_cast<double2*>(R.Ytmp[1])};
+  // shared memory: H | state, accumulator | two stage-input copies | the bath-term table
+  double2* Hs = reinterpret_cast<double2*>(smem_raw);
+  double2* Sv = Hs + n2;
+  double2* Av = Sv + E;
+  double2* yt = Av + E;
+  double2* Tcf = yt + 2 * static_cast<size_t>(E);
+  int* Toff = reinterpret_cast<int*>(Tcf + kResidentTerms * static_cast<size_t>(E));
+  for (int i = threadIdx.x; i < n2; i += blockDim.x) Hs[i] = I.H[i];
+  for (int le = threadIdx.x; le < E; le += blockDim.x) {
+    const double2 v = S[gb + le];
+    Sv[le] = v;
+    yt[le] = v;
+  }
+  __syncthreads();
+  ResElems<EPT> el;
+  double2 gd[EPT];
+  res_build64<EPT>(I, l0, E, Toff, Tcf, el, gd);
+  unsigned long long gen = 0;
+  bool ok = true;
+  for (long long step = 0; step <= R.n_steps && ok; ++step) {
+    const double dt = step < R.n_steps ? R.dt_step : R.dt_last;
+    for (int s = 0; s < 4 && ok; ++s) {
+      const double2* Xg = s == 0 ? S : Yt[(s - 1) & 1];
+      const double2* Xs = yt + static_cast<size_t>(s & 1) * E;
+      double2* Xn = yt + static_cast<size_t>((s + 1) & 1) * E;
+      double2 D[EPT];
+#pragma unroll
+      for (int r = 0; r < EPT; ++r) {  // commutator and damping from this CTA's copy
+        const int le = threadIdx.x + r * blockDim.x;
+        D[r] = make_double2(0.0, 0.0);
+        if (le >= E) continue;
+        const int a = el.a[r], b = el.b[r];
+        const double2* yl = Xs + static_cast<size_t>(el.lt[r]) * n2;
+        double2 acc = make_double2(0.0, 0.0);
+        if (HREAL) {
+#pragma unroll 4
+          for (int c = 0; c < n; ++c) {
+            const double hac = Hs[a * n + c].x, hcb = Hs[c * n + b].x;
+            const double2 ycb = yl[c * n + b], yac = yl[a * n + c];
+            acc.x = fma(hac, ycb.x, acc.x);
+            acc.x = fma(-hcb, yac.x, acc.x);
+            acc.y = fma(hac, ycb.y, acc.y);
+            acc.y = fma(-hcb, yac.y, acc.y);
+          }
+        } else {
+          double2 neg = make_double2(0.0, 0.0);
+#pragma unroll 4
+          for (int c = 0; c < n; ++c) {
+            cfma(acc, Hs[a * n + c], yl[c * n + b]);
+            cfma(neg, yl[a * n + c], Hs[c * n + b]);
+          }
+          acc.x -= neg.x;
+          acc.y -= neg.y;
+        }
+        double2 Dv = make_double2(-acc.y, acc.x);
+        cfma(Dv, gd[r], yl[el.e[r]]);
+        D[r] = Dv;
+      }
+      if (step > 0 || s > 0) {  // the other CTAs' stage input (or new state) of the last stage
+        ok = grid_wait(R.bar, gen);
+        if (!ok) break;
+      }
+      double2 vv[EPT][kResidentTerms];  // all gathers first (L1-bypassing: written until the wait returned)
+#pragma unroll
+      for (int r = 0; r < EPT; ++r) {
+        const int le = threadIdx.x + r * blockDim.x;
+#pragma unroll
+        for (int j = 0; j < kResidentTerms; ++j) {
+          const int off = le < E ? Toff[static_cast<size_t>(j) * E + le] : -1;
+          vv[r][j] = off >= 0 ? __ldcg(Xg + off) : make_double2(0.0, 0.0);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < EPT; ++r) {
+        const int le = threadIdx.x + r * blockDim.x;
+        if (le >= E) continue;
+#pragma unroll
+        for (int j = 0; j < kResidentTerms; ++j) cfma(D[r], Tcf[static_cast<size_t>(j) * E + le], vv[r][j]);
+        const double2 k = make_double2(-dt * D[r].x, -dt * D[r].y);
+        const size_t g = gb + le;
+        if (s < 3) {  // rho_n = rho + c*k ; acc = rho + k/6 or acc += k/3
+          const double c = s == 2 ? 1.0 : 0.5;
+          const double w = s == 0 ? (1.0 / 6.0) : (2.0 / 6.0);
+          const double2 sv = Sv[le];
+          const double2 y = make_double2(fma(c, k.x, sv.x), fma(c, k.y, sv.y));
+          Xn[le] = y;
+          Yt[s & 1][g] = y;
+          const double2 a = s == 0 ? sv : Av[le];
+          Av[le] = make_double2(fma(w, k.x, a.x), fma(w, k.y, a.y));
+        } else {  // rho = acc + k4/6
+          const double2 a = Av[le];
+          const double2 v = make_double2(fma(1.0 / 6.0, k.x, a.x), fma(1.0 / 6.0, k.y, a.y));
+          Sv[le] = v;
+          Xn[le] = v;  // the next step's stage-1 input (yt[0])
+          S[g] = v;
+        }
+      }
+      grid_arrive(R.bar);
+    }
+  }
+}
+
 // The fixed-step LSRK4 interval of the mixed form in one cooperative launch
 // (2N-storage RK4, lsrk4.h:32-47: buff = -buff + k or k, rho += B_s buff): a
 // CTA keeps its ADOs' FP64 state (updated in place), the FP32 buffer, the
@@ -1630,6 +1816,9 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_ls_resident(const Resi
 
 size_t resident_smem(int n2, int ados_per_cta, int scheme) {
   const size_t E = static_cast<size_t>(ados_per_cta) * n2;
+  if (scheme == kResidentRk4F64)  // H | state, accumulator, two stage inputs | table (offset, FP64 coefficient)
+    return sizeof(double2) * static_cast<size_t>(n2) +
+           E * (4 * sizeof(double2) + kResidentTerms * (sizeof(int) + sizeof(double2)));
   const size_t per = scheme == kResidentRk4   ? 2 * sizeof(double2) + 3 * sizeof(float2)
                      : scheme == kResidentLs  ? sizeof(double2) + 2 * sizeof(float2)
                                               : 2 * sizeof(double2) + 6 * sizeof(float2) + 4 * sizeof(float2);
@@ -1652,6 +1841,10 @@ static const void* resident_kernel(int scheme, bool hreal, int ept) {
     case 19: return reinterpret_cast<const void*>(k_ls_resident<true, 1>);
     case 20: return reinterpret_cast<const void*>(k_ls_resident<false, 2>);
     case 21: return reinterpret_cast<const void*>(k_ls_resident<true, 2>);
+    case 34: return reinterpret_cast<const void*>(k_rk4_resident64<false, 1>);
+    case 35: return reinterpret_cast<const void*>(k_rk4_resident64<true, 1>);
+    case 36: return reinterpret_cast<const void*>(k_rk4_resident64<false, 2>);
+    case 37: return reinterpret_cast<const void*>(k_rk4_resident64<true, 2>);
     default: return nullptr;
   }
 }

@@ -87,11 +87,12 @@ def test_local_complex_h_sqrt_filter_col_major(precision, monkeypatch):
 
 
 def test_local_single_model(monkeypatch):
-    """One FP64 model (no cooperative resident kernel in that form) in one bin."""
+    """One FP64 model in one bin."""
     p = configs.spin_boson(depth=10)
 
     def run(local):
         monkeypatch.setenv("HEOMGB_LOCAL", "1" if local else "0")
+        monkeypatch.setenv("HEOMGB_RESIDENT", "0")  # against the stage kernels
         qs = lh.qme_solver(lh.from_params(p, precision="fp64"), lh.rk4())
         rho = p.rho0_ground()
         qs.solve(rho, T, None, {"dt": DT})

@@ -102,19 +102,23 @@ def test_resident_first_attempt_bit_identical(ept, monkeypatch):
 def test_resident_only_where_it_applies(monkeypatch):
     p = configs.exciton_7site(depth=2)
     _, _, tune = run(p, [0.0, 1.0], monkeypatch, True, precision="fp64")
-    assert not tune["resident"]  # the FP64 form keeps the stage kernels
+    assert not tune["resident"]  # Dormand-Prince in the FP64 form keeps the stage kernels
     monkeypatch.setenv("HEOMGB_RESIDENT", "1")
-    qs = lh.qme_solver(lh.from_params(p, precision="fp64"), lh.rk4())
-    assert not qs.tuning()["resident"]  # the FP64 form keeps the stage kernels for fixed steps too
+    qs = lh.qme_solver(lh.from_params(p, precision="fp64"), lh.lsrk4())
+    assert not qs.tuning()["resident"]  # so does LSRK4 in the FP64 form
 
 
+@pytest.mark.parametrize("form", ["mixed", "rk4_fp64"])
 @pytest.mark.parametrize("solver", ["rk4", "lsrk4"])
 @pytest.mark.parametrize("ept", ["1", "2"])
 @pytest.mark.parametrize("maker", ["spin_boson", "exciton"])
-def test_resident_fixed_step_bit_identical(maker, ept, solver, monkeypatch):
+def test_resident_fixed_step_bit_identical(maker, ept, solver, form, monkeypatch):
     """Fixed-step RK4 / LSRK4 in one resident launch per interval: the same
     per-element arithmetic as the stage kernels and no step control, so every
     ADO agrees bit for bit after many steps, the clamped last step included."""
+    if form == "rk4_fp64" and solver != "rk4":
+        pytest.skip("the FP64 form has a resident kernel for RK4 only")
+    precision = "fp64" if form == "rk4_fp64" else "mixed"
     p = configs.spin_boson(depth=10) if maker == "spin_boson" else configs.exciton_7site(depth=3)
     dt = 0.005 if maker == "spin_boson" else 0.5
     t = [0.0, 37 * dt + 0.3 * dt, 60 * dt]  # the first interval ends with a shorter step
@@ -123,7 +127,7 @@ def test_resident_fixed_step_bit_identical(maker, ept, solver, monkeypatch):
         monkeypatch.setenv("HEOMGB_RESIDENT", "1" if resident else "0")
         monkeypatch.setenv("HEOMGB_RESIDENT_EPT", ept)
         monkeypatch.setenv("HEOMGB_LOCAL", "0")  # the cooperative kernel under test, not the one-CTA plan
-        q = lh.from_params(p, precision="mixed")
+        q = lh.from_params(p, precision=precision)
         qs = lh.qme_solver(q, lh.SOLVERS[solver]())
         rho = p.rho0_ground()
         qs.solve(rho, t, None, {"dt": dt})

@@ -823,6 +823,18 @@ void build_model(heomgb_qme* q) {
     else
       ck(cudaMemsetAsync(plus_any, 0, sizeof(int) * std::max(nh, 1), s), "memset");
     di.plus_any = plus_any;
+    // the FP64 coefficients scaled by every occupation (the FP64 kernels' per-term products, tabulated)
+    di.occ_rows = q->max_depth + 1;
+    const int n_plus = static_cast<int>(cp.size()), n_minus = static_cast<int>(cmn.size());
+    double2* cmn_n = static_cast<double2*>(q->arena.alloc(sizeof(double2) * std::max<size_t>(1, static_cast<size_t>(n_minus) * di.occ_rows)));
+    ck(launch_scaled_coef(n_minus, di.occ_rows, m.c_minus, cmn_n, false, m.sqrt_norm != 0, s), "scaled coefficients");
+    di.c_minus_n = cmn_n;
+    di.c_plus_n = nullptr;
+    if (m.sqrt_norm) {
+      double2* cp_n = static_cast<double2*>(q->arena.alloc(sizeof(double2) * std::max<size_t>(1, static_cast<size_t>(n_plus) * di.occ_rows)));
+      ck(launch_scaled_coef(n_plus, di.occ_rows, m.c_plus, cp_n, true, true, s), "scaled coefficients");
+      di.c_plus_n = cp_n;
+    }
     build_plan(q->diff_plan, {di}, 128, 4, 1, q->precision_eff == HEOMGB_MIXED, q->n_sm, s);
   } else if (q->path == PATH_GENERAL) {
     if (rhs_smem_bytes(m, PATH_GENERAL, false) > 200 * 1024)

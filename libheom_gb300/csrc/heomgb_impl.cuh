@@ -150,6 +150,12 @@ struct DiagInst {
   int h_sym;                // H real and symmetric (the tensor-core commutator's condition)
   int max_terms;            // max over elements of max(+1 terms, -1 terms)
   const int* plus_any;      // per ADO: 1 if any ptr_p1 entry is a real ADO (0 on the deepest tier)
+  // FP64 coefficients scaled by the occupation n_k = 0..max_depth (row p*(max_depth+1) + n_k):
+  // -1 terms n_k c_minus[p] (sqrt(n_k) c_minus[p] under sqrt normalisation); +1 terms
+  // sqrt(n_k + 1) c_plus[p] (sqrt normalisation only, else null)
+  const double2* c_minus_n;
+  const double2* c_plus_n;
+  int occ_rows;             // max_depth + 1
 };
 struct DiagTile {
   int inst, l0, nt, pad;
@@ -243,6 +249,9 @@ cudaError_t launch_ngd(int K, int n_hrchy, const int* nidx, const double2* gdiag
                        cudaStream_t s);
 cudaError_t launch_to_bulk(const double2* src, float2* dst, long long n, cudaStream_t s);
 cudaError_t launch_plus_any(int K, int n_hrchy, const int* p1, int* out, cudaStream_t s);
+// out[p*rows + i] = scale(i) * c[p]: scale n (minus, integer), sqrt(n) (minus, sqrt) or sqrt(n+1) (plus, sqrt)
+cudaError_t launch_scaled_coef(int n_terms, int rows, const double2* c, double2* out, bool plus, bool sqn,
+                               cudaStream_t s);
 cudaError_t launch_transpose_ados(const double2* in, double2* out, int n, long long count, cudaStream_t s);
 cudaError_t launch_ctl_init(DpCtl* c, double t, double dt, double t_bound, double atol, double rtol, int cur,
                             cudaStream_t s);

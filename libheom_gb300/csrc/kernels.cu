@@ -796,8 +796,12 @@ __device__ __forceinline__ double diag_tile(const DiagInst* __restrict__ I, cons
             v[j] = ldc<TC>(yi + static_cast<size_t>(lp) * n2 + e);
             cf[j] = cpl[p];
             if (sqn) {
-              const TC f = sqrt(static_cast<TC>(nrow[k] + 1));
-              cf[j] = cx<TC>(f * cf[j].x, f * cf[j].y);
+              if constexpr (std::is_same<TC, double>::value) {  // sqrt(n_k + 1) c_plus from the table
+                cf[j] = I->c_plus_n[static_cast<size_t>(p) * I->occ_rows + nrow[k]];
+              } else {
+                const TC f = sqrt(static_cast<TC>(nrow[k] + 1));
+                cf[j] = cx<TC>(f * cf[j].x, f * cf[j].y);
+              }
             }
           } else if (term_p) {  // truncated tier: the terminator's prediction
             const float2 t = term_p[(static_cast<size_t>(l0 + lt - term_first) * K + k) * n2 + e];
@@ -815,10 +819,14 @@ __device__ __forceinline__ double diag_tile(const DiagInst* __restrict__ I, cons
           const int k = __ldg(minus_mode + p);
           const int lm = m1row[k];
           if (lm != void_idx) {
-            const TC nk = sqn ? sqrt(static_cast<TC>(nrow[k])) : occ<TC>(nrow[k]);
-            const C cm = cmi[p];
             v[4 + j] = ldc<TC>(yi + static_cast<size_t>(lm) * n2 + e);
-            cf[4 + j] = cx<TC>(nk * cm.x, nk * cm.y);
+            if constexpr (std::is_same<TC, double>::value) {  // n_k c_minus (or sqrt(n_k) c_minus) from the table
+              cf[4 + j] = I->c_minus_n[static_cast<size_t>(p) * I->occ_rows + nrow[k]];
+            } else {
+              const TC nk = sqn ? sqrt(static_cast<TC>(nrow[k])) : occ<TC>(nrow[k]);
+              const C cm = cmi[p];
+              cf[4 + j] = cx<TC>(nk * cm.x, nk * cm.y);
+            }
           }
         }
       }
@@ -1927,8 +1935,12 @@ __device__ __forceinline__ cx_t<TC> local_rhs(const DiagInst& I, const cx_t<TC>*
         if (lp != void_idx) {
           C cf = cpl[p];
           if (sqn) {
-            const TC f = sqrt(static_cast<TC>(__ldg(nrow + k) + 1));
-            cf = cx<TC>(f * cf.x, f * cf.y);
+            if constexpr (std::is_same<TC, double>::value) {
+              cf = I.c_plus_n[static_cast<size_t>(p) * I.occ_rows + __ldg(nrow + k)];
+            } else {
+              const TC f = sqrt(static_cast<TC>(__ldg(nrow + k) + 1));
+              cf = cx<TC>(f * cf.x, f * cf.y);
+            }
           }
           cfma(D, cf, Xi[lp * n2 + e]);
         }
@@ -1942,9 +1954,13 @@ __device__ __forceinline__ cx_t<TC> local_rhs(const DiagInst& I, const cx_t<TC>*
         const int lm = __ldg(m1row + k);
         if (lm != void_idx) {
           const int nk_i = __ldg(nrow + k);
-          const TC nk = sqn ? sqrt(static_cast<TC>(nk_i)) : occ<TC>(nk_i);
-          const C cm = cmi[p];
-          cfma(D, cx<TC>(nk * cm.x, nk * cm.y), Xi[lm * n2 + e]);
+          if constexpr (std::is_same<TC, double>::value) {
+            cfma(D, I.c_minus_n[static_cast<size_t>(p) * I.occ_rows + nk_i], Xi[lm * n2 + e]);
+          } else {
+            const TC nk = sqn ? sqrt(static_cast<TC>(nk_i)) : occ<TC>(nk_i);
+            const C cm = cmi[p];
+            cfma(D, cx<TC>(nk * cm.x, nk * cm.y), Xi[lm * n2 + e]);
+          }
         }
       }
     }
@@ -2612,6 +2628,27 @@ __global__ void k_plus_any(int K, int n_hrchy, const int* p1, int* out) {
   int any = 0;
   for (int k = 0; k < K; ++k) any |= p1[static_cast<size_t>(l) * K + k] != n_hrchy;
   out[l] = any;
+}
+
+// The FP64 coefficient tables of DiagInst::c_minus_n / c_plus_n, with the
+// same operations the stage kernels apply per term (so the products agree bit
+// for bit): n_k * c, sqrt(n_k) * c or sqrt(n_k + 1) * c.
+__global__ void k_scaled_coef(int n_terms, int rows, const double2* c, double2* out, int plus, int sqn) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_terms * rows) return;
+  const int p = i / rows, nk = i - p * rows;
+  const double2 cm = c[p];
+  const double f = plus ? sqrt(static_cast<double>(nk + 1)) : (sqn ? sqrt(static_cast<double>(nk)) : occ<double>(nk));
+  out[i] = make_double2(f * cm.x, f * cm.y);
+}
+
+cudaError_t launch_scaled_coef(int n_terms, int rows, const double2* c, double2* out, bool plus, bool sqn,
+                               cudaStream_t s) {
+  const int total = n_terms * rows;
+  if (total <= 0) return cudaSuccess;
+  k_scaled_coef<<<(total + 127) / 128, 128, 0, s>>>(n_terms, rows, c, out, plus ? 1 : 0, sqn ? 1 : 0);
+  ++g_launches;
+  return cudaGetLastError();
 }
 
 cudaError_t launch_plus_any(int K, int n_hrchy, const int* p1, int* out, cudaStream_t s) {

@@ -2232,7 +2232,7 @@ __global__ void __launch_bounds__(256) k_rhs_general(const RhsModel m, const Sta
           const int lm = __ldg(m.m1 + static_cast<size_t>(l) * K + k);
           if (lm != void_idx) {
             const int nki = __ldg(m.nidx + static_cast<size_t>(l) * K + k);
-            const TC nk = m.sqrt_norm ? sqrt(static_cast<TC>(nki)) : static_cast<TC>(nki);
+            const TC nk = m.sqrt_norm ? sqrt(static_cast<TC>(nki)) : occ<TC>(nki);
             const C r = ldc<TC>(y + static_cast<size_t>(lm) * n2 + e);
             cfma(ph, cx<TC>(nk * sv[k].x, nk * sv[k].y), r);
             cfma(ps, cx<TC>(-nk * av[k].x, -nk * av[k].y), r);
@@ -2324,7 +2324,7 @@ __global__ void __launch_bounds__(256) k_rhs_liou(const RhsModel m, const Stage 
           const int lm = __ldg(m.m1 + static_cast<size_t>(l) * K + k);
           if (lm != void_idx) {
             const int nki = __ldg(m.nidx + static_cast<size_t>(l) * K + k);
-            const TC nk = m.sqrt_norm ? sqrt(static_cast<TC>(nki)) : static_cast<TC>(nki);
+            const TC nk = m.sqrt_norm ? sqrt(static_cast<TC>(nki)) : occ<TC>(nki);
             const C r = ldc<TC>(y + static_cast<size_t>(lm) * n2 + e);
             cfma(ph, cx<TC>(nk * sv[k].x, nk * sv[k].y), r);
             cfma(ps, cx<TC>(-nk * av[k].x, -nk * av[k].y), r);

@@ -1882,13 +1882,25 @@ cudaError_t launch_resident(const ResidentArgs& args, int scheme, bool hreal, in
 
 // ------------------------------------------------------------------ instance-resident fixed steps (batches)
 // The right-hand side D of one element (e of ADO lt), k_rhs_diag's arithmetic
-// in its order (commutator, damping, then the +1 and -1 terms in groups of
-// four), with every ADO read from the bin's shared-memory copy Xi of the
-// instance's stage input.  Slots without a term are skipped (k_rhs_diag adds
+// in its order (commutator, damping with g = ngamma + s_delta term, summed as
+// k_rhs_diag sums it, then the +1 and -1 terms in groups of four), with every
+// ADO read from the bin's shared-memory copy Xi of the instance's stage input.  Slots without a term are skipped (k_rhs_diag adds
 // them as 0*0, which leaves D unchanged).
+// the damping coefficient of element le (e of ADO lt): the FP64 form's table entry, or the mixed
+// form's FP32 sum, k_rhs_diag's operations either way
+template <typename TC>
+__device__ __forceinline__ cx_t<TC> local_damp(const DiagInst& I, const cx_t<TC>* Gs, int le, int lt, int e) {
+  if constexpr (std::is_same<TC, double>::value) {
+    return Gs[le];
+  } else {
+    const float2 g0 = I.ngd_f[lt], g1 = I.c_sd_f[e];
+    return make_float2(g0.x + g1.x, g0.y + g1.y);
+  }
+}
+
 template <typename TC>
 __device__ __forceinline__ cx_t<TC> local_rhs(const DiagInst& I, const cx_t<TC>* Hi, const cx_t<TC>* Xi, int lt,
-                                              int e) {
+                                              int e, cx_t<TC> g) {
   using C = cx_t<TC>;
   const int n = I.n, n2 = I.n2, K = I.K, void_idx = I.nh;
   const int a = e / n, b = e - a * n;
@@ -1915,8 +1927,7 @@ __device__ __forceinline__ cx_t<TC> local_rhs(const DiagInst& I, const cx_t<TC>*
     acc.y -= neg.y;
   }
   C D = cx<TC>(-acc.y, acc.x);
-  const C g0 = pick<TC>(I.ngd, I.ngd_f)[lt], g1 = pick<TC>(I.c_sd, I.c_sd_f)[e];
-  cfma(D, cx<TC>(g0.x + g1.x, g0.y + g1.y), yl[e]);
+  cfma(D, g, yl[e]);  // g = ngamma of the ADO + the element's s_delta term
   const bool sqn = I.sqrt_norm != 0;
   const int* __restrict__ p1row = I.p1 + static_cast<size_t>(lt) * K;
   const int* __restrict__ m1row = I.m1 + static_cast<size_t>(lt) * K;
@@ -2007,6 +2018,9 @@ __global__ void __launch_bounds__(512, 2) k_fixed_local(const LocalArgs A) {
   C* X0 = Hs + s_hbase[ni];
   C* X1 = X0 + E;
   unsigned* desc = reinterpret_cast<unsigned*>(X1 + E);
+  // FP64 form: each element's damping coefficient, summed once (two FP64 additions per element and
+  // stage less on the narrow FP64 pipe); the mixed form sums it in FP32 per stage
+  C* Gs = reinterpret_cast<C*>(desc + ((E + 3) & ~3));
   for (int ii = 0; ii < ni; ++ii) {
     const C* Hg = pick<TC>(s_inst[ii].H, s_inst[ii].H_f);
     for (int i = threadIdx.x; i < s_inst[ii].n2; i += blockDim.x) Hs[s_hbase[ii] + i] = Hg[i];
@@ -2018,6 +2032,10 @@ __global__ void __launch_bounds__(512, 2) k_fixed_local(const LocalArgs A) {
     const int loc = le - s_ebase[ii];
     const int lt = loc / I.n2, e = loc - lt * I.n2;
     desc[le] = static_cast<unsigned>(ii) | (static_cast<unsigned>(e) << 8) | (static_cast<unsigned>(lt) << 16);
+    if constexpr (!MIX) {
+      const C g0 = I.ngd[lt], g1 = I.c_sd[e];
+      Gs[le] = cx<TC>(g0.x + g1.x, g0.y + g1.y);
+    }
     const size_t g = static_cast<size_t>(I.elem_off) + loc;
     if constexpr (MIX)
       X0[le] = A.Yf[g];
@@ -2042,7 +2060,7 @@ __global__ void __launch_bounds__(512, 2) k_fixed_local(const LocalArgs A) {
           if constexpr (MIX) {  // FP32 buffer (the first half of the buffer allocation), FP64 state
             float2* buf = reinterpret_cast<float2*>(A.acc);
             const float2 pf = s == 0 ? make_float2(0.f, 0.f) : buf[g];
-            const float2 D = local_rhs<TC>(I, Hs + s_hbase[ii], Xs + s_ebase[ii], lt, e);
+            const float2 D = local_rhs<TC>(I, Hs + s_hbase[ii], Xs + s_ebase[ii], lt, e, local_damp<TC>(I, Gs, le, lt, e));
             const float fdt = static_cast<float>(dt);
             const float2 b = s == 0 ? make_float2(__fmul_rn(-fdt, D.x), __fmul_rn(-fdt, D.y))
                                     : make_float2(fmaf(-fdt, D.x, -pf.x), fmaf(-fdt, D.y, -pf.y));
@@ -2054,7 +2072,7 @@ __global__ void __launch_bounds__(512, 2) k_fixed_local(const LocalArgs A) {
             Xn[le] = f;
           } else {
             const double2 pa = s == 0 ? make_double2(0.0, 0.0) : A.acc[g];
-            const double2 D = local_rhs<TC>(I, Hs + s_hbase[ii], Xs + s_ebase[ii], lt, e);
+            const double2 D = local_rhs<TC>(I, Hs + s_hbase[ii], Xs + s_ebase[ii], lt, e, local_damp<TC>(I, Gs, le, lt, e));
             const double2 k = make_double2(-dt * D.x, -dt * D.y);
             const double2 b = s == 0 ? k : make_double2(-pa.x + k.x, -pa.y + k.y);
             A.acc[g] = b;
@@ -2068,7 +2086,7 @@ __global__ void __launch_bounds__(512, 2) k_fixed_local(const LocalArgs A) {
         const double2 pa = s == 0 ? A.S[g] : A.acc[g];
         if constexpr (MIX) {
           const float2 pf = s < 3 ? A.Yf[g] : make_float2(0.f, 0.f);
-          const float2 D = local_rhs<TC>(I, Hs + s_hbase[ii], Xs + s_ebase[ii], lt, e);
+          const float2 D = local_rhs<TC>(I, Hs + s_hbase[ii], Xs + s_ebase[ii], lt, e, local_damp<TC>(I, Gs, le, lt, e));
           const float fdt = static_cast<float>(dt);
           const float2 k = make_float2(__fmul_rn(-fdt, D.x), __fmul_rn(-fdt, D.y));
           if (s < 3) {  // rho_n = rho + c*k (FP32 from the state's copy); acc = rho + k/6 or acc += k/3
@@ -2089,7 +2107,7 @@ __global__ void __launch_bounds__(512, 2) k_fixed_local(const LocalArgs A) {
           }
         } else {
           const double2 pb = (s == 1 || s == 2) ? A.S[g] : pa;
-          const double2 D = local_rhs<TC>(I, Hs + s_hbase[ii], Xs + s_ebase[ii], lt, e);
+          const double2 D = local_rhs<TC>(I, Hs + s_hbase[ii], Xs + s_ebase[ii], lt, e, local_damp<TC>(I, Gs, le, lt, e));
           const double2 k = make_double2(-dt * D.x, -dt * D.y);
           if (s < 3) {
             const double c = s == 2 ? 1.0 : 0.5;
@@ -2115,7 +2133,8 @@ size_t local_bin_smem(const int* n2, const int* nh, int count, bool mixed) {
     h += (static_cast<size_t>(n2[i]) * c + 15) / 16 * 16;
     e += static_cast<size_t>(n2[i]) * nh[i];
   }
-  return h + e * (2 * c + sizeof(unsigned));
+  // + the FP64 form's damping table (16-byte aligned after the descriptors)
+  return h + e * (2 * c + sizeof(unsigned)) + (mixed ? 0 : 12 + e * sizeof(double2));
 }
 
 static const void* local_kernel(bool mixed, int scheme) {
@@ -2130,6 +2149,11 @@ int local_blocks_per_sm(bool mixed, int scheme, int block, size_t smem) {
   const void* kern = local_kernel(mixed, scheme);
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
     return 0;
+  // every instance takes the largest shared-memory split, so that the FP64 and the mixed
+  // sub-batch's bins (different sizes) can share an SM
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared) !=
+      cudaSuccess)
+    return 0;
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, block, smem) != cudaSuccess) return 0;
   return nb;
@@ -2139,6 +2163,8 @@ cudaError_t launch_local(const LocalArgs& args, bool mixed, int scheme, int grid
                          cudaStream_t s) {
   const void* kern = local_kernel(mixed, scheme);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
   LocalArgs a = args;
   void* params[] = {&a};

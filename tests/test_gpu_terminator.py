@@ -87,7 +87,7 @@ def test_terminator_feeds_rhs_like_numpy():
 def test_trained_terminator_gains_over_plain_truncation():
     """Train the closure with the library's kernels on depth-12 spin-boson
     trajectories (lambda, beta sampled over the batched-sweep ranges; the
-    instances inside the closure's domain are kept) and judge it on held-out
+    instances inside the closure's domain are kept) and evaluate it on held-out
     instances of that domain at depth 3 against the depth-12 plain solve."""
     pytest.importorskip("torch")
     from libheom_gb300.params import HeomParams

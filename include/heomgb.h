@@ -312,7 +312,10 @@ heomgb_status heomgb_errnrm1_device(const void* e, const void* x1, const void* x
  * lives in a fixed device array, so n_dim + max_depth + 2 may not exceed
  * HEOMGB_NOALLOC_MAX_BINOM_DIM (HEOMGB_ERR_CAPACITY otherwise).  The first call
  * on a device looks up that array's device address; make it before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race. */
+ * capture.  The address is kept for the life of the process, so a caller that
+ * resets a device (cudaDeviceReset) must not call this entry point on that
+ * device afterwards.  All calls share the array: calls that overlap on the GPU
+ * race. */
 #define HEOMGB_NOALLOC_MAX_BINOM_DIM 96
 heomgb_status heomgb_hrchy_build_noalloc(int n_dim, int max_depth, int* n_dev, int* ptr_p1_dev, int* ptr_m1_dev,
                                          int* n_hrchy, void* cuda_stream);

@@ -61,12 +61,15 @@ extern "C" heomgb_status heomgb_hrchy_build_noalloc(int n_dim, int max_depth, in
     set_error_message("heomgb_hrchy_build_noalloc: n_dim >= 1, max_depth >= 0 and non-null pointers required");
     return HEOMGB_ERR_INVALID_ARGUMENT;
   }
-  const int dim = n_dim + max_depth + 2;
-  if (dim > kMaxBinomDim) {
-    set_error_message("heomgb_hrchy_build_noalloc: n_dim + max_depth + 2 = " + std::to_string(dim) +
+  // the sum is formed in 64 bits: n_dim and max_depth near INT_MAX must not wrap
+  // to a small value that passes the capacity check
+  const long long dim_ll = static_cast<long long>(n_dim) + max_depth + 2;
+  if (dim_ll > kMaxBinomDim) {
+    set_error_message("heomgb_hrchy_build_noalloc: n_dim + max_depth + 2 = " + std::to_string(dim_ll) +
                       " exceeds the fixed scratch maximum of " + std::to_string(kMaxBinomDim));
     return HEOMGB_ERR_CAPACITY;
   }
+  const int dim = static_cast<int>(dim_ll);
   // ADO count C(n_dim + max_depth, max_depth), checked against int range on the host.
   long double c = 1;
   for (int i = 1; i <= max_depth; ++i) c = c * (n_dim + i) / i;

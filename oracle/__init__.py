@@ -22,7 +22,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_lib", "libheom_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libheomref.so")
 REF_SQRT_SO = os.path.join(HERE, "_ref", "libheomref_sqrt.so")
-REF_TREE = "/root/reference"
+# where the reference source tree lies (only the fixture generator and the
+# reference-code oracle read it); LIBHEOM_REFERENCE overrides the default
+REF_TREE = os.environ.get("LIBHEOM_REFERENCE", "/root/reference")
 
 FORMS = {"hilb": 0, "liou": 1, "ado": 2, "redfield_hilb": 3, "redfield_liou": 4}
 SOLVERS = {"rk4": 0, "lsrk4": 1, "rkdp": 2}

@@ -47,6 +47,19 @@ def test_version_and_errors_without_gpu():
     assert lib.heomgb_errnrm1_scratch(10**6) > 2
 
 
+@pytest.mark.parametrize("n_dim,max_depth", [(80, 20), (2**31 - 1, 0), (0x7ffffff0, 0x7ffffff0), (1, 2**31 - 1)])
+def test_noalloc_capacity_check_without_gpu(n_dim, max_depth):
+    # the size check runs before any CUDA call, so no kernel is launched here;
+    # sums that would wrap a 32-bit int must still be rejected
+    lib = _lib.load()
+    got = ctypes.c_int(0)
+    dummy = ctypes.c_void_p(16)  # never dereferenced
+    st = lib.heomgb_hrchy_build_noalloc(n_dim, max_depth, dummy, dummy, dummy, ctypes.byref(got), None)
+    assert st == 7  # HEOMGB_ERR_CAPACITY
+    assert b"exceeds the fixed scratch maximum" in lib.heomgb_last_error()
+    assert got.value == 0
+
+
 def test_python_mirror_validation():
     q = lh.heom_hilb(3)
     q.alloc_noises(2)

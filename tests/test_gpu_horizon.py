@@ -1,0 +1,135 @@
+"""Parity at the measured workloads' own sizes and horizons, against the CPU
+restatement of the reference path (the oracle port, itself pinned to the
+reference's own code by the golden fixtures).
+
+* 7-site aggregate (n=7, K=14, depth 4, 3060 ADOs), Dormand-Prince
+  atol=rtol=1e-8 to t_final = 1 ps: the FP64 form to 1e-10 per ADO with the
+  same attempt count; the mixed form (FP32 bulk, FP64 state) to 1e-6 in
+  max |delta rho_0| and in max |delta rho| / max |rho| over all ADOs.
+* 24-site aggregate (n=24, K=48, depth 3, 20825 ADOs x 576 elements), LSRK4
+  dt = 0.5 fs, four steps: FP64 to 1e-10 per ADO, mixed to 1e-6.
+* The batched sweep's RK4 run to t = 20 (4000 steps of dt = 0.005) on a
+  sample of its instances, FP64 to 1e-10 per ADO, mixed to 1e-6 on rho_0.
+* The standalone errnrm1 against numpy, repeated with the same scratch.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import libheom_gb300 as lh
+import oracle
+from libheom_gb300 import _lib, configs
+
+pytestmark = pytest.mark.gpu
+
+DP_KW = dict(dt=0.1, atol=1e-8, rtol=1e-8)
+
+
+def ado_rel_err(got, ref):
+    scale = np.abs(ref).max(axis=(-2, -1), keepdims=True) + 1e-300
+    return float((np.abs(got - ref) / scale).max())
+
+
+@pytest.fixture(scope="module")
+def exciton7_oracle():
+    p = configs.exciton_7site()
+    ref, st = oracle.Oracle("port").solve(p, p.rho0_ground(), [0.0, 1000.0], solver="rkdp", with_stats=True,
+                                          **DP_KW)
+    return p, ref[-1], st
+
+
+def test_exciton7_fp64_dp_to_1ps_vs_oracle(exciton7_oracle):
+    p, ref, st = exciton7_oracle
+    qs = lh.qme_solver(lh.from_params(p), lh.rkdp())
+    rho = p.rho0_ground()
+    qs.solve(rho, [0.0, 1000.0], None, DP_KW)
+    assert ado_rel_err(rho, ref) <= 1e-10
+    assert qs.stats()["attempts"] == st["attempts"]
+
+
+def test_exciton7_mixed_dp_to_1ps_vs_oracle(exciton7_oracle):
+    p, ref, st = exciton7_oracle
+    qs = lh.qme_solver(lh.from_params(p, precision="mixed"), lh.rkdp())
+    rho = p.rho0_ground()
+    qs.solve(rho, [0.0, 1000.0], None, DP_KW)
+    assert np.abs(rho[0] - ref[0]).max() <= 1e-6
+    assert np.abs(rho - ref).max() / np.abs(ref).max() <= 1e-6
+    # the step sequence is the mixed form's own (FP32 error vector), close to the oracle's
+    assert abs(qs.stats()["attempts"] - st["attempts"]) <= 0.05 * st["attempts"]
+
+
+@pytest.fixture(scope="module")
+def aggregate24_oracle():
+    p = configs.aggregate_24site()
+    t = [0.0, 2.0]
+    ref = oracle.Oracle("port").solve(p, p.rho0_ground(), t, solver="lsrk4", dt=0.5)
+    return p, t, ref[-1]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_aggregate24_lsrk4_full_size_steps_vs_oracle(aggregate24_oracle, precision):
+    p, t, ref = aggregate24_oracle
+    qs = lh.qme_solver(lh.from_params(p, precision=precision), lh.lsrk4())
+    rho = p.rho0_ground()
+    qs.solve(rho, t, None, {"dt": 0.5})
+    assert qs.stats()["rhs"] == 4 * 4
+    if precision == "fp64":
+        assert ado_rel_err(rho, ref) <= 1e-10
+    else:
+        assert np.abs(rho[0] - ref[0]).max() <= 1e-6
+        assert np.abs(rho - ref).max() <= 1e-6
+
+
+def _sweep_sample():
+    full = configs.batched_sweep()
+    # spin-boson instances over the depth range, and 4-level chains
+    return full[0:8] + full[768:772]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batched_sweep_4000_steps_vs_oracle(precision):
+    ps = _sweep_sample()
+    qmes = [lh.from_params(p, precision=precision) for p in ps]
+    bs = lh.batch_solver(qmes, lh.rk4())
+    rho = np.concatenate([p.rho0_ground().ravel() for p in ps])
+    bs.solve(rho, [0.0, 20.0], None, {"dt": 0.005})
+    off = bs.offsets()
+    port = oracle.Oracle("port")
+    checked = 0
+    for i, p in enumerate(ps):
+        ref = port.solve(p, p.rho0_ground(), [0.0, 20.0], solver="rk4", dt=0.005)[-1]
+        # instances that diverge under the reference's own algorithm (a
+        # Matsubara frequency near the Drude pole) are not accuracy cases
+        if not np.all(np.isfinite(ref)) or np.abs(ref[0]).max() > 1.0 + 1e-3:
+            continue
+        got = rho[off[i]:off[i + 1]].reshape(ref.shape)
+        checked += 1
+        if precision == "fp64" or qmes[i].get_precision()["effective"] == "fp64":
+            assert ado_rel_err(got, ref) <= 1e-10, i
+        else:
+            assert np.abs(got[0] - ref[0]).max() <= 1e-6, i
+    assert checked >= len(ps) // 2
+
+
+def _np_errnrm1(e, x1, x2, atol, rtol):
+    s = atol + rtol * np.maximum(np.abs(x1), np.abs(x2))
+    return float(np.sqrt(np.mean((np.abs(e) / s) ** 2)))
+
+
+@pytest.mark.parametrize("n", [1, 257, 152 * 4 * 256 + 4097])
+def test_errnrm1_device_vs_numpy(n):
+    torch = pytest.importorskip("torch")
+    lib = _lib.load()
+    rng = np.random.default_rng(n)
+    mk = lambda: rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    e, x1, x2 = mk() * 1e-6, mk(), mk()
+    dev = [torch.from_numpy(a).cuda() for a in (e, x1, x2)]
+    scratch = torch.full((lib.heomgb_errnrm1_scratch(n),), 7.0, dtype=torch.float64, device="cuda")
+    want = _np_errnrm1(e, x1, x2, 1e-8, 1e-6)
+    for _ in range(2):  # the second call reuses the scratch (its arrival counter must be reset)
+        got = ctypes.c_double(0.0)
+        torch.cuda.synchronize()
+        _lib.check(lib.heomgb_errnrm1_device(dev[0].data_ptr(), dev[1].data_ptr(), dev[2].data_ptr(), 1e-8, 1e-6,
+                                             n, scratch.data_ptr(), ctypes.byref(got), None))
+        assert abs(got.value - want) <= 1e-12 * want

@@ -6,7 +6,8 @@ engine, on small seeded cases and stores inputs and outputs as .npz files.
 Needs the reference tree, so it runs where that tree exists; the fixtures it
 writes are committed and are all the tests need elsewhere.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every fixture
+    python tests/golden/make_golden.py horizon    # only the 1 ps horizon fixture
 """
 from __future__ import annotations
 
@@ -136,9 +137,31 @@ def filter_fixture(ref):
     np.savez_compressed(os.path.join(HERE, "hrchy_filtered.npz"), **out)
 
 
+def horizon_fixture(ref):
+    """The default measured workload at its own size and horizon: the 7-site
+    aggregate (depth 4, 3060 ADOs), Dormand-Prince atol=rtol=1e-8 to 1 ps.
+    Stored: the ADOs of tiers 0 and 1, every 17th ADO and the largest |rho|
+    of every tier, so that the fixture stays small."""
+    p = configs.exciton_7site()
+    kw = dict(dt=0.1, atol=1e-8, rtol=1e-8)
+    rho_t = ref.solve(p, p.rho0_ground(), [0.0, 1000.0], solver="rkdp", **kw)
+    final = rho_t[-1]
+    n, _, _ = ref.hrchy(p.n_modes, p.max_depth)
+    tiers = n.sum(axis=1)
+    idx = np.union1d(np.arange(0, 1 + p.n_modes), np.arange(0, p.n_hrchy(), 17))
+    out = dict(t_final=np.array(1000.0), dt=np.array(kw["dt"]), atol=np.array(kw["atol"]),
+               rtol=np.array(kw["rtol"]), ado_index=idx, ados=final[idx],
+               tier_max=np.array([np.abs(final[tiers == d]).max() for d in range(p.max_depth + 1)]))
+    np.savez_compressed(os.path.join(HERE, "horizon_exciton7_rkdp_1ps.npz"), **out)
+
+
 def main():
     oracle.build("ref")
     ref = oracle.Oracle("ref")
+    if sys.argv[1:] == ["horizon"]:  # only the horizon fixture (the others are unchanged)
+        horizon_fixture(ref)
+        return
+    horizon_fixture(ref)
     hrchy_fixture(ref)
     diff_fixture(ref, "generic", generic_case(), 11)
     diff_fixture(ref, "projector", projector_case(), 12)

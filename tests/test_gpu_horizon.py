@@ -3,9 +3,11 @@ restatement of the reference path (the oracle port, itself pinned to the
 reference's own code by the golden fixtures).
 
 * 7-site aggregate (n=7, K=14, depth 4, 3060 ADOs), Dormand-Prince
-  atol=rtol=1e-8 to t_final = 1 ps: the FP64 form to 1e-10 per ADO with the
-  same attempt count; the mixed form (FP32 bulk, FP64 state) to 1e-6 in
-  max |delta rho_0| and in max |delta rho| / max |rho| over all ADOs.
+  atol=rtol=1e-8 to t_final = 1 ps, against the port and against the
+  reference's own output (golden fixture): the FP64 form to 1e-10 of the
+  state's largest element with the same attempt count; the mixed form (FP32
+  bulk, FP64 state) to 1e-6 in max |delta rho_0| and in max |delta rho| /
+  max |rho| over all ADOs.
 * 24-site aggregate (n=24, K=48, depth 3, 20825 ADOs x 576 elements), LSRK4
   dt = 0.5 fs, four steps: FP64 to 1e-10 per ADO, mixed to 1e-6.
 * The batched sweep's RK4 run to t = 20 (4000 steps of dt = 0.005) on a
@@ -13,6 +15,7 @@ reference's own code by the golden fixtures).
 * The standalone errnrm1 against numpy, repeated with the same scratch.
 """
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -22,6 +25,7 @@ import oracle
 from libheom_gb300 import _lib, configs
 
 pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
 
 DP_KW = dict(dt=0.1, atol=1e-8, rtol=1e-8)
 
@@ -39,13 +43,36 @@ def exciton7_oracle():
     return p, ref[-1], st
 
 
+def horizon_fixture():
+    """The reference's own code run to 1 ps on the same workload (a subset of
+    its ADOs and the largest |rho| of every tier; tests/golden/make_golden.py)."""
+    return np.load(os.path.join(GOLD, "horizon_exciton7_rkdp_1ps.npz"))
+
+
+# Error criteria at 1 ps.  Relative to the state's largest element (|rho_0|):
+# two correct FP64 implementations that sum in different orders (the
+# reference's own build and the CPU restatement) agree to 1.3e-15 there.  Per
+# ADO, relative to each ADO's own largest element, the same two differ by up
+# to 1.2e-9 after the 328 attempts: the deepest tier is 3.6e7 times smaller
+# than rho_0 and fed by much larger neighbours, so rounding that is tiny on
+# the state's scale is not on that ADO's.  The per-ADO bound is set above that
+# floor.
+GLOBAL_REL = 1e-10
+PER_ADO_REL = 1e-7
+
+
 def test_exciton7_fp64_dp_to_1ps_vs_oracle(exciton7_oracle):
     p, ref, st = exciton7_oracle
     qs = lh.qme_solver(lh.from_params(p), lh.rkdp())
     rho = p.rho0_ground()
     qs.solve(rho, [0.0, 1000.0], None, DP_KW)
-    assert ado_rel_err(rho, ref) <= 1e-10
     assert qs.stats()["attempts"] == st["attempts"]
+    assert np.abs(rho - ref).max() / np.abs(ref).max() <= GLOBAL_REL
+    assert ado_rel_err(rho, ref) <= PER_ADO_REL
+    z = horizon_fixture()
+    got = rho[z["ado_index"]]
+    assert np.abs(got - z["ados"]).max() / z["tier_max"].max() <= GLOBAL_REL
+    assert ado_rel_err(got, z["ados"]) <= PER_ADO_REL
 
 
 def test_exciton7_mixed_dp_to_1ps_vs_oracle(exciton7_oracle):
@@ -55,6 +82,8 @@ def test_exciton7_mixed_dp_to_1ps_vs_oracle(exciton7_oracle):
     qs.solve(rho, [0.0, 1000.0], None, DP_KW)
     assert np.abs(rho[0] - ref[0]).max() <= 1e-6
     assert np.abs(rho - ref).max() / np.abs(ref).max() <= 1e-6
+    z = horizon_fixture()
+    assert np.abs(rho[0] - z["ados"][0]).max() <= 1e-6
     # the step sequence is the mixed form's own (FP32 error vector), close to the oracle's
     assert abs(qs.stats()["attempts"] - st["attempts"]) <= 0.05 * st["attempts"]
 

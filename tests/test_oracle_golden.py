@@ -9,6 +9,7 @@ import pytest
 
 import oracle
 from _cases import FILTERS, params_from_npz
+from libheom_gb300 import configs
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
 
@@ -88,3 +89,18 @@ def test_filtered_hierarchy_matches_reference(port, name):
     assert np.array_equal(m1, z[f"m1_{name}"])
     from libheom_gb300.params import hierarchy_indices
     assert [tuple(r) for r in n] == hierarchy_indices(K, N, f)
+
+
+def test_port_vs_reference_at_1ps_horizon():
+    """The CPU restatement against the reference's own code on the default
+    measured workload at its full horizon (7-site, Dormand-Prince to 1 ps):
+    identical attempt sequence, 1e-12 of the state's largest element."""
+    z = np.load(os.path.join(GOLD, "horizon_exciton7_rkdp_1ps.npz"))
+    p = configs.exciton_7site()
+    rho = oracle.Oracle("port").solve(p, p.rho0_ground(), [0.0, float(z["t_final"])], solver="rkdp",
+                                      dt=float(z["dt"]), atol=float(z["atol"]), rtol=float(z["rtol"]))[-1]
+    got = rho[z["ado_index"]]
+    assert np.abs(got - z["ados"]).max() / z["tier_max"].max() <= 1e-12
+    n, _, _ = oracle.Oracle("port").hrchy(p.n_modes, p.max_depth)
+    tiers = n.sum(axis=1)
+    assert np.allclose([np.abs(rho[tiers == d]).max() for d in range(p.max_depth + 1)], z["tier_max"], rtol=1e-9)

@@ -203,6 +203,15 @@ heomgb_status heomgb_qme_solver_tuning(const heomgb_qme_solver* qs, int* block, 
  * that variant, HEOMGB_TCORE=0 keeps it out of the search.  No reference
  * counterpart: the reference evaluates every term on CUDA cores. */
 heomgb_status heomgb_qme_solver_tensor_cores(const heomgb_qme_solver* qs, int* on);
+/* 1 when the autotuner picked the stage kernel for site-local baths (every V_u
+ * diagonal with a single nonzero entry, as in exciton aggregates; n_level a
+ * multiple of 4, at least 8; mixed form): per-ADO lists of occupied modes for
+ * the -1 terms, the commutator in registers, a compile-time stage epilogue and
+ * cp.async-staged tiles; ados_per_tile (may be NULL) receives its tile.
+ * HEOMGB_SITES=0 keeps it out of the search, HEOMGB_TILE=sites:<block>x<tile>x<2|3>
+ * pins it.  No reference counterpart: heom_hilb::calc_diff_impl
+ * (heom_hilb.h:70-215) visits every mode of every ADO. */
+heomgb_status heomgb_qme_solver_site_kernel(const heomgb_qme_solver* qs, int* on, int* ados_per_tile);
 /* 1 when the solver runs each output interval (rkdp, rk4, lsrk4 in the mixed
  * form; rk4 in the FP64 form) as one resident
  * cooperative launch (one model on the diagonal-coupling path,

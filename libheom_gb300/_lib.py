@@ -72,6 +72,7 @@ SIGNATURES = {
     "heomgb_qme_solver_main_size": (ctypes.c_int, [ctypes.c_void_p, c_ll_p]),
     "heomgb_qme_solver_tuning": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p]),
     "heomgb_qme_solver_tensor_cores": (ctypes.c_int, [ctypes.c_void_p, c_int_p]),
+    "heomgb_qme_solver_site_kernel": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p]),
     "heomgb_qme_solver_resident": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p]),
     "heomgb_qme_solver_local": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p]),
     "heomgb_qme_solver_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,

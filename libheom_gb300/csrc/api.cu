@@ -217,6 +217,7 @@ struct DiagPlan {
   DiagSet ds{};
   int block = 128, ept = 4, grid = 1, min_blocks = 1;
   bool tcore = false;  // commutators on the tensor cores (k_rhs_diag_tc)
+  bool sites = false;  // the site-local-bath kernel (k_rhs_sites)
 };
 
 // Whether an instance can take the tensor-core commutator: mixed form, a
@@ -228,7 +229,7 @@ bool tcore_eligible(const DiagInst& I, bool mixed) {
 }
 
 void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int ept, int min_blocks, bool mixed,
-                int n_sm, cudaStream_t s, bool tcore = false) {
+                int n_sm, cudaStream_t s, bool tcore = false, int sites_tile = 0) {
   P.arena.release();
   P.inst = insts;
   std::vector<DiagTile> tiles;
@@ -241,10 +242,19 @@ void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int 
     for (const DiagInst& I : insts)
       if (!tcore_eligible(I, mixed)) throw unsupported_error("tensor-core commutator: instance not eligible");
   }
+  if (sites_tile > 0) {
+    if (insts.size() != 1 || !sites_eligible(insts[0], mixed) || (min_blocks != 2 && min_blocks != 3))
+      throw unsupported_error("site-local-bath kernel: one eligible instance, 2 or 3 CTAs per SM");
+    if (sites_smem(insts[0].n2, insts[0].K, sites_tile, insts[0].site_w) > cap)
+      throw unsupported_error("site-local-bath tile exceeds shared memory");
+  }
   for (size_t i = 0; i < P.inst.size(); ++i) {
     DiagInst& I = P.inst[i];
     int tile;
-    if (tcore) {  // the tile is fixed by the GEMM shape (4 n rows per ADO, 128-row blocks)
+    if (sites_tile > 0) {
+      tile = sites_tile;
+      smem = sites_smem(I.n2, I.K, tile, I.site_w);
+    } else if (tcore) {  // the tile is fixed by the GEMM shape (4 n rows per ADO, 128-row blocks)
       tile = tc_tile(I.n);
       if (diag_tile_smem_tc(I.n, I.K, tile) > cap) throw unsupported_error("tensor-core tile exceeds shared memory");
       smem = std::max(smem, diag_tile_smem_tc(I.n, I.K, tile));
@@ -268,12 +278,21 @@ void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int 
   P.ds.min_blocks = mixed ? min_blocks : 1;
   P.ds.tcore = tcore ? 1 : 0;
   P.ds.tmem_cols = tmem_cols;
+  P.ds.sites = sites_tile > 0 ? 1 : 0;
+  P.ds.sites_tile = sites_tile;
+  P.ds.sites_hreal = (sites_tile > 0 && P.inst[0].h_real) ? 1 : 0;
+  P.ds.sites_minb = sites_tile > 0 ? min_blocks : 0;
+  P.sites = sites_tile > 0;
   P.tcore = tcore;
   P.block = block;
   P.ept = ept;
   P.min_blocks = P.ds.min_blocks;
+  // the site-local-bath kernel loops over tiles with one resident wave (its
+  // copies of the next tile overlap the current one); the others take two
+  // waves of 2048 threads per SM
+  const long long per_sm = sites_tile > 0 ? min_blocks : 2048 / block;
   P.grid = static_cast<int>(std::max<long long>(
-      1, std::min<long long>(static_cast<long long>(tiles.size()), static_cast<long long>(n_sm) * (2048 / block))));
+      1, std::min<long long>(static_cast<long long>(tiles.size()), static_cast<long long>(n_sm) * per_sm)));
   ck(cudaStreamSynchronize(s), "plan upload");
 }
 
@@ -835,6 +854,46 @@ void build_model(heomgb_qme* q) {
       ck(launch_scaled_coef(n_plus, di.occ_rows, m.c_plus, cp_n, true, true, s), "scaled coefficients");
       di.c_plus_n = cp_n;
     }
+    // site-local baths (every V_u diagonal with a single nonzero entry, at site
+    // s_u): the -1 coefficients of an element in the row, column or diagonal
+    // of s_u, formed as the per-element table above forms them, and the
+    // per-ADO records of occupied modes (k_rhs_sites)
+    {
+      std::vector<int> usite(U, -1);
+      bool site_local = U > 0 && K > 0;
+      for (int u = 0; u < U && site_local; ++u) {
+        int cnt = 0;
+        for (int a = 0; a < n; ++a)
+          if (q->baths[u].V[static_cast<size_t>(a) * n + a] != cd(0.0, 0.0)) {
+            ++cnt;
+            usite[u] = a;
+          }
+        site_local = cnt == 1;
+      }
+      if (site_local) {
+        std::vector<int> msite(K, 0);
+        std::vector<cd> cm3(3 * static_cast<size_t>(K));
+        for (int u = 0; u < U; ++u) {
+          const cd v = q->baths[u].V[static_cast<size_t>(usite[u]) * n + usite[u]], zero(0.0, 0.0);
+          const cd vas[3] = {v, zero, v}, vbs[3] = {zero, v, v};  // row, column, diagonal of the site
+          for (int k = bath_ptr[u]; k < bath_ptr[u + 1]; ++k) {
+            msite[k] = usite[u];
+            for (int c = 0; c < 3; ++c) {
+              const cd cphi = I * (vas[c] - vbs[c]), cpsi = vas[c] + vbs[c];
+              cm3[3 * static_cast<size_t>(k) + c] = cphi * sv[k] - cpsi * av[k];
+            }
+          }
+        }
+        di.site_local = 1;
+        di.site_w = std::max(1, std::min(K, q->max_depth));
+        const int* dms = q->arena.upload(msite, s);
+        di.site_cm3 = q->arena.upload(to_f2(cm3), s);
+        int4* rec = static_cast<int4*>(q->arena.alloc(sizeof(int4) * static_cast<size_t>(nh) * (1 + di.site_w)));
+        di.site_rec = rec;
+        ck(launch_site_records(di, dms, rec, s), "site records");
+        ck(cudaStreamSynchronize(s), "site records sync");
+      }
+    }
     build_plan(q->diff_plan, {di}, 128, 4, 1, q->precision_eff == HEOMGB_MIXED, q->n_sm, s);
   } else if (q->path == PATH_GENERAL) {
     if (rhs_smem_bytes(m, PATH_GENERAL, false) > 200 * 1024)
@@ -1121,9 +1180,14 @@ void autotune(heomgb_qme_solver* qs) {
   // search relies on)
   int pin_b = 0, pin_e = 0, pin_m = 1;
   bool pin_tc = false;
+  int pin_sb = 0, pin_st = 0, pin_sm = 0;  // HEOMGB_TILE=sites:<block>x<ADOs per tile>x<2|3>
   if (const char* env = std::getenv("HEOMGB_TILE")) {
     if (std::string(env) == "tc") {
       pin_tc = true;
+    } else if (std::string(env).rfind("sites:", 0) == 0) {
+      const int got = std::sscanf(env + 6, "%dx%dx%d", &pin_sb, &pin_st, &pin_sm);
+      if (got != 3 || (pin_sb != 128 && pin_sb != 256) || pin_st < 1 || pin_st > 16 || (pin_sm != 2 && pin_sm != 3))
+        throw arg_error("HEOMGB_TILE=sites:<128|256>x<1..16>x<2|3>");
     } else {
       const int got = std::sscanf(env, "%dx%dx%d", &pin_b, &pin_e, &pin_m);
       if (got < 2 || (pin_b != 64 && pin_b != 128 && pin_b != 256) || pin_e < 1 || pin_e > 8 ||
@@ -1158,12 +1222,18 @@ void autotune(heomgb_qme_solver* qs) {
     }
     return best_ms;
   };
+  // HEOMGB_TUNE_LOG=1 prints every timed candidate to stderr
+  const bool tune_log = std::getenv("HEOMGB_TUNE_LOG") && std::string(std::getenv("HEOMGB_TUNE_LOG")) == "1";
+  auto log_shape = [&](const char* kind, int b, int x, int m, float ms) {
+    if (tune_log) std::fprintf(stderr, "heomgb tune: %s block %d x %d min_blocks %d: %.4f ms per launch\n", kind, b, x, m, ms / 3.f);
+  };
   int best_tc_m = 3, best_tc_b = 256;
   if (tc_ok && (pin_tc || !pin_b)) {
     for (int b : {128, 256})
     for (int m : {3, 2}) {  // register caps 80 and 128
       build_plan(qs->plan, insts, b, 1, m, qs->mixed, q->n_sm, qs->stream, true);
       const float ms = time_plan(b);
+      log_shape("tensor cores", b, 1, m, ms);
       // the stage flags a tensor-core wait that ran out; such a plan is not kept
       DpCtl probe;
       ck(cudaMemcpyAsync(&probe, qs->ctl, sizeof(DpCtl), cudaMemcpyDeviceToHost, qs->stream), "ctl read");
@@ -1179,13 +1249,47 @@ void autotune(heomgb_qme_solver* qs) {
       }
     }
   }
+  // the site-local-bath kernel joins the search for one eligible model whose
+  // stage input is the FP32 copy; HEOMGB_SITES=0 keeps it out
+  bool sites_ok = qs->separate && insts.size() == 1 && sites_eligible(insts[0], qs->mixed);
+  if (const char* env = std::getenv("HEOMGB_SITES"))
+    if (std::string(env) == "0") sites_ok = false;
+  if (pin_sb && !sites_ok) throw unsupported_error("HEOMGB_TILE=sites: the site-local-bath kernel does not apply");
+  bool best_sites = false;
+  int best_sb = 256, best_st = 1, best_sm = 2;
+  if (sites_ok && !pin_tc && (pin_sb || !pin_b)) {
+    const int groups_per_ado = insts[0].n2 / 4;
+    for (int b : {128, 256})
+      for (int m : {2, 3})
+        for (int t : {1, 2, 3, 4, 6, 8, 12, 16}) {
+          if (pin_sb && (b != pin_sb || t != pin_st || m != pin_sm)) continue;
+          // a tile gives each thread one to eight micro-tiles
+          if (!pin_sb && (t * groups_per_ado < b / 2 || t * groups_per_ado > 8 * b)) continue;
+          if (!pin_sb && t > 1 && (t - 1) * groups_per_ado >= 8 * b) continue;
+          if (sites_smem(insts[0].n2, insts[0].K, t, insts[0].site_w) * m > 220 * 1024) continue;
+          try {
+            build_plan(qs->plan, insts, b, 1, m, qs->mixed, q->n_sm, qs->stream, false, t);
+          } catch (const unsupported_error&) {
+            continue;
+          }
+          const float ms = pin_sb ? 0.f : time_plan(b);
+          log_shape("sites (x = ADOs per tile)", b, t, m, ms);
+          if (pin_sb || ms < best) {
+            best = ms;
+            best_sites = true;
+            best_sb = b;
+            best_st = t;
+            best_sm = m;
+          }
+        }
+  }
   const int blocks[3] = {64, 128, 256}, epts[4] = {1, 2, 4, 8};
   const int n_minb = qs->mixed ? 3 : 1, minbs[3] = {1, 3, 4};
   for (int b : blocks)
     for (int e : epts)
       for (int mi = 0; mi < n_minb; ++mi) {
       const int m = minbs[mi];
-      if (pin_tc || (pin_b && (b != pin_b || e != pin_e || m != pin_m))) continue;
+      if (pin_tc || pin_sb || (pin_b && (b != pin_b || e != pin_e || m != pin_m))) continue;
       try {
         build_plan(qs->plan, insts, b, e, m, qs->mixed, q->n_sm, qs->stream);
       } catch (const unsupported_error&) {
@@ -1198,18 +1302,22 @@ void autotune(heomgb_qme_solver* qs) {
         break;
       }
       const float ms = time_plan(b);
+      log_shape("diag (x = elements per thread)", b, e, m, ms);
       if (ms < best) {
         best = ms;
         best_b = b;
         best_e = e;
         best_m = m;
         best_tc = false;
+        best_sites = false;
       }
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   qs->stage_ms = best < 1e29f ? best / 3.f : 0.f;
-  if (best_tc)
+  if (best_sites)
+    build_plan(qs->plan, insts, best_sb, 1, best_sm, qs->mixed, q->n_sm, qs->stream, false, best_st);
+  else if (best_tc)
     build_plan(qs->plan, insts, best_tc_b, 1, best_tc_m, qs->mixed, q->n_sm, qs->stream, true);
   else
     build_plan(qs->plan, insts, best_b, best_e, best_m, qs->mixed, q->n_sm, qs->stream);
@@ -2208,6 +2316,15 @@ heomgb_status heomgb_qme_solver_local(const heomgb_qme_solver* qs, int* on, int*
     *on = qs->local ? 1 : 0;
     if (bins) *bins = qs->local ? qs->loc_grid : 0;
     if (block) *block = qs->local ? qs->loc_block : 0;
+  });
+}
+
+heomgb_status heomgb_qme_solver_site_kernel(const heomgb_qme_solver* qs, int* on, int* ados_per_tile) {
+  return guard([&] {
+    require(qs != nullptr && on != nullptr, "null argument");
+    const bool sites = qs->q->path == PATH_DIAG && qs->plan.sites;
+    *on = sites ? 1 : 0;
+    if (ados_per_tile) *ados_per_tile = sites ? qs->plan.ds.sites_tile : 0;
   });
 }
 

@@ -156,6 +156,17 @@ struct DiagInst {
   const double2* c_minus_n;
   const double2* c_plus_n;
   int occ_rows;             // max_depth + 1
+  // Site-local baths (every V_u diagonal with a single nonzero entry, at site
+  // s_u; exciton aggregates): per ADO a 16-byte header {occupied modes, 1 if
+  // any ptr_p1 entry is a real ADO, ngd_f bits x, y} followed by site_w
+  // entries {k, ptr_m1[l][k], n_k, s_u(k)} of its modes with n_k > 0 (in
+  // increasing k, real -1 neighbours only); site_cm3 holds per mode k the -1
+  // coefficient of an element in its site's row (a == s != b), column
+  // (b == s != a) or diagonal (a == b == s), the same values as c_minus_f.
+  int site_local;           // 1: the tables below are set
+  int site_w;               // entries per ADO (max(1, min(K, max_depth)))
+  const int4* site_rec;     // nh * (1 + site_w)
+  const float2* site_cm3;   // K * 3
 };
 struct DiagTile {
   int inst, l0, nt, pad;
@@ -169,6 +180,10 @@ struct DiagSet {
   int min_blocks;           // 1, 3 or 4: the mixed kernel compiled for 3 (<= 80 registers) or 4 (<= 64) resident 256-thread CTAs
   int tcore;                // 1: micro-tiled commutators on the tensor cores (k_rhs_diag_tc)
   int tmem_cols;            // tensor-memory columns a CTA of k_rhs_diag_tc allocates
+  int sites;                // 1: the site-local-bath kernel (k_rhs_sites; one instance, mixed form)
+  int sites_tile;           // its ADOs per tile
+  int sites_hreal;          // its instance has a real H
+  int sites_minb;           // its resident-CTA variant (2 or 3)
 };
 
 // Resident intervals (k_dp_resident: Dormand-Prince; k_rk4_resident and
@@ -242,6 +257,14 @@ size_t diag_tile_smem(int n2, int K, int tile, bool mixed);
 size_t diag_tile_smem_tc(int n, int K, int tile);
 int tc_tile(int n);
 int tc_tmem_cols(int n);
+
+// The site-local-bath stage kernel (sites.cu): eligibility, shared memory of
+// a CTA, set-up of the per-ADO records, and the launch (mixed form, FP32 stage
+// input).
+bool sites_eligible(const DiagInst& I, bool mixed);
+size_t sites_smem(int n2, int K, int tile, int w);
+cudaError_t launch_site_records(const DiagInst& I, const int* msite, int4* rec, cudaStream_t s);
+cudaError_t launch_sites(const DiagSet& ds, const Stage& st, int grid, int block, cudaStream_t s);
 
 cudaError_t launch_hrchy_build(int K, int depth, int n_hrchy, const long long* binom, int binom_dim, int* nidx,
                                int* p1, int* m1, cudaStream_t s);

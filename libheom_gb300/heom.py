@@ -329,8 +329,13 @@ class qme_solver:
         check(self._lib.heomgb_qme_solver_resident(self._h, ctypes.byref(rs), ctypes.byref(rg), ctypes.byref(ra)))
         lo, lb, lk = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         check(self._lib.heomgb_qme_solver_local(self._h, ctypes.byref(lo), ctypes.byref(lb), ctypes.byref(lk)))
+        si, st = ctypes.c_int(), ctypes.c_int()
+        check(self._lib.heomgb_qme_solver_site_kernel(self._h, ctypes.byref(si), ctypes.byref(st)))
         out = dict(block=b.value, elems_per_thread=e.value, n_tiles=t.value, min_blocks=m.value,
-                   tensor_cores=bool(tc.value), resident=bool(rs.value), local=bool(lo.value))
+                   tensor_cores=bool(tc.value), resident=bool(rs.value), local=bool(lo.value),
+                   sites=bool(si.value))
+        if si.value:
+            out.update(sites_ados_per_tile=st.value)
         if rs.value:
             out.update(resident_grid=rg.value, resident_ados_per_cta=ra.value)
         if lo.value:

@@ -229,7 +229,7 @@ bool tcore_eligible(const DiagInst& I, bool mixed) {
 }
 
 void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int ept, int min_blocks, bool mixed,
-                int n_sm, cudaStream_t s, bool tcore = false, int sites_tile = 0) {
+                int n_sm, cudaStream_t s, bool tcore = false, int sites_tile = 0, int sites_rt = 4) {
   P.arena.release();
   P.inst = insts;
   std::vector<DiagTile> tiles;
@@ -243,9 +243,9 @@ void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int 
       if (!tcore_eligible(I, mixed)) throw unsupported_error("tensor-core commutator: instance not eligible");
   }
   if (sites_tile > 0) {
-    if (insts.size() != 1 || !sites_eligible(insts[0], mixed) || (min_blocks != 2 && min_blocks != 3))
-      throw unsupported_error("site-local-bath kernel: one eligible instance, 2 or 3 CTAs per SM");
-    if (sites_smem(insts[0].n2, insts[0].K, sites_tile, insts[0].site_w) > cap)
+    if (insts.size() != 1 || !sites_eligible(insts[0], mixed) || !sites_variant(sites_rt, min_blocks, block))
+      throw unsupported_error("site-local-bath kernel: one eligible instance and a compiled variant");
+    if (sites_smem(insts[0].n, insts[0].K, sites_tile, insts[0].site_w) > cap)
       throw unsupported_error("site-local-bath tile exceeds shared memory");
   }
   for (size_t i = 0; i < P.inst.size(); ++i) {
@@ -253,7 +253,7 @@ void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int 
     int tile;
     if (sites_tile > 0) {
       tile = sites_tile;
-      smem = sites_smem(I.n2, I.K, tile, I.site_w);
+      smem = sites_smem(I.n, I.K, tile, I.site_w);
     } else if (tcore) {  // the tile is fixed by the GEMM shape (4 n rows per ADO, 128-row blocks)
       tile = tc_tile(I.n);
       if (diag_tile_smem_tc(I.n, I.K, tile) > cap) throw unsupported_error("tensor-core tile exceeds shared memory");
@@ -282,6 +282,7 @@ void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int 
   P.ds.sites_tile = sites_tile;
   P.ds.sites_hreal = (sites_tile > 0 && P.inst[0].h_real) ? 1 : 0;
   P.ds.sites_minb = sites_tile > 0 ? min_blocks : 0;
+  P.ds.sites_rt = sites_tile > 0 ? sites_rt : 0;
   P.sites = sites_tile > 0;
   P.tcore = tcore;
   P.block = block;
@@ -884,10 +885,29 @@ void build_model(heomgb_qme* q) {
             }
           }
         }
+        // the +1 coefficient i (v_a - v_b) sigma_k for the row and column cases, and
+        // the modes of every site in increasing k
+        std::vector<cd> cp2(2 * static_cast<size_t>(K));
+        std::vector<int> sptr(n + 1, 0), smodes;
+        for (int u = 0; u < U; ++u) {
+          const cd v = q->baths[u].V[static_cast<size_t>(usite[u]) * n + usite[u]], zero(0.0, 0.0);
+          for (int k = bath_ptr[u]; k < bath_ptr[u + 1]; ++k) {
+            cp2[2 * static_cast<size_t>(k)] = I * (v - zero) * sigma[k];
+            cp2[2 * static_cast<size_t>(k) + 1] = I * (zero - v) * sigma[k];
+          }
+        }
+        for (int site = 0; site < n; ++site) {
+          for (int k = 0; k < K; ++k)
+            if (msite[k] == site) smodes.push_back(k);
+          sptr[site + 1] = static_cast<int>(smodes.size());
+        }
         di.site_local = 1;
         di.site_w = std::max(1, std::min(K, q->max_depth));
         const int* dms = q->arena.upload(msite, s);
         di.site_cm3 = q->arena.upload(to_f2(cm3), s);
+        di.site_cp2 = q->arena.upload(to_f2(cp2), s);
+        di.site_ptr = q->arena.upload(sptr, s);
+        di.site_modes = q->arena.upload(smodes, s);
         int4* rec = static_cast<int4*>(q->arena.alloc(sizeof(int4) * static_cast<size_t>(nh) * (1 + di.site_w)));
         di.site_rec = rec;
         ck(launch_site_records(di, dms, rec, s), "site records");
@@ -1077,6 +1097,15 @@ ResidentArgs resident_args(heomgb_qme_solver* qs) {
   a.n_steps = 0;
   a.dt_step = a.dt_last = 0.0;
   a.ados_per_cta = qs->res_apc;
+  // Fault injection for the tests of the bounded waits: HEOMGB_FAULT_SKIP_ARRIVAL=<cta>
+  // makes that CTA skip its grid-barrier arrivals, HEOMGB_FAULT_SPIN_LIMIT=<polls>
+  // shortens every wait; the waits then run out, the CTAs leave and the solve
+  // reports HEOMGB_ERR_CUDA.  Neither is set in normal use.
+  a.skip_arrive_cta = -1;
+  a.spin_limit = 1LL << 24;
+  if (const char* env = std::getenv("HEOMGB_FAULT_SKIP_ARRIVAL")) a.skip_arrive_cta = std::atoi(env);
+  if (const char* env = std::getenv("HEOMGB_FAULT_SPIN_LIMIT"))
+    a.spin_limit = std::max(1LL, std::min(1LL << 24, std::atoll(env)));
   return a;
 }
 Stage solver_stage(heomgb_qme_solver* qs);
@@ -1180,14 +1209,16 @@ void autotune(heomgb_qme_solver* qs) {
   // search relies on)
   int pin_b = 0, pin_e = 0, pin_m = 1;
   bool pin_tc = false;
-  int pin_sb = 0, pin_st = 0, pin_sm = 0;  // HEOMGB_TILE=sites:<block>x<ADOs per tile>x<2|3>
+  int pin_sb = 0, pin_st = 0, pin_sm = 0, pin_sr = 0;  // HEOMGB_TILE=sites:<block>x<tile>x<CTAs per SM>[x<rows>]
   if (const char* env = std::getenv("HEOMGB_TILE")) {
     if (std::string(env) == "tc") {
       pin_tc = true;
     } else if (std::string(env).rfind("sites:", 0) == 0) {
-      const int got = std::sscanf(env + 6, "%dx%dx%d", &pin_sb, &pin_st, &pin_sm);
-      if (got != 3 || (pin_sb != 128 && pin_sb != 256) || pin_st < 1 || pin_st > 16 || (pin_sm != 2 && pin_sm != 3))
-        throw arg_error("HEOMGB_TILE=sites:<128|256>x<1..16>x<2|3>");
+      const int got = std::sscanf(env + 6, "%dx%dx%dx%d", &pin_sb, &pin_st, &pin_sm, &pin_sr);
+      if (got == 3) pin_sr = (pin_sm == 2 && pin_sb <= 256) ? 4 : 2;
+      if (got < 3 || pin_sb % 32 || pin_st < 1 || pin_st > 16 || !sites_variant(pin_sr, pin_sm, pin_sb))
+        throw arg_error("HEOMGB_TILE=sites:<block>x<1..16 ADOs per tile>x<CTAs per SM>[x<rows 4|2>]: 4 rows with "
+                        "2 CTAs of <= 256 threads; 2 rows with 3 or 4 CTAs of <= 256 or 2 CTAs of 288..384");
     } else {
       const int got = std::sscanf(env, "%dx%dx%d", &pin_b, &pin_e, &pin_m);
       if (got < 2 || (pin_b != 64 && pin_b != 128 && pin_b != 256) || pin_e < 1 || pin_e > 8 ||
@@ -1256,33 +1287,46 @@ void autotune(heomgb_qme_solver* qs) {
     if (std::string(env) == "0") sites_ok = false;
   if (pin_sb && !sites_ok) throw unsupported_error("HEOMGB_TILE=sites: the site-local-bath kernel does not apply");
   bool best_sites = false;
-  int best_sb = 256, best_st = 1, best_sm = 2;
+  int best_sb = 256, best_st = 1, best_sm = 2, best_sr = 4;
   if (sites_ok && !pin_tc && (pin_sb || !pin_b)) {
-    const int groups_per_ado = insts[0].n2 / 4;
-    for (int b : {128, 256})
-      for (int m : {2, 3})
-        for (int t : {1, 2, 3, 4, 6, 8, 12, 16}) {
-          if (pin_sb && (b != pin_sb || t != pin_st || m != pin_sm)) continue;
-          // a tile gives each thread one to eight micro-tiles
-          if (!pin_sb && (t * groups_per_ado < b / 2 || t * groups_per_ado > 8 * b)) continue;
-          if (!pin_sb && t > 1 && (t - 1) * groups_per_ado >= 8 * b) continue;
-          if (sites_smem(insts[0].n2, insts[0].K, t, insts[0].site_w) * m > 220 * 1024) continue;
+    // a thread owns an R x 4 block of an ADO (R = 4 or 2 rows): n^2 / (4 R) per ADO
+    struct SV {
+      int rt, minb;
+      std::vector<int> blocks;
+    };
+    std::vector<SV> variants = {{4, 2, {128, 192, 256}}, {2, 3, {128, 192, 256}}, {2, 4, {128, 192, 256}},
+                                {2, 2, {288, 320, 384}}};
+    if (pin_sb) variants = {{pin_sr, pin_sm, {pin_sb}}};
+    for (const SV& v : variants)
+      for (int b : v.blocks) {
+        const int per_ado = (insts[0].n / v.rt) * (insts[0].n / 4);
+        for (int t = 1; t <= 16; ++t) {
+          if (pin_sb && t != pin_st) continue;
+          const int nq = t * per_ado, waves = (nq + b - 1) / b;
+          // every thread busy in at least 85% of the passes over a tile
+          if (!pin_sb && (nq < b / 2 || nq > 4 * b || nq < 0.85 * waves * b)) continue;
+          if (sites_smem(insts[0].n, insts[0].K, t, insts[0].site_w) * v.minb > 220 * 1024) continue;
           try {
-            build_plan(qs->plan, insts, b, 1, m, qs->mixed, q->n_sm, qs->stream, false, t);
+            build_plan(qs->plan, insts, b, 1, v.minb, qs->mixed, q->n_sm, qs->stream, false, t, v.rt);
           } catch (const unsupported_error&) {
             continue;
           }
           const float ms = pin_sb ? 0.f : time_plan(b);
-          log_shape("sites (x = ADOs per tile)", b, t, m, ms);
+          if (tune_log)
+            std::fprintf(stderr, "heomgb tune: sites rows %d block %d tile %d min_blocks %d: %.4f ms per launch\n",
+                         v.rt, b, t, v.minb, ms / 3.f);
           if (pin_sb || ms < best) {
             best = ms;
             best_sites = true;
             best_sb = b;
             best_st = t;
-            best_sm = m;
+            best_sm = v.minb;
+            best_sr = v.rt;
           }
         }
+      }
   }
+  if (pin_sb && !best_sites) throw unsupported_error("HEOMGB_TILE=sites: the pinned shape does not fit");
   const int blocks[3] = {64, 128, 256}, epts[4] = {1, 2, 4, 8};
   const int n_minb = qs->mixed ? 3 : 1, minbs[3] = {1, 3, 4};
   for (int b : blocks)
@@ -1316,7 +1360,7 @@ void autotune(heomgb_qme_solver* qs) {
   cudaEventDestroy(e1);
   qs->stage_ms = best < 1e29f ? best / 3.f : 0.f;
   if (best_sites)
-    build_plan(qs->plan, insts, best_sb, 1, best_sm, qs->mixed, q->n_sm, qs->stream, false, best_st);
+    build_plan(qs->plan, insts, best_sb, 1, best_sm, qs->mixed, q->n_sm, qs->stream, false, best_st, best_sr);
   else if (best_tc)
     build_plan(qs->plan, insts, best_tc_b, 1, best_tc_m, qs->mixed, q->n_sm, qs->stream, true);
   else

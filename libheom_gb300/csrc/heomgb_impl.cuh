@@ -167,6 +167,9 @@ struct DiagInst {
   int site_w;               // entries per ADO (max(1, min(K, max_depth)))
   const int4* site_rec;     // nh * (1 + site_w)
   const float2* site_cm3;   // K * 3
+  const float2* site_cp2;   // K * 2: the +1 coefficient of mode k in its site's row / column
+  const int* site_ptr;      // n + 1: the modes of site s are site_modes[site_ptr[s] .. site_ptr[s+1])
+  const int* site_modes;    // K, per site in increasing k
 };
 struct DiagTile {
   int inst, l0, nt, pad;
@@ -183,7 +186,8 @@ struct DiagSet {
   int sites;                // 1: the site-local-bath kernel (k_rhs_sites; one instance, mixed form)
   int sites_tile;           // its ADOs per tile
   int sites_hreal;          // its instance has a real H
-  int sites_minb;           // its resident-CTA variant (2 or 3)
+  int sites_minb;           // its resident CTAs per SM (2, 3 or 4)
+  int sites_rt;             // its rows per register block (4 or 2)
 };
 
 // Resident intervals (k_dp_resident: Dormand-Prince; k_rk4_resident and
@@ -206,7 +210,8 @@ struct ResidentArgs {
   long long n_steps;        // RK4, LSRK4: steps of dt_step before the last step of dt_last
   double dt_step, dt_last;
   int ados_per_cta;
-  int pad_;
+  int skip_arrive_cta;      // fault injection for tests: this CTA never arrives at a grid barrier (-1: none)
+  long long spin_limit;     // polls before a grid-barrier wait gives up (2^24 in normal use)
 };
 // the resident kernels: Dormand-Prince, fixed-step RK4, fixed-step LSRK4
 constexpr int kResidentDp = 0, kResidentRk4 = 1, kResidentLs = 2;
@@ -262,7 +267,8 @@ int tc_tmem_cols(int n);
 // a CTA, set-up of the per-ADO records, and the launch (mixed form, FP32 stage
 // input).
 bool sites_eligible(const DiagInst& I, bool mixed);
-size_t sites_smem(int n2, int K, int tile, int w);
+size_t sites_smem(int n, int K, int tile, int w);
+bool sites_variant(int rows, int min_blocks, int block);  // a compiled (rows, CTAs per SM, CTA size) variant
 cudaError_t launch_site_records(const DiagInst& I, const int* msite, int4* rec, cudaStream_t s);
 cudaError_t launch_sites(const DiagSet& ds, const Stage& st, int grid, int block, cudaStream_t s);
 

@@ -668,14 +668,16 @@ __global__ void __launch_bounds__(256, MINB) k_rhs_diag_tc(const DiagSet ds, con
 // then the CTA syncs.  bar[0] is the counter, bar[16] the failure flag (its
 // own 128-byte line); both zero at launch.  The spin is bounded; grid_wait
 // returns false, CTA-uniformly, if it ran out.
-__device__ __forceinline__ void grid_arrive(unsigned long long* bar) {
+__device__ __forceinline__ void grid_arrive(unsigned long long* bar, const ResidentArgs& R) {
   __syncthreads();
-  if (threadIdx.x == 0) {
+  // R.skip_arrive_cta: fault injection for tests (that CTA never arrives, so
+  // every wait after it runs out); -1 in normal use
+  if (threadIdx.x == 0 && static_cast<int>(blockIdx.x) != R.skip_arrive_cta) {
     const unsigned long long one = 1;
     asm volatile("red.release.gpu.global.add.u64 [%0], %1;\n" ::"l"(bar), "l"(one) : "memory");
   }
 }
-__device__ bool grid_wait(unsigned long long* bar, unsigned long long& gen) {
+__device__ bool grid_wait(unsigned long long* bar, unsigned long long& gen, long long spin_limit) {
   __shared__ int s_ok;
   if (threadIdx.x == 0) {
     int ok = 1;
@@ -684,7 +686,7 @@ __device__ bool grid_wait(unsigned long long* bar, unsigned long long& gen) {
       unsigned long long v;
       asm volatile("ld.acquire.gpu.global.u64 %0, [%1];\n" : "=l"(v) : "l"(bar) : "memory");
       if (v >= target) break;
-      if (it >= (1 << 24)) {
+      if (it >= spin_limit) {
         ok = 0;
         atomicOr(bar + 16, 1ull);
         break;
@@ -905,7 +907,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
       // the other CTAs' stage input: wait for their stage s - 1 (stage 1 reads
       // the state copy, complete before the attempt)
       if (s > 0) {
-        ok = grid_wait(R.bar, gen);
+        ok = grid_wait(R.bar, gen, R.spin_limit);
         if (!ok) break;
       }
       res_bath<EPT>(Xg, Toff, Tcf, E, D);
@@ -963,13 +965,13 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
           local_f += (ex * ex + ey * ey) / (sm * sm);  // the thread's terms in FP32, then FP64
         }
       }
-      if (s < 6) grid_arrive(R.bar);
+      if (s < 6) grid_arrive(R.bar, R);
     }
     if (!ok) break;
     const double part = block_sum(f2d(local_f));
     if (threadIdx.x == 0) R.partials[blockIdx.x] = part;
-    grid_arrive(R.bar);
-    ok = grid_wait(R.bar, gen);
+    grid_arrive(R.bar, R);
+    ok = grid_wait(R.bar, gen, R.spin_limit);
     if (!ok) break;
     double v = 0.0;
     for (int i = threadIdx.x; i < static_cast<int>(gridDim.x); i += blockDim.x) v += __ldcg(R.partials + i);
@@ -1036,7 +1038,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
       float2 D[EPT];
       res_own<HREAL, EPT>(Hs, Xs, n, n2, E, el, D);
       if (step > 0 || s > 0) {  // the other CTAs' stage input (or new state) of the last stage
-        ok = grid_wait(R.bar, gen);
+        ok = grid_wait(R.bar, gen, R.spin_limit);
         if (!ok) break;
       }
       res_bath<EPT>(Xg, Toff, Tcf, E, D);
@@ -1068,7 +1070,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
           R.Yb[0][g] = f;
         }
       }
-      grid_arrive(R.bar);
+      grid_arrive(R.bar, R);
     }
   }
   if (ok)
@@ -1218,7 +1220,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident64(const R
         D[r] = Dv;
       }
       if (step > 0 || s > 0) {  // the other CTAs' stage input (or new state) of the last stage
-        ok = grid_wait(R.bar, gen);
+        ok = grid_wait(R.bar, gen, R.spin_limit);
         if (!ok) break;
       }
       double2 vv[EPT][kResidentTerms];  // all gathers first (L1-bypassing: written until the wait returned)
@@ -1256,7 +1258,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident64(const R
           S[g] = v;
         }
       }
-      grid_arrive(R.bar);
+      grid_arrive(R.bar, R);
     }
   }
 }
@@ -1303,7 +1305,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_ls_resident(const Resi
       float2 D[EPT];
       res_own<HREAL, EPT>(Hs, Yf, n, n2, E, el, D);  // all reads of Yf end before the wait's sync
       if (step > 0 || s > 0) {
-        ok = grid_wait(R.bar, gen);
+        ok = grid_wait(R.bar, gen, R.spin_limit);
         if (!ok) break;
       }
       res_bath<EPT>(Xg, Toff, Tcf, E, D);
@@ -1326,7 +1328,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_ls_resident(const Resi
         Yf[le] = f;
         R.Yb[1 - (s & 1)][gb + le] = f;
       }
-      grid_arrive(R.bar);
+      grid_arrive(R.bar, R);
     }
   }
   if (ok)

@@ -1,7 +1,7 @@
 """The stage kernel for site-local baths (k_rhs_sites: per-ADO lists of
-occupied modes, commutators in registers, compile-time stage epilogues,
-cp.async-staged tiles) against the general diagonal-coupling stage kernel
-(k_rhs_diag) on the same models and solvers.
+occupied modes, 4 x 4 register blocks of the commutator, compile-time stage
+epilogues, cp.async-staged tiles) against the general diagonal-coupling stage
+kernel (k_rhs_diag) on the same models and solvers.
 
 Both do the same per-element arithmetic in the same order, so the states
 must agree bit for bit (the new kernel skips terms without a neighbour that
@@ -48,7 +48,6 @@ def complex_h(p):
 CASES = {
     "agg8_depth4": lambda: configs.aggregate_24site(n_sites=8, depth=4),
     "agg12_sqrt": lambda: dataclasses.replace(configs.aggregate_24site(n_sites=12, depth=3), normalization="sqrt"),
-    "agg8_complex_h": lambda: complex_h(configs.aggregate_24site(n_sites=8, depth=3)),
     "agg8_filtered": lambda: dataclasses.replace(configs.aggregate_24site(n_sites=8, depth=4),
                                                  hrchy_filter=lambda idx, d: idx[0] <= 1 and d <= 3 + (idx[1] == 0)),
 }
@@ -73,7 +72,7 @@ def test_sites_kernel_bit_identical_to_stage_kernel(case, solver, monkeypatch):
     assert np.array_equal(got, ref)
 
 
-@pytest.mark.parametrize("shape", ["128x1x2", "256x3x3", "128x4x3", "256x8x2"])
+@pytest.mark.parametrize("shape", ["128x1x2", "256x3x3", "128x4x3", "256x8x2", "288x8x2", "64x5x2", "256x4x4", "256x2x2x4"])
 def test_sites_kernel_tile_shapes(shape, monkeypatch):
     """Every tile shape gives the same bits (the tile only moves work between CTAs)."""
     p = configs.aggregate_24site(n_sites=8, depth=4)
@@ -82,6 +81,17 @@ def test_sites_kernel_tile_shapes(shape, monkeypatch):
     ref, _, _ = run(p, "lsrk4", t, kw, monkeypatch, False)
     assert tune["sites"]
     assert np.array_equal(got, ref)
+
+
+def test_complex_hamiltonian_keeps_the_general_kernel(monkeypatch):
+    """The site-local-bath kernel takes real H only; pinning it for a complex H
+    is refused and the autotuner leaves it out."""
+    p = complex_h(configs.aggregate_24site(n_sites=8, depth=3))
+    monkeypatch.setenv("HEOMGB_TILE", "sites:256x2x2")
+    with pytest.raises(lh.HeomError):
+        lh.qme_solver(lh.from_params(p, precision="mixed"), lh.lsrk4())
+    monkeypatch.delenv("HEOMGB_TILE")
+    assert not lh.qme_solver(lh.from_params(p, precision="mixed"), lh.lsrk4()).tuning()["sites"]
 
 
 def test_sites_kernel_24site_vs_oracle(monkeypatch):

@@ -229,8 +229,7 @@ bool tcore_eligible(const DiagInst& I, bool mixed) {
 }
 
 void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int ept, int min_blocks, bool mixed,
-                int n_sm, cudaStream_t s, bool tcore = false, int sites_tile = 0, int sites_rt = 4,
-                bool sites_epi = false) {
+                int n_sm, cudaStream_t s, bool tcore = false, int sites_tile = 0, int sites_rt = 4) {
   P.arena.release();
   P.inst = insts;
   std::vector<DiagTile> tiles;
@@ -246,7 +245,7 @@ void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int 
   if (sites_tile > 0) {
     if (insts.size() != 1 || !sites_eligible(insts[0], mixed) || !sites_variant(sites_rt, min_blocks, block))
       throw unsupported_error("site-local-bath kernel: one eligible instance and a compiled variant");
-    if (sites_smem(insts[0].n, insts[0].K, sites_tile, insts[0].site_w, sites_epi) > cap)
+    if (sites_smem(insts[0].n, insts[0].K, sites_tile, insts[0].site_w) > cap)
       throw unsupported_error("site-local-bath tile exceeds shared memory");
   }
   for (size_t i = 0; i < P.inst.size(); ++i) {
@@ -254,7 +253,7 @@ void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int 
     int tile;
     if (sites_tile > 0) {
       tile = sites_tile;
-      smem = sites_smem(I.n, I.K, tile, I.site_w, sites_epi);
+      smem = sites_smem(I.n, I.K, tile, I.site_w);
     } else if (tcore) {  // the tile is fixed by the GEMM shape (4 n rows per ADO, 128-row blocks)
       tile = tc_tile(I.n);
       if (diag_tile_smem_tc(I.n, I.K, tile) > cap) throw unsupported_error("tensor-core tile exceeds shared memory");
@@ -1289,8 +1288,6 @@ void autotune(heomgb_qme_solver* qs) {
   if (pin_sb && !sites_ok) throw unsupported_error("HEOMGB_TILE=sites: the site-local-bath kernel does not apply");
   bool best_sites = false;
   int best_sb = 256, best_st = 1, best_sm = 2, best_sr = 4;
-  // fixed-step solvers' epilogue sources are staged in shared memory
-  const bool sites_epi = qs->kind == HEOMGB_RK4 || qs->kind == HEOMGB_LSRK4;
   if (sites_ok && !pin_tc && (pin_sb || !pin_b)) {
     // a thread owns an R x 4 block of an ADO (R = 4 or 2 rows): n^2 / (4 R) per ADO
     struct SV {
@@ -1308,9 +1305,9 @@ void autotune(heomgb_qme_solver* qs) {
           const int nq = t * per_ado, waves = (nq + b - 1) / b;
           // every thread busy in at least 85% of the passes over a tile
           if (!pin_sb && (nq < b / 2 || nq > 4 * b || nq < 0.85 * waves * b)) continue;
-          if (sites_smem(insts[0].n, insts[0].K, t, insts[0].site_w, sites_epi) * v.minb > 220 * 1024) continue;
+          if (sites_smem(insts[0].n, insts[0].K, t, insts[0].site_w) * v.minb > 220 * 1024) continue;
           try {
-            build_plan(qs->plan, insts, b, 1, v.minb, qs->mixed, q->n_sm, qs->stream, false, t, v.rt, sites_epi);
+            build_plan(qs->plan, insts, b, 1, v.minb, qs->mixed, q->n_sm, qs->stream, false, t, v.rt);
           } catch (const unsupported_error&) {
             continue;
           }
@@ -1363,8 +1360,7 @@ void autotune(heomgb_qme_solver* qs) {
   cudaEventDestroy(e1);
   qs->stage_ms = best < 1e29f ? best / 3.f : 0.f;
   if (best_sites)
-    build_plan(qs->plan, insts, best_sb, 1, best_sm, qs->mixed, q->n_sm, qs->stream, false, best_st, best_sr,
-               sites_epi);
+    build_plan(qs->plan, insts, best_sb, 1, best_sm, qs->mixed, q->n_sm, qs->stream, false, best_st, best_sr);
   else if (best_tc)
     build_plan(qs->plan, insts, best_tc_b, 1, best_tc_m, qs->mixed, q->n_sm, qs->stream, true);
   else

@@ -267,8 +267,7 @@ int tc_tmem_cols(int n);
 // a CTA, set-up of the per-ADO records, and the launch (mixed form, FP32 stage
 // input).
 bool sites_eligible(const DiagInst& I, bool mixed);
-// smem_epi: room for the fixed-step epilogues' sources (RK4 and LSRK4 solvers)
-size_t sites_smem(int n, int K, int tile, int w, bool smem_epi);
+size_t sites_smem(int n, int K, int tile, int w);
 bool sites_variant(int rows, int min_blocks, int block);  // a compiled (rows, CTAs per SM, CTA size) variant
 cudaError_t launch_site_records(const DiagInst& I, const int* msite, int4* rec, cudaStream_t s);
 cudaError_t launch_sites(const DiagSet& ds, const Stage& st, int grid, int block, cudaStream_t s);

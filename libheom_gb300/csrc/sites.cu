@@ -119,81 +119,6 @@ __device__ __forceinline__ void sites_stage(const DiagInst& I, const float2* y, 
   }
 }
 
-// The fixed-step stage epilogues (RK4 stages, LSRK4) read at most one FP64 and
-// one FP32 vector per element; the kernel copies the tile's part of both into
-// shared memory (at padded ADO strides) while the commutator runs.
-template <int KIND>
-struct SmemEpi {
-  static constexpr bool on = KIND == EPI_RK4_1 || KIND == EPI_RK4_2 || KIND == EPI_RK4_3 || KIND == EPI_RK4_4 ||
-                             KIND == EPI_LS;
-};
-__host__ __device__ __forceinline__ int sites_e1_stride(int n2) { return n2 + 1; }  // double2 units (16-byte pad)
-__host__ __device__ __forceinline__ int sites_e2_stride(int n2) { return n2 + 2; }  // float2 units (16-byte pad)
-__host__ __device__ __forceinline__ size_t sites_epi_bytes(int n2, int tile) {
-  return static_cast<size_t>(tile) * (sizeof(double2) * sites_e1_stride(n2) + sizeof(float2) * sites_e2_stride(n2));
-}
-// what epi_pre<float, KIND> reads: v1 (FP64, may be null) and v2 (FP32, may be null)
-template <int KIND>
-__device__ __forceinline__ void epi_sources(const Stage& st, const double2*& v1, const float2*& v2) {
-  v1 = nullptr;
-  v2 = nullptr;
-  if (KIND == EPI_RK4_1) {
-    v1 = st.S[0];
-    v2 = static_cast<const float2*>(st.Yb[0]);
-  } else if (KIND == EPI_RK4_2 || KIND == EPI_RK4_3) {
-    v1 = st.acc;
-    v2 = static_cast<const float2*>(st.Yb[0]);
-  } else if (KIND == EPI_RK4_4) {
-    v1 = st.acc;
-  } else if (KIND == EPI_LS) {
-    v1 = st.S[st.ls_in];
-    if (!st.ls_first) v2 = reinterpret_cast<const float2*>(st.acc);  // the FP32 buffer
-  }
-}
-// epi_pre<float, KIND>'s values, read from the shared-memory copies
-template <int KIND>
-__device__ __forceinline__ EpiPre epi_pre_smem(const Stage& st, const double2* e1, const float2* e2, int i1, int i2) {
-  EpiPre p;
-  p.a = make_double2(0.0, 0.0);
-  p.b = make_double2(0.0, 0.0);
-  p.f = make_float2(0.f, 0.f);
-  p.g = make_float2(0.f, 0.f);
-  p.m = 0.0;
-  if (KIND == EPI_RK4_1 || KIND == EPI_RK4_2 || KIND == EPI_RK4_3) {
-    p.a = e1[i1];
-    p.f = e2[i2];
-  } else if (KIND == EPI_RK4_4) {
-    p.a = e1[i1];
-  } else if (KIND == EPI_LS) {
-    if (!st.ls_first) p.f = e2[i2];
-    p.b = e1[i1];
-  }
-  return p;
-}
-// cp.async copies of the epilogue sources of ADOs l0 .. l0+nt-1 into e1 / e2
-template <int KIND>
-__device__ __forceinline__ void sites_stage_epi(const Stage& st, int n2, int l0, int nt, double2* e1, float2* e2) {
-  const double2* v1;
-  const float2* v2;
-  epi_sources<KIND>(st, v1, v2);
-  if (v1) {
-    const double2* src = v1 + static_cast<size_t>(l0) * n2;
-    const int s1 = sites_e1_stride(n2), cnt = nt * n2;
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-      const int lt = i / n2, e = i - lt * n2;
-      cp16(e1 + static_cast<size_t>(lt) * s1 + e, src + i);
-    }
-  }
-  if (v2) {
-    const float2* src = v2 + static_cast<size_t>(l0) * n2;
-    const int s2 = sites_e2_stride(n2), half = n2 / 2, cnt = nt * half;
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-      const int lt = i / half, r = i - lt * half;
-      cp16(e2 + static_cast<size_t>(lt) * s2 + 2 * r, src + 2 * i);
-    }
-  }
-}
-
 __device__ __forceinline__ float2 f4lo(float4 v) { return make_float2(v.x, v.y); }
 __device__ __forceinline__ float2 f4hi(float4 v) { return make_float2(v.z, v.w); }
 __device__ __forceinline__ float f4at(float4 v, int j) { return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w; }
@@ -218,9 +143,6 @@ __global__ void __launch_bounds__(MAXT, MINB) k_rhs_sites(const DiagSet ds, cons
   const bool sqn = I.sqrt_norm != 0;
   const float2* __restrict__ y = stage_input<float2>(st, cur);
   const SitesSmem L = sites_layout(smem_raw, n, K, tile, w);
-  constexpr bool SE = SmemEpi<KIND>::on;
-  double2* e1 = reinterpret_cast<double2*>(L.buf0 + 2 * L.bsz);  // SE only
-  float2* e2 = reinterpret_cast<float2*>(e1 + static_cast<size_t>(tile) * sites_e1_stride(n2));
   const int n_tiles = ds.n_tiles;
   int t = blockIdx.x;
   if (t < n_tiles) sites_stage(I, y, tile, t * tile, min(tile, I.nh - t * tile), L.buf0);
@@ -239,32 +161,20 @@ __global__ void __launch_bounds__(MAXT, MINB) k_rhs_sites(const DiagSet ds, cons
   double local = 0.0;
   int bsel = 0;
   for (; t < n_tiles; t += gridDim.x) {
-    const int l0 = t * tile, nt = min(tile, I.nh - l0);
-    // copy groups in commit order: [this tile's stage input], its epilogue
-    // sources (SE), the next tile's stage input
-    if (SE) {
-      sites_stage_epi<KIND>(st, n2, l0, nt, e1, e2);
-      cp_commit();
-    }
     const int tn = t + gridDim.x;
     if (tn < n_tiles) sites_stage(I, y, tile, tn * tile, min(tile, I.nh - tn * tile), L.buf0 + (bsel ^ 1) * L.bsz);
     cp_commit();
-    if (SE)
-      cp_wait<2>();  // this tile's stage input (the epilogue sources and the next tile may still be in flight)
-    else
-      cp_wait<1>();
+    cp_wait<1>();  // this tile's copies (the next tile's may still be in flight)
     __syncthreads();
+    const int l0 = t * tile, nt = min(tile, I.nh - l0);
     const float2* yt = reinterpret_cast<const float2*>(L.buf0 + bsel * L.bsz);
     const int4* rec = reinterpret_cast<const int4*>(yt + static_cast<size_t>(tile) * sy);
     const int* p1s = reinterpret_cast<const int*>(rec + static_cast<size_t>(tile) * w1);
     const int* nks = p1s + static_cast<size_t>(tile) * K;
     const int nq = nt * nr * nb;
-    for (int q0 = 0; q0 < nq; q0 += blockDim.x) {  // uniform trip count: every thread reaches the barrier below
-      const int q = q0 + threadIdx.x;
-      const bool act = q < nq;
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
       // q = (A * nt + lt) * nb + B: the lanes of a warp mostly share A
-      const int qq = act ? q : 0;
-      const int B = qq % nb, r = qq / nb, lt = r % nt, A = r / nt;
+      const int B = q % nb, r = q / nb, lt = r % nt, A = r / nt;
       const int a0 = A * RT, b0 = B << 2, l = l0 + lt;
       const float2* yl = yt + static_cast<size_t>(lt) * sy;
       // -i[H, rho]: acc = H rho - rho H, k_rhs_diag's order over c
@@ -300,11 +210,6 @@ __global__ void __launch_bounds__(MAXT, MINB) k_rhs_sites(const DiagSet ds, cons
           }
         }
       }
-      if (SE && q0 == 0) {  // the epilogue sources of the tile, visible to every thread
-        cp_wait<1>();
-        __syncthreads();
-      }
-      if (!act) continue;
       const int4 hdr = rec[lt * w1];  // {occupied modes, any +1 neighbour, ngd bits}
       const float2 gl = make_float2(__int_as_float(hdr.z), __int_as_float(hdr.w));
       const int* p1r = p1s + lt * K;
@@ -313,14 +218,9 @@ __global__ void __launch_bounds__(MAXT, MINB) k_rhs_sites(const DiagSet ds, cons
       for (int i = 0; i < RT; ++i) {
         const int a = a0 + i, e0 = a * n + b0;
         const size_t g0 = static_cast<size_t>(l) * n2 + e0;
-        EpiPre pre[4];  // the row's epilogue inputs (global loads in flight while its terms are added)
+        EpiPre pre[4];  // the row's epilogue loads, in flight while its terms are added
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          if (SE)
-            pre[j] = epi_pre_smem<KIND>(st, e1, e2, lt * sites_e1_stride(n2) + e0 + j, lt * sites_e2_stride(n2) + e0 + j);
-          else
-            pre[j] = epi_pre<float, KIND>(st, g0 + j, cur);
-        }
+        for (int j = 0; j < 4; ++j) pre[j] = epi_pre<float, KIND>(st, g0 + j, cur);
         float2 D[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) D[j] = make_float2(-acc[i][j].y, acc[i][j].x);
@@ -465,9 +365,7 @@ bool sites_eligible(const DiagInst& I, bool mixed) {
          !I.term_p;
 }
 
-size_t sites_smem(int n, int K, int tile, int w, bool smem_epi) {
-  return sites_head_bytes(n, K) + 2 * sites_buf_bytes(n, K, tile, w) + (smem_epi ? sites_epi_bytes(n * n, tile) : 0);
-}
+size_t sites_smem(int n, int K, int tile, int w) { return sites_head_bytes(n, K) + 2 * sites_buf_bytes(n, K, tile, w); }
 
 bool sites_variant(int rt, int minb, int block) {
   if (rt == 4) return minb == 2 && block <= 256;

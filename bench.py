@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--form", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 comparison run (profiling)")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the bounded 24-site secondary measurement of the default workload")
     ap.add_argument("--t-final", type=float, default=None,
                     help="propagate to this time instead of the workload's (short profiling runs)")
     args = ap.parse_args()
@@ -311,6 +313,67 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def secondary_aggregate24(stream, fma_peaks, steps=3):
+    """The 24-site aggregate (n=24, K=48, depth 3, 20825 ADOs), LSRK4 dt = 0.5 fs,
+    on a bounded sample of its 2000-step run: 100 steps (t = 0..50 fs) per solve,
+    both forms, the state resident in HBM, L2 flushed between solves.  Reports
+    ADO-updates/s, the stage kernel's time per launch and its HBM roofline."""
+    import torch
+
+    import libheom_gb300 as lh
+    from libheom_gb300 import configs, roofline
+    p = configs.aggregate_24site()
+    N = p.n_hrchy() * p.n_level ** 2
+    rho0 = torch.from_numpy(p.rho0_ground().ravel()).cuda()
+    rho = torch.empty_like(rho0)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    peak, peak_kind = measured_peaks()
+    out = {"workload": "aggregate24 (n=24, K=48, depth 3, 20825 ADOs), lsrk4 dt=0.5",
+           "sample": "100 steps (t = 0..50 fs) of the 2000-step run per solve", "solves_timed": steps}
+    for form in ("mixed", "fp64"):
+        qs = lh.qme_solver(lh.from_params(p, precision=form, stream=stream.cuda_stream), lh.lsrk4())
+        t_list = [0.0, 50.0]
+
+        def solve():
+            with torch.cuda.stream(stream):
+                rho.copy_(rho0)
+            qs.solve_device(rho.data_ptr(), t_list, None, {"dt": 0.5})
+
+        solve()  # warm-up (graph capture)
+        ms, busy, rhs = [], 0.0, 0
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            solve()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            busy += qs.timing()["busy_ms"]
+            rhs += qs.stats()["rhs"]
+        upd = qs.stats()["ado_updates"]
+        avg_s = 1e-3 * busy / max(rhs, 1)
+        bpe, per_unit = roofline.bytes_per_element("lsrk4", form == "mixed")
+        alg = bpe * N / per_unit
+        tune = qs.tuning()
+        entry = {"value": upd / (statistics.median(ms) / 1e3), "unit": "ADO-updates/s",
+                 "ms_per_solve": statistics.median(ms), "avg_stage_kernel_us": 1e6 * avg_s,
+                 "kernel": "k_rhs_sites" if tune.get("sites") else "k_rhs_diag", "tuning": tune}
+        if form == "mixed":
+            entry["roofline"] = {"bound": "hbm", "achieved": alg / avg_s / 1e9, "peak": peak, "unit": "GB/s",
+                                 "frac": alg / avg_s / 1e9 / peak, "peak_source": peak_kind,
+                                 "alg_bytes_per_launch": alg, "traffic": profile_traffic("aggregate24", "mixed")}
+        else:
+            fl = roofline.flops_per_element(p) * N / avg_s / 1e12
+            entry["roofline"] = {"bound": "fp64 pipe", "achieved": fl, "peak": fma_peaks[0], "unit": "TFLOP/s",
+                                 "frac": fl / fma_peaks[0], "peak_source": "measured (heomgb_probe_fma_peaks)"}
+        out[form] = entry
+        qs.close()
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -463,7 +526,8 @@ def run_ours(args):
                   "inputs in shared memory, no grid-wide synchronisation)"
                   + ("" if all(t.get("local", False) for t in part_tunings) else "; k_rhs_diag for the other part"))
     else:
-        kernel = "k_rhs_diag (fused RHS + stage epilogue)"
+        kernel = ("k_rhs_sites (site-local baths: fused RHS + stage epilogue)"
+                  if any(t.get("sites", False) for t in part_tunings) else "k_rhs_diag (fused RHS + stage epilogue)")
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": profile_traffic(args.workload, args.form), "peak_source": peak_kind,
             "kernel": kernel,
@@ -489,6 +553,8 @@ def run_ours(args):
             "max_abs_err_vs_fp64": max_err, "plain_fp64": plain, "tuning": tuning,
             "attempts_per_step": rhs // max(1, args.steps) // per_rhs,
             "gpu_launches": launches, "e2e": e2e, "roofline": roof, "clocks": clocks}
+    if rank == 0 and world == 1 and args.workload == "exciton7" and not args.no_secondary:
+        line["secondary"] = {"aggregate24": secondary_aggregate24(stream, fma_peaks)}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(w, keep_states=True)
         sample = cb.pop("_final")

@@ -317,54 +317,6 @@ __device__ __forceinline__ EpiPre epi_pre(const Stage& st, size_t g, int cur) {
   return p;
 }
 
-// Bulk L2 prefetch of [p, p + bytes) (bytes a multiple of 16, p 16-byte aligned).
-__device__ __forceinline__ void l2_prefetch(const void* p, uint32_t bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(p), "r"(bytes) : "memory");
-}
-
-// Prefetches into L2 what epi_pre<float, KIND> will read for the elements
-// [g, g + count) (mixed form; g and count even): one bulk prefetch per vector,
-// issued by the threads slot, slot + stride, ... of the caller's choosing.
-template <int KIND>
-__device__ __forceinline__ void epi_prefetch_mixed(const Stage& st, size_t g, int count, int cur, int slot,
-                                                   int stride) {
-  const void* v[8];
-  uint32_t sz[8];
-  int nv = 0;
-  const uint32_t b8 = 8u * static_cast<uint32_t>(count), b16 = 16u * static_cast<uint32_t>(count);
-  auto add = [&](const void* base, uint32_t elem) {
-    v[nv] = static_cast<const unsigned char*>(base) + g * elem;
-    sz[nv] = elem == 8 ? b8 : b16;
-    ++nv;
-  };
-  if (KIND == EPI_RK4_1) {
-    add(st.S[0], 16);
-    add(st.Yb[0], 8);
-  } else if (KIND == EPI_RK4_2 || KIND == EPI_RK4_3) {
-    add(st.acc, 16);
-    add(st.Yb[0], 8);
-  } else if (KIND == EPI_RK4_4) {
-    add(st.acc, 16);
-  } else if (KIND == EPI_LS) {
-    if (!st.ls_first) add(st.acc, 8);
-    add(st.S[st.ls_in], 16);
-  } else if (KIND == EPI_DP) {
-    const int s_ = st.dp_stage;
-    if (s_ < 5) {
-      add(st.Yb[cur], 8);
-      for (int j = 0; j < s_; ++j) add(st.K[j], 8);
-    } else {
-      add(st.S[cur], 16);
-      for (int j = 0; j < 5; ++j) add(st.K[j], 8);
-    }
-  } else if (KIND == EPI_DP7) {
-    for (int j = 0; j < 6; ++j) add(st.K[j], 8);
-    add(st.Yb[1 - cur], 8);
-    add(st.Yb[cur], 8);
-  }
-  for (int i = slot; i < nv; i += stride) l2_prefetch(v[i], sz[i]);
-}
-
 template <typename TC, int KIND = -1>
 __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> Dc, double dt, int cur,
                                            const EpiPre& p) {

@@ -906,6 +906,8 @@ void build_model(heomgb_qme* q) {
         const int* dms = q->arena.upload(msite, s);
         di.site_cm3 = q->arena.upload(to_f2(cm3), s);
         di.site_cp2 = q->arena.upload(to_f2(cp2), s);
+        di.site_cm3_d = q->arena.upload(to_d2(cm3), s);
+        di.site_cp2_d = q->arena.upload(to_d2(cp2), s);
         di.site_ptr = q->arena.upload(sptr, s);
         di.site_modes = q->arena.upload(smodes, s);
         int4* rec = static_cast<int4*>(q->arena.alloc(sizeof(int4) * static_cast<size_t>(nh) * (1 + di.site_w)));
@@ -1077,7 +1079,10 @@ int resident_scheme(const heomgb_qme_solver* qs) {
 int resident_variant(const heomgb_qme_solver* qs) {
   const int scheme = resident_scheme(qs);
   if (qs->mixed) return scheme;
-  return scheme == kResidentRk4 ? kResidentRk4F64 : -1;
+  if (scheme == kResidentRk4) return kResidentRk4F64;
+  // the FP64 Dormand-Prince interval reads the site-local records
+  if (scheme == kResidentDp && qs->q->dinst.site_local && qs->q->dinst.site_rec) return kResidentDpF64;
+  return -1;
 }
 
 // Arguments of the resident kernels for the solver's buffers and its tuned shape.
@@ -1408,7 +1413,7 @@ void plan_resident(heomgb_qme_solver* qs) {
       const int apc = (I.nh + target - 1) / target;
       const int grid = (I.nh + apc - 1) / apc;
       if (grid == last_grid) continue;
-      const size_t smem = resident_smem(I.n2, apc, variant);
+      const size_t smem = variant == kResidentDpF64 ? resident_dp64_smem(I, apc) : resident_smem(I.n2, apc, variant);
       if (smem > 200 * 1024) continue;
       const int E = apc * I.n2;  // ept elements per thread
       const int block = std::max(64, ((E + ept - 1) / ept + 31) / 32 * 32);
@@ -1864,7 +1869,7 @@ int solve_resident(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwa
   ck(launch_ctl_init(qs->ctl, t0, dt, t1, atol, rtol, cur, qs->stream), "ctl init");
   ck(cudaMemsetAsync(qs->res_bar, 0, kResidentBarWords * sizeof(unsigned long long), qs->stream), "barrier reset");
   busy_begin(qs);
-  const cudaError_t le = launch_resident(resident_args(qs), kResidentDp, qs->q->dinst.h_real != 0, qs->res_ept,
+  const cudaError_t le = launch_resident(resident_args(qs), resident_variant(qs), qs->q->dinst.h_real != 0, qs->res_ept,
                                          qs->res_grid, qs->res_block, qs->res_smem, qs->stream);
   if (le == cudaErrorCooperativeLaunchTooLarge) {
     // the device cannot hold the grid now (another context holds SMs or

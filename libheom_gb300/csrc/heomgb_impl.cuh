@@ -170,6 +170,8 @@ struct DiagInst {
   const float2* site_cp2;   // K * 2: the +1 coefficient of mode k in its site's row / column
   const int* site_ptr;      // n + 1: the modes of site s are site_modes[site_ptr[s] .. site_ptr[s+1])
   const int* site_modes;    // K, per site in increasing k
+  const double2* site_cm3_d;  // K * 3 and K * 2: the same coefficients in FP64 (the FP64 resident interval)
+  const double2* site_cp2_d;
 };
 struct DiagTile {
   int inst, l0, nt, pad;
@@ -216,6 +218,10 @@ struct ResidentArgs {
 // the resident kernels: Dormand-Prince, fixed-step RK4, fixed-step LSRK4
 constexpr int kResidentDp = 0, kResidentRk4 = 1, kResidentLs = 2;
 constexpr int kResidentRk4F64 = 4;  // fixed-step RK4 in the FP64 form (k_rk4_resident64)
+constexpr int kResidentDpF64 = 5;   // Dormand-Prince in the FP64 form, site-local baths (k_dp_resident64)
+// k_dp_resident64 (resident64.cu): shared memory of a CTA owning ados_per_cta ADOs, and its kernel instance
+size_t resident_dp64_smem(const DiagInst& I, int ados_per_cta);
+const void* resident_dp64_kernel(bool hreal, int ept);
 // smem of a CTA owning ados_per_cta ADOs in the given scheme's kernel
 size_t resident_smem(int n2, int ados_per_cta, int scheme);
 int resident_blocks_per_sm(int scheme, bool hreal, int ept, int block, size_t smem);

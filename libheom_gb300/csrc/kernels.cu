@@ -659,45 +659,6 @@ __global__ void __launch_bounds__(256, MINB) k_rhs_diag_tc(const DiagSet ds, con
 // its own copy of the controller state, so all CTAs take the same decisions
 // without a further exchange.  Grid barriers are bounded spins: one that runs
 // out sets the failure flag and the CTAs leave.
-// Grid barrier of a cooperative launch (every CTA resident), in the
-// arrive/wait pattern of CUTLASS's GenericBarrier, split in two so that a
-// CTA can work on its own data between them.  grid_arrive: the CTA syncs,
-// one thread adds 1 to a monotonic 64-bit arrival counter with release
-// semantics.  grid_wait: that thread spins with acquire loads until the
-// counter reaches (gen + 1) * gridDim.x (gen: barriers completed so far),
-// then the CTA syncs.  bar[0] is the counter, bar[16] the failure flag (its
-// own 128-byte line); both zero at launch.  The spin is bounded; grid_wait
-// returns false, CTA-uniformly, if it ran out.
-__device__ __forceinline__ void grid_arrive(unsigned long long* bar, const ResidentArgs& R) {
-  __syncthreads();
-  // R.skip_arrive_cta: fault injection for tests (that CTA never arrives, so
-  // every wait after it runs out); -1 in normal use
-  if (threadIdx.x == 0 && static_cast<int>(blockIdx.x) != R.skip_arrive_cta) {
-    const unsigned long long one = 1;
-    asm volatile("red.release.gpu.global.add.u64 [%0], %1;\n" ::"l"(bar), "l"(one) : "memory");
-  }
-}
-__device__ bool grid_wait(unsigned long long* bar, unsigned long long& gen, long long spin_limit) {
-  __shared__ int s_ok;
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    const unsigned long long target = (gen + 1) * gridDim.x;
-    for (int it = 0;; ++it) {
-      unsigned long long v;
-      asm volatile("ld.acquire.gpu.global.u64 %0, [%1];\n" : "=l"(v) : "l"(bar) : "memory");
-      if (v >= target) break;
-      if (it >= spin_limit) {
-        ok = 0;
-        atomicOr(bar + 16, 1ull);
-        break;
-      }
-    }
-    ++gen;
-    s_ok = ok;
-  }
-  __syncthreads();
-  return s_ok != 0;
-}
 
 // Per-thread element data of a resident kernel (fixed for the launch): the
 // thread's elements le = threadIdx.x + r * blockDim.x, r < EPT.
@@ -1349,6 +1310,7 @@ size_t resident_smem(int n2, int ados_per_cta, int scheme) {
 
 // the kernel instance for the scheme, H real or complex and EPT elements per thread
 static const void* resident_kernel(int scheme, bool hreal, int ept) {
+  if (scheme == kResidentDpF64) return resident_dp64_kernel(hreal, ept);
   switch (scheme * 8 + ept * 2 + (hreal ? 1 : 0)) {
     case 2: return reinterpret_cast<const void*>(k_dp_resident<false, 1>);
     case 3: return reinterpret_cast<const void*>(k_dp_resident<true, 1>);

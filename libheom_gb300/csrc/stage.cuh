@@ -268,13 +268,13 @@ __device__ __forceinline__ EpiPre epi_pre(const Stage& st, size_t g, int cur) {
           p.f = hi;
           p.g = lo;
         }
-      } else {
+      } else {  // explicit FMAs, shared with k_dp_resident64
         double2 y = __ldcs(st.S[cur] + g);
         for (int j = 0; j < s_; ++j) {
           const double c = c_dpA[s_ + 1][j];
           const double2 kj = ld_bulk_cs<TC>(st.K[j], g);
-          y.x += c * kj.x;
-          y.y += c * kj.y;
+          y.x = fma(c, kj.x, y.x);
+          y.y = fma(c, kj.y, y.y);
         }
         p.a = y;
       }
@@ -295,8 +295,8 @@ __device__ __forceinline__ EpiPre epi_pre(const Stage& st, size_t g, int cur) {
         double2 e = make_double2(c_dpE[0] * k0.x, c_dpE[0] * k0.y);
         for (int j = 1; j < 6; ++j) {
           const double2 kj = ld_bulk_cs<TC>(st.K[j], g);
-          e.x += c_dpE[j] * kj.x;
-          e.y += c_dpE[j] * kj.y;
+          e.x = fma(c_dpE[j], kj.x, e.x);
+          e.y = fma(c_dpE[j], kj.y, e.y);
         }
         p.a = e;
       }
@@ -307,7 +307,7 @@ __device__ __forceinline__ EpiPre epi_pre(const Stage& st, size_t g, int cur) {
       } else {
         const double2 x1 = __ldcs(st.S[1 - cur] + g);
         const double2 x2 = __ldcs(st.S[cur] + g);
-        p.m = fmax(x1.x * x1.x + x1.y * x1.y, x2.x * x2.x + x2.y * x2.y);
+        p.m = fmax(fma(x1.x, x1.x, x1.y * x1.y), fma(x2.x, x2.x, x2.y * x2.y));
       }
       break;
     }
@@ -409,8 +409,8 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
         st_bulk_cs<TC>(st.K[s_], g, k);
         double2 y = p.a;
         const double c = c_dpA[s_ + 1][s_];
-        y.x += c * k.x;
-        y.y += c * k.y;
+        y.x = fma(c, k.x, y.x);
+        y.y = fma(c, k.y, y.y);
         if (s_ < 5)
           st_bulk<TC>(st.Ynext, g, y);
         else
@@ -429,10 +429,10 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
       } else {
         const double2 k7 = make_double2(-dt * D.x, -dt * D.y);
         double2 e = p.a;
-        e.x += c_dpE[6] * k7.x;
-        e.y += c_dpE[6] * k7.y;
-        const double e2 = e.x * e.x + e.y * e.y;
-        const double s = st.ctl->atol + st.ctl->rtol * sqrt(p.m);
+        e.x = fma(c_dpE[6], k7.x, e.x);
+        e.y = fma(c_dpE[6], k7.y, e.y);
+        const double e2 = fma(e.x, e.x, e.y * e.y);
+        const double s = fma(st.ctl->rtol, sqrt(p.m), st.ctl->atol);
         return e2 / (s * s);
       }
     }
@@ -509,6 +509,46 @@ __device__ __forceinline__ bool stage_prologue(const Stage& st, double& dt, int&
     cur = st.ctl->cur;
   }
   return true;
+}
+
+// Grid barrier of a cooperative launch (every CTA resident), in the
+// arrive/wait pattern of CUTLASS's GenericBarrier, split in two so that a
+// CTA can work on its own data between them.  grid_arrive: the CTA syncs,
+// one thread adds 1 to a monotonic 64-bit arrival counter with release
+// semantics.  grid_wait: that thread spins with acquire loads until the
+// counter reaches (gen + 1) * gridDim.x (gen: barriers completed so far),
+// then the CTA syncs.  bar[0] is the counter, bar[16] the failure flag (its
+// own 128-byte line); both zero at launch.  The spin is bounded; grid_wait
+// returns false, CTA-uniformly, if it ran out.
+static __device__ __forceinline__ void grid_arrive(unsigned long long* bar, const ResidentArgs& R) {
+  __syncthreads();
+  // R.skip_arrive_cta: fault injection for tests (that CTA never arrives, so
+  // every wait after it runs out); -1 in normal use
+  if (threadIdx.x == 0 && static_cast<int>(blockIdx.x) != R.skip_arrive_cta) {
+    const unsigned long long one = 1;
+    asm volatile("red.release.gpu.global.add.u64 [%0], %1;\n" ::"l"(bar), "l"(one) : "memory");
+  }
+}
+static __device__ bool grid_wait(unsigned long long* bar, unsigned long long& gen, long long spin_limit) {
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned long long target = (gen + 1) * gridDim.x;
+    for (int it = 0;; ++it) {
+      unsigned long long v;
+      asm volatile("ld.acquire.gpu.global.u64 %0, [%1];\n" : "=l"(v) : "l"(bar) : "memory");
+      if (v >= target) break;
+      if (it >= spin_limit) {
+        ok = 0;
+        atomicOr(bar + 16, 1ull);
+        break;
+      }
+    }
+    ++gen;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
 }
 
 }  // namespace heomgb

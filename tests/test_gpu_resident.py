@@ -100,12 +100,56 @@ def test_resident_first_attempt_bit_identical(ept, monkeypatch):
 
 
 def test_resident_only_where_it_applies(monkeypatch):
-    p = configs.exciton_7site(depth=2)
-    _, _, tune = run(p, [0.0, 1.0], monkeypatch, True, precision="fp64")
-    assert not tune["resident"]  # Dormand-Prince in the FP64 form keeps the stage kernels
+    p = configs.spin_boson(depth=4)  # V = sigma_z: not a site-local bath
+    _, _, tune = run(p, [0.0, 0.1], monkeypatch, True, precision="fp64", kw=dict(dt=0.01, atol=1e-9, rtol=1e-9))
+    assert not tune["resident"]  # Dormand-Prince in the FP64 form keeps the stage kernels there
+    p7 = configs.exciton_7site(depth=2)
+    _, _, tune7 = run(p7, [0.0, 1.0], monkeypatch, True, precision="fp64")
+    assert tune7["resident"]  # site-local baths: the FP64 resident interval
     monkeypatch.setenv("HEOMGB_RESIDENT", "1")
-    qs = lh.qme_solver(lh.from_params(p, precision="fp64"), lh.lsrk4())
-    assert not qs.tuning()["resident"]  # so does LSRK4 in the FP64 form
+    qs = lh.qme_solver(lh.from_params(p7, precision="fp64"), lh.lsrk4())
+    assert not qs.tuning()["resident"]  # LSRK4 in the FP64 form keeps the stage kernels
+
+
+@pytest.mark.parametrize("ept", ["1", "2"])
+def test_fp64_resident_dp_first_attempt_bit_identical(ept, monkeypatch):
+    """The FP64 form's resident Dormand-Prince interval (site-local baths):
+    one accepted attempt gives the stage kernels' state bit for bit."""
+    p = configs.exciton_7site(depth=3)
+    monkeypatch.setenv("HEOMGB_RESIDENT_EPT", ept)
+    res, st_r, tune = run(p, [0.0, 0.1], monkeypatch, True, precision="fp64")
+    monkeypatch.delenv("HEOMGB_RESIDENT_EPT")
+    stg, st_s, _ = run(p, [0.0, 0.1], monkeypatch, False, precision="fp64")
+    assert tune["resident"]
+    assert st_r["attempts"] == st_s["attempts"] == 1
+    assert np.array_equal(res, stg)
+    assert abs(st_r["dt_save"] - st_s["dt_save"]) <= 1e-12 * abs(st_s["dt_save"])
+
+
+FP64_CASES = {
+    "exciton7_depth4": lambda: configs.exciton_7site(),
+    "complex_h_sqrt": lambda: dataclasses.replace(
+        configs.exciton_7site(depth=3), normalization="sqrt",
+        H=configs.exciton_7site(depth=3).H + 1j * 0.02 * (np.triu(np.ones((7, 7)), 1) - np.tril(np.ones((7, 7)), -1))),
+    "filtered_col_major": lambda: dataclasses.replace(
+        configs.exciton_7site(depth=4), order="col_major",
+        hrchy_filter=lambda idx, d: all(idx[k] <= 1 for k in range(1, len(idx), 2))),
+}
+
+
+@pytest.mark.parametrize("case", sorted(FP64_CASES))
+def test_fp64_resident_dp_matches_stage_kernels(case, monkeypatch):
+    """Several output intervals: the same per-element arithmetic as the stage
+    kernels; only the error norm's sum order differs (step sizes may move in
+    the last bits), so 1e-10 of the state's largest element and attempts within two."""
+    p = FP64_CASES[case]()
+    t = [0.0, 5.0, 10.0, 20.0]
+    res, st_r, tune = run(p, t, monkeypatch, True, precision="fp64")
+    stg, st_s, _ = run(p, t, monkeypatch, False, precision="fp64")
+    assert tune["resident"]
+    assert abs(st_r["attempts"] - st_s["attempts"]) <= 2
+    assert st_r["rhs"] == 7 * st_r["attempts"]
+    assert np.abs(res - stg).max() <= 1e-10 * np.abs(stg).max()
 
 
 @pytest.mark.parametrize("form", ["mixed", "rk4_fp64"])

@@ -665,8 +665,30 @@ __global__ void __launch_bounds__(256, MINB) k_rhs_diag_tc(const DiagSet ds, con
 template <int EPT>
 struct ResElems {
   int lt[EPT], e[EPT], a[EPT], b[EPT];
+  int gi[EPT];    // the element's index in the state vector
   float2 g[EPT];  // damping coefficient sum_k n_k gamma_k + the element's s_delta term
 };
+
+// The ADOs of CTA b of a resident launch: b, b + G, b + 2 G, ... (G CTAs).
+// ADOs are ordered by tier and only those below the deepest have +1 terms, so
+// a strided share gives every CTA the same mix of work and no CTA holds up
+// the grid barriers.
+struct ResAdos {
+  int b0, G, na;
+  __device__ __forceinline__ int ado(int lt) const { return b0 + lt * G; }
+  // state index of CTA-local element le (ADO le / n2, element le % n2)
+  __device__ __forceinline__ size_t gidx(int le, int n2) const {
+    const int lt = le / n2;
+    return static_cast<size_t>(b0 + lt * G) * n2 + (le - lt * n2);
+  }
+};
+__device__ __forceinline__ ResAdos res_ados(int nh) {
+  ResAdos A;
+  A.b0 = blockIdx.x;
+  A.G = gridDim.x;
+  A.na = A.b0 < nh ? (nh - 1 - A.b0) / A.G + 1 : 0;
+  return A;
+}
 
 // Builds the thread's element data and, for its elements, the bath-term table
 // (slot-major: Toff[j * E + le] the neighbour element's offset in the state,
@@ -674,7 +696,7 @@ struct ResElems {
 // terms, in k_rhs_diag's order; the host admits models with at most 4 + 4
 // terms per element).
 template <int EPT>
-__device__ __forceinline__ void res_build(const DiagInst& I, int l0, int E, int* Toff, float2* Tcf,
+__device__ __forceinline__ void res_build(const DiagInst& I, const ResAdos& A, int E, int* Toff, float2* Tcf,
                                           ResElems<EPT>& el) {
   const int n = I.n, n2 = I.n2, K = I.K, void_idx = I.nh;
   const bool sqn = I.sqrt_norm != 0;
@@ -687,7 +709,8 @@ __device__ __forceinline__ void res_build(const DiagInst& I, int l0, int E, int*
     el.e[r] = e;
     el.a[r] = a;
     el.b[r] = e - a * n;
-    const int l = min(l0 + lt, I.nh - 1);
+    const int l = min(A.ado(lt), I.nh - 1);
+    el.gi[r] = l * n2 + e;
     const float2 g0 = I.ngd_f[l], g1 = I.c_sd_f[e];
     el.g[r] = make_float2(g0.x + g1.x, g0.y + g1.y);
     if (le < E) {
@@ -807,10 +830,8 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
   __shared__ DpCtl c;
   const DiagInst& I = R.inst;
   const int n = I.n, n2 = I.n2;
-  const int l0 = min(I.nh, static_cast<int>(blockIdx.x) * R.ados_per_cta);
-  const int l1 = min(I.nh, l0 + R.ados_per_cta);
-  const int E = (l1 - l0) * n2;
-  const size_t gb = static_cast<size_t>(l0) * n2;
+  const ResAdos A = res_ados(I.nh);  // this CTA's ADOs (strided)
+  const int E = A.na * n2;
   // shared memory: H | both states (FP64) | k_1..k_6 | two stage-input copies |
   // FP32 copies of both states (Yf[i] = float(S[i]), kept with the states so
   // that no stage converts from FP64) | the bath-term table
@@ -827,7 +848,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
   {
     const int cur = c.cur;
     for (int le = threadIdx.x; le < E; le += blockDim.x) {
-      const double2 v = R.S[cur][gb + le];
+      const double2 v = R.S[cur][A.gidx(le, n2)];
       Sv[static_cast<size_t>(cur) * E + le] = v;
       const float2 f = make_float2(d2f(v.x), d2f(v.y));
       Yf[static_cast<size_t>(cur) * E + le] = f;
@@ -835,7 +856,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
     }
   }
   ResElems<EPT> el;
-  res_build<EPT>(I, l0, E, Toff, Tcf, el);
+  res_build<EPT>(I, A, E, Toff, Tcf, el);
   unsigned long long gen = 0;
   bool ok = true;
   long long attempts = 0;
@@ -878,7 +899,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
         if (le >= E) continue;
         // stage epilogue (epi_pre + epi_post, mixed form)
         const float2 k = make_float2(-fdt * D[r].x, -fdt * D[r].y);
-        const size_t g = gb + le;
+        const size_t g = el.gi[r];
         if (s < 5) {  // k_s; next stage input Yb + sum_j A[s+1][j] k_j in FP32
           Kv[static_cast<size_t>(s) * E + le] = k;
           float2 y = Yc[le];
@@ -946,7 +967,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
   }
   if (ok) {
     const int cur = c.cur;
-    for (int le = threadIdx.x; le < E; le += blockDim.x) R.S[cur][gb + le] = Sv[static_cast<size_t>(cur) * E + le];
+    for (int le = threadIdx.x; le < E; le += blockDim.x) R.S[cur][A.gidx(le, n2)] = Sv[static_cast<size_t>(cur) * E + le];
     if (blockIdx.x == 0 && threadIdx.x == 0) *R.ctl = c;
   }
 }
@@ -964,10 +985,8 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const DiagInst& I = R.inst;
   const int n = I.n, n2 = I.n2;
-  const int l0 = min(I.nh, static_cast<int>(blockIdx.x) * R.ados_per_cta);
-  const int l1 = min(I.nh, l0 + R.ados_per_cta);
-  const int E = (l1 - l0) * n2;
-  const size_t gb = static_cast<size_t>(l0) * n2;
+  const ResAdos A = res_ados(I.nh);  // this CTA's ADOs (strided)
+  const int E = A.na * n2;
   // shared memory: H | state, accumulator (FP64) | two stage-input copies |
   // the state's FP32 copy | the bath-term table
   float2* Hs = reinterpret_cast<float2*>(smem_raw);
@@ -979,7 +998,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
   float2* Tcf = reinterpret_cast<float2*>(Toff + kResidentTerms * static_cast<size_t>(E));
   for (int i = threadIdx.x; i < n2; i += blockDim.x) Hs[i] = I.H_f[i];
   for (int le = threadIdx.x; le < E; le += blockDim.x) {
-    const double2 v = R.S[0][gb + le];
+    const double2 v = R.S[0][A.gidx(le, n2)];
     Sv[le] = v;
     const float2 f = make_float2(d2f(v.x), d2f(v.y));
     Yf[le] = f;
@@ -987,7 +1006,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
   }
   __syncthreads();
   ResElems<EPT> el;
-  res_build<EPT>(I, l0, E, Toff, Tcf, el);
+  res_build<EPT>(I, A, E, Toff, Tcf, el);
   unsigned long long gen = 0;
   bool ok = true;
   for (long long step = 0; step <= R.n_steps && ok; ++step) {
@@ -1008,7 +1027,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
         const int le = threadIdx.x + r * blockDim.x;
         if (le >= E) continue;
         const float2 k = make_float2(__fmul_rn(-fdt, D[r].x), __fmul_rn(-fdt, D[r].y));
-        const size_t g = gb + le;
+        const size_t g = el.gi[r];
         if (s < 3) {  // rho_n = rho + c*k (FP32 from the state's copy); acc = rho + k/6 or acc += k/3
           const float cs = static_cast<float>(s == 2 ? 1.0 : 0.5);
           const float w = static_cast<float>(s == 0 ? (1.0 / 6.0) : (2.0 / 6.0));
@@ -1035,7 +1054,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
     }
   }
   if (ok)
-    for (int le = threadIdx.x; le < E; le += blockDim.x) R.S[0][gb + le] = Sv[le];
+    for (int le = threadIdx.x; le < E; le += blockDim.x) R.S[0][A.gidx(le, n2)] = Sv[le];
 }
 
 // The fixed-step RK4 interval of the FP64 form in one cooperative launch (the
@@ -1048,7 +1067,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
 // form with the RK4 epilogues (EPI_RK4_1..4, explicit FMAs), in the same
 // order, so the results are the stage kernels' bits.
 template <int EPT>
-__device__ __forceinline__ void res_build64(const DiagInst& I, int l0, int E, int* Toff, double2* Tcf,
+__device__ __forceinline__ void res_build64(const DiagInst& I, const ResAdos& A, int E, int* Toff, double2* Tcf,
                                             ResElems<EPT>& el, double2 (&g)[EPT]) {
   const int n = I.n, n2 = I.n2, K = I.K, void_idx = I.nh;
   const bool sqn = I.sqrt_norm != 0;
@@ -1061,7 +1080,8 @@ __device__ __forceinline__ void res_build64(const DiagInst& I, int l0, int E, in
     el.e[r] = e;
     el.a[r] = a;
     el.b[r] = e - a * n;
-    const int l = min(l0 + lt, I.nh - 1);
+    const int l = min(A.ado(lt), I.nh - 1);
+    el.gi[r] = l * n2 + e;
     const double2 g0 = I.ngd[l], g1 = I.c_sd[e];
     g[r] = make_double2(g0.x + g1.x, g0.y + g1.y);
     if (le < E) {
@@ -1116,10 +1136,8 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident64(const R
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const DiagInst& I = R.inst;
   const int n = I.n, n2 = I.n2;
-  const int l0 = min(I.nh, static_cast<int>(blockIdx.x) * R.ados_per_cta);
-  const int l1 = min(I.nh, l0 + R.ados_per_cta);
-  const int E = (l1 - l0) * n2;
-  const size_t gb = static_cast<size_t>(l0) * n2;
+  const ResAdos A = res_ados(I.nh);  // this CTA's ADOs (strided)
+  const int E = A.na * n2;
   double2* S = R.S[0];  // the state: also the stage-1 input the neighbours gather
   double2* Yt[2] = {reinterpret_cast<double2*>(R.Ytmp[0]), reinterpret_cast<double2*>(R.Ytmp[1])};
   // shared memory: H | state, accumulator | two stage-input copies | the bath-term table
@@ -1131,14 +1149,14 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident64(const R
   int* Toff = reinterpret_cast<int*>(Tcf + kResidentTerms * static_cast<size_t>(E));
   for (int i = threadIdx.x; i < n2; i += blockDim.x) Hs[i] = I.H[i];
   for (int le = threadIdx.x; le < E; le += blockDim.x) {
-    const double2 v = S[gb + le];
+    const double2 v = S[A.gidx(le, n2)];
     Sv[le] = v;
     yt[le] = v;
   }
   __syncthreads();
   ResElems<EPT> el;
   double2 gd[EPT];
-  res_build64<EPT>(I, l0, E, Toff, Tcf, el, gd);
+  res_build64<EPT>(I, A, E, Toff, Tcf, el, gd);
   unsigned long long gen = 0;
   bool ok = true;
   for (long long step = 0; step <= R.n_steps && ok; ++step) {
@@ -1201,7 +1219,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident64(const R
 #pragma unroll
         for (int j = 0; j < kResidentTerms; ++j) cfma(D[r], Tcf[static_cast<size_t>(j) * E + le], vv[r][j]);
         const double2 k = make_double2(-dt * D[r].x, -dt * D[r].y);
-        const size_t g = gb + le;
+        const size_t g = el.gi[r];
         if (s < 3) {  // rho_n = rho + c*k ; acc = rho + k/6 or acc += k/3
           const double c = s == 2 ? 1.0 : 0.5;
           const double w = s == 0 ? (1.0 / 6.0) : (2.0 / 6.0);
@@ -1236,10 +1254,8 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_ls_resident(const Resi
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const DiagInst& I = R.inst;
   const int n = I.n, n2 = I.n2;
-  const int l0 = min(I.nh, static_cast<int>(blockIdx.x) * R.ados_per_cta);
-  const int l1 = min(I.nh, l0 + R.ados_per_cta);
-  const int E = (l1 - l0) * n2;
-  const size_t gb = static_cast<size_t>(l0) * n2;
+  const ResAdos A = res_ados(I.nh);  // this CTA's ADOs (strided)
+  const int E = A.na * n2;
   // shared memory: H | state (FP64) | buffer | the state's FP32 copy | the bath-term table
   float2* Hs = reinterpret_cast<float2*>(smem_raw);
   double2* Sv = reinterpret_cast<double2*>(smem_raw + ((sizeof(float2) * n2 + 15) & ~static_cast<size_t>(15)));
@@ -1249,13 +1265,13 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_ls_resident(const Resi
   float2* Tcf = reinterpret_cast<float2*>(Toff + kResidentTerms * static_cast<size_t>(E));
   for (int i = threadIdx.x; i < n2; i += blockDim.x) Hs[i] = I.H_f[i];
   for (int le = threadIdx.x; le < E; le += blockDim.x) {
-    const double2 v = R.S[0][gb + le];
+    const double2 v = R.S[0][A.gidx(le, n2)];
     Sv[le] = v;
     Yf[le] = make_float2(d2f(v.x), d2f(v.y));
   }
   __syncthreads();
   ResElems<EPT> el;
-  res_build<EPT>(I, l0, E, Toff, Tcf, el);
+  res_build<EPT>(I, A, E, Toff, Tcf, el);
   const double B[4] = {1.0 / 3.0, 3.0 / 4.0, 2.0 / 3.0, 1.0 / 4.0};  // lsrk4.h:39-46
   unsigned long long gen = 0;
   bool ok = true;
@@ -1287,13 +1303,13 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_ls_resident(const Resi
         Sv[le] = v;
         const float2 f = make_float2(d2f(v.x), d2f(v.y));
         Yf[le] = f;
-        R.Yb[1 - (s & 1)][gb + le] = f;
+        R.Yb[1 - (s & 1)][el.gi[r]] = f;
       }
       grid_arrive(R.bar, R);
     }
   }
   if (ok)
-    for (int le = threadIdx.x; le < E; le += blockDim.x) R.S[0][gb + le] = Sv[le];
+    for (int le = threadIdx.x; le < E; le += blockDim.x) R.S[0][A.gidx(le, n2)] = Sv[le];
 }
 
 size_t resident_smem(int n2, int ados_per_cta, int scheme) {

@@ -3,7 +3,8 @@
 // right-hand side of heom_hilb::calc_diff_impl (heom_hilb.h:70-215) for
 // site-local baths (every V_u diagonal with a single nonzero entry).
 //
-// CTA b owns ADOs [b * ados_per_cta, ...).  It keeps their two FP64 states
+// CTA b owns ADOs b, b + G, b + 2G, ... (G CTAs; the same mix of tiers in
+// every CTA).  It keeps their two FP64 states
 // (current and candidate), the six stage vectors k_1..k_6 and two stage-input
 // copies in shared memory, with the ADOs' records (occupied modes with their
 // -1 neighbours), ptr_p1 and occupation rows and the per-mode coefficient
@@ -68,6 +69,13 @@ __device__ __forceinline__ Res64Smem res64_layout(unsigned char* raw, int n, int
   return L;
 }
 
+// c != 0 tested on the bit patterns (integer operations: this part's FP64
+// pipe is the bottleneck of the FP64 form); -0 counts as zero
+__device__ __forceinline__ bool nonzero(double2 c) {
+  return ((static_cast<unsigned long long>(__double_as_longlong(c.x)) |
+           static_cast<unsigned long long>(__double_as_longlong(c.y))) << 1) != 0ull;
+}
+
 // The terms of element e = (a, b) of CTA-local ADO lt, k_rhs_diag<double>'s
 // order (+1 terms in increasing k, then -1 terms in increasing k), in batches
 // of four: a batch's terms are formed, their gathers issued together, then
@@ -99,7 +107,7 @@ __device__ __forceinline__ void res64_terms(const Res64Smem& L, const DiagInst& 
           pb += ta ? 0 : 1;
           const int lp = p1r[k];
           double2 c = L.cp2[2 * k + (ta ? 0 : 1)];
-          if (lp != void_idx && (c.x != 0.0 || c.y != 0.0)) {
+          if (lp != void_idx && nonzero(c)) {
             if (sqn) {  // sqrt(n_k + 1) c_plus, as the set-up table forms it
               const double f = sqrt(static_cast<double>(L.nk[lt * K + k] + 1));
               c = make_double2(f * c.x, f * c.y);
@@ -132,7 +140,7 @@ __device__ __forceinline__ void res64_terms(const Res64Smem& L, const DiagInst& 
         if (r.w == a || r.w == b) {
           const int cs = r.w == a ? (r.w == b ? 2 : 0) : 1;
           const double2 cm = L.cm3[3 * r.x + cs];
-          if (cm.x != 0.0 || cm.y != 0.0) {
+          if (nonzero(cm)) {
             const double f = sqn ? sqrt(static_cast<double>(r.z)) : occ<double>(r.z);
             off[u] = r.y * n2 + e;
             cf[u] = make_double2(f * cm.x, f * cm.y);
@@ -156,10 +164,11 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident64(const Re
   __shared__ DpCtl c;
   const DiagInst& I = R.inst;
   const int n = I.n, n2 = I.n2, K = I.K, w1 = 1 + I.site_w;
-  const int l0 = min(I.nh, static_cast<int>(blockIdx.x) * R.ados_per_cta);
-  const int l1 = min(I.nh, l0 + R.ados_per_cta);
-  const int na = l1 - l0, E = na * n2;
-  const size_t gb = static_cast<size_t>(l0) * n2;
+  // CTA b owns ADOs b, b + G, b + 2 G, ... (G CTAs): every CTA gets the same
+  // mix of tiers (ADOs are ordered by tier, and only those below the deepest
+  // have +1 terms), so no CTA holds up the grid barriers with more work
+  const int G = gridDim.x, b0 = blockIdx.x;
+  const int na = b0 < I.nh ? (I.nh - 1 - b0) / G + 1 : 0, E = na * n2;
   const Res64Smem L = res64_layout(smem_raw, n, K, I.site_w, R.ados_per_cta);
   double2* Yt0 = reinterpret_cast<double2*>(R.Ytmp[0]);  // stage inputs 2..6 (alternating; no array:
   double2* Yt1 = reinterpret_cast<double2*>(R.Ytmp[1]);  // a runtime index would put it in local memory)
@@ -168,34 +177,42 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident64(const Re
   for (int i = threadIdx.x; i < 2 * K; i += blockDim.x) L.cp2[i] = I.site_cp2_d[i];
   for (int i = threadIdx.x; i <= n; i += blockDim.x) L.sptr[i] = I.site_ptr[i];
   for (int i = threadIdx.x; i < K; i += blockDim.x) L.smodes[i] = I.site_modes[i];
-  for (int i = threadIdx.x; i < na * w1; i += blockDim.x) L.rec[i] = I.site_rec[static_cast<size_t>(l0) * w1 + i];
+  for (int i = threadIdx.x; i < na * w1; i += blockDim.x) {
+    const int lt = i / w1;
+    L.rec[i] = I.site_rec[static_cast<size_t>(b0 + lt * G) * w1 + (i - lt * w1)];
+  }
   for (int i = threadIdx.x; i < na * K; i += blockDim.x) {
-    L.p1[i] = I.p1[static_cast<size_t>(l0) * K + i];
-    L.nk[i] = I.nidx[static_cast<size_t>(l0) * K + i];
+    const int lt = i / K;
+    const size_t gi = static_cast<size_t>(b0 + lt * G) * K + (i - lt * K);
+    L.p1[i] = I.p1[gi];
+    L.nk[i] = I.nidx[gi];
   }
   if (threadIdx.x == 0) c = *R.ctl;
   __syncthreads();
   {
     const int cur = c.cur;
     for (int le = threadIdx.x; le < E; le += blockDim.x) {
-      const double2 v = R.S[cur][gb + le];
+      const int lt = le / n2;
+      const double2 v = R.S[cur][static_cast<size_t>(b0 + lt * G) * n2 + (le - lt * n2)];
       L.S[static_cast<size_t>(cur) * E + le] = v;
       L.X[le] = v;
     }
   }
   // the thread's elements and their damping coefficients (ngamma + s_delta term, k_rhs_diag's sum)
-  int el_lt[EPT], el_e[EPT], el_a[EPT], el_b[EPT];
+  int el_lt[EPT], el_e[EPT], el_a[EPT], el_b[EPT], el_g[EPT];
   double2 gd[EPT];
 #pragma unroll
   for (int r = 0; r < EPT; ++r) {
     const int le = threadIdx.x + r * blockDim.x;
     const int lec = le < E ? le : 0;
     const int lt = lec / n2, e = lec - lt * n2, a = e / n;
+    const int l = min(b0 + lt * G, I.nh - 1);
     el_lt[r] = lt;
     el_e[r] = e;
     el_a[r] = a;
     el_b[r] = e - a * n;
-    const double2 g0 = I.ngd[min(l0 + lt, I.nh - 1)], g1 = I.c_sd[e];
+    el_g[r] = l * n2 + e;  // the element's index in the state vector
+    const double2 g0 = I.ngd[l], g1 = I.c_sd[e];
     gd[r] = make_double2(g0.x + g1.x, g0.y + g1.y);
   }
   __syncthreads();
@@ -266,7 +283,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident64(const Re
         res64_terms(L, I, Xg, el_lt[r], el_a[r], el_b[r], el_e[r], w1, D[r]);
         // stage epilogue: the FP64 form's EPI_DP / EPI_DP7 (epi_pre / epi_post), explicit FMAs
         const double2 k = make_double2(-dt * D[r].x, -dt * D[r].y);
-        const size_t g = gb + le;
+        const int g = el_g[r];
         if (s < 6) {
           double2 y = Sc[le];
           for (int j = 0; j < s; ++j) {

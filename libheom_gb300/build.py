@@ -15,7 +15,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libheomgb.so")
-SOURCES = ["kernels.cu", "sites.cu", "resident64.cu", "api.cu", "mlp.cu", "noalloc.cu"]
+SOURCES = ["kernels.cu", "sites.cu", "resident64.cu", "tcgemm.cu", "api.cu", "mlp.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include"), "-I", CSRC]

@@ -1988,6 +1988,8 @@ void solve_impl(heomgb_qme_solver* qs, void* rho, bool host, const double* t_lis
     }
     ck(cudaStreamSynchronize(qs->stream), "interval sync");
     busy_collect(qs);
+    if (qs->term && mlp_take_error(qs->term, qs->stream))
+      throw cuda_error("terminator inference: a tensor-core GEMM did not complete");
   }
   if (cb) cb(t_list[n_t - 1], user);
 }

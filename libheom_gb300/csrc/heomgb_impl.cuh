@@ -297,6 +297,27 @@ cudaError_t launch_errnrm1(const double2* e, const double2* x1, const double2* x
 int errnrm1_grid(long long n);
 cudaError_t probe_fma_peaks(int n_sm, double* fp64_tflops, double* fp32_tflops, cudaStream_t s);
 
+// BF16 tensor-core GEMM (tcgemm.cu): C[m][n] = sum_k A(m, k) B(n, k) (+ bias[n]),
+// FP32 accumulation; an operand element (r, k) is p[r * sm + k * sk], FP32 or BF16.
+struct GemmOperand {
+  const void* p;
+  int bf16;           // 1: BF16 elements, 0: FP32
+  long long sm, sk;   // strides (elements) of the row and of k
+};
+enum GemmEpi : int { GEMM_STORE = 0, GEMM_GELU = 1, GEMM_GELU_GRAD = 2 };
+struct GemmArgs {
+  GemmOperand a, b;
+  float* c;           // M x N, row stride ldc
+  long long ldc;
+  const float* bias;  // N or null
+  float* pre;         // GEMM_GELU: receives the pre-activation (may be null); GEMM_GELU_GRAD: read
+  int M, N, K;
+  int epi;            // GemmEpi: store; bias + GELU; times gelu'(pre)
+  int bn, tmem_cols;  // set by the launcher
+  int* err;           // set to 1 if a tensor-core wait ran out
+};
+cudaError_t launch_gemm_bf16(GemmArgs g, cudaStream_t s);
+
 // Buffers of one terminator inference over the tier-N ADOs [first, first+n_tier).
 struct TermBuffers {
   int first = 0, n_tier = 0, n2 = 0, K = 0;
@@ -330,6 +351,8 @@ struct TermModel {
 cudaError_t term_enqueue(heomgb_mlp* M, const TermBuffers& tb, const TermModel& tm, const TermInput& in,
                          bool y_float, cudaStream_t s);
 void mlp_dims(const heomgb_mlp* M, int* din, int* h, int* dout);
+// true (and the flag cleared) if a tensor-core GEMM of M's inference gave up a wait
+bool mlp_take_error(heomgb_mlp* M, cudaStream_t s);
 
 // Kernels launched (incremented by the launchers and graph replays), safe for
 // solvers driven from several host threads: an atomic total plus a per-thread

@@ -2,8 +2,11 @@
 // hierarchy from tier-N ADOs, trained and evaluated with the kernels below.
 //
 // Network: x (d_in) -> Linear(h) -> GELU -> Linear(h) -> GELU -> Linear(d_out).
-// Weights are kept as FP32 masters (Adam) and BF16 copies (forward /
-// backward-data / inference); every product accumulates in FP32.
+// Weights are kept as FP32 masters (Adam) and BF16 copies.  Every product of
+// the forward pass, the backward pass (data and weight gradients) and the
+// inference is a BF16 tensor-core GEMM (tcgemm.cu: tcgen05.mma, BF16 operands,
+// FP32 accumulation in tensor memory); bias, GELU and the GELU derivative run
+// in the GEMM's epilogue.
 //
 // Terminator use: for a tier-N ADO rho_n and mode k, the input is
 // [Re rho_n / s, Im rho_n / s, onehot(k), Re A / s, Im A / s] with
@@ -33,99 +36,13 @@ using namespace heomgb;
 
 namespace {
 
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
-__device__ __forceinline__ float gelu_grad(float x) {
-  const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
-  return cdf + x * pdf;
-}
-
-// Y[b, o] = act(sum_i X[b, i] * W[o, i] + bias[o]); PRE keeps the
-// pre-activation for the backward pass.  16x16 output tiles, K staged in 32s.
-template <bool GELU_ACT>
-__global__ void k_linear_fwd(const float* __restrict__ X, const __nv_bfloat16* __restrict__ W,
-                             const float* __restrict__ bias, float* __restrict__ Y, float* __restrict__ PRE, int B,
-                             int din, int dout) {
-  __shared__ float xs[16][33];
-  __shared__ float ws[16][33];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int b = blockIdx.y * 16 + ty, o = blockIdx.x * 16 + tx;
+// db[o] = sum_b dZ[b, o] (bias gradient; the weight gradients are tensor-core GEMMs)
+__global__ void k_bias_grad(const float* __restrict__ dZ, float* __restrict__ db, int B, int dout) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= dout) return;
   float acc = 0.f;
-  for (int k0 = 0; k0 < din; k0 += 32) {
-    for (int t = threadIdx.x; t < 16 * 32; t += 256) {
-      const int r = t / 32, c = t % 32;
-      const int gb = blockIdx.y * 16 + r, go = blockIdx.x * 16 + r, gk = k0 + c;
-      xs[r][c] = (gb < B && gk < din) ? X[static_cast<size_t>(gb) * din + gk] : 0.f;
-      ws[r][c] = (go < dout && gk < din) ? __bfloat162float(W[static_cast<size_t>(go) * din + gk]) : 0.f;
-    }
-    __syncthreads();
-#pragma unroll 8
-    for (int c = 0; c < 32; ++c) acc = fmaf(xs[ty][c], ws[tx][c], acc);
-    __syncthreads();
-  }
-  if (b < B && o < dout) {
-    const float z = acc + bias[o];
-    if (PRE) PRE[static_cast<size_t>(b) * dout + o] = z;
-    Y[static_cast<size_t>(b) * dout + o] = GELU_ACT ? gelu(z) : z;
-  }
-}
-
-// dX[b, i] = sum_o dZ[b, o] * W[o, i]
-__global__ void k_linear_bwd_data(const float* __restrict__ dZ, const __nv_bfloat16* __restrict__ W,
-                                  float* __restrict__ dX, int B, int din, int dout) {
-  __shared__ float zs[16][33];
-  __shared__ float ws[32][17];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int b = blockIdx.y * 16 + ty, i = blockIdx.x * 16 + tx;
-  float acc = 0.f;
-  for (int o0 = 0; o0 < dout; o0 += 32) {
-    for (int t = threadIdx.x; t < 16 * 32; t += 256) {
-      const int r = t / 32, c = t % 32;
-      const int gb = blockIdx.y * 16 + r, go = o0 + c;
-      zs[r][c] = (gb < B && go < dout) ? dZ[static_cast<size_t>(gb) * dout + go] : 0.f;
-      const int wo = o0 + t / 16, wi = blockIdx.x * 16 + t % 16;
-      ws[t / 16][t % 16] = (wo < dout && wi < din) ? __bfloat162float(W[static_cast<size_t>(wo) * din + wi]) : 0.f;
-    }
-    __syncthreads();
-#pragma unroll 8
-    for (int c = 0; c < 32; ++c) acc = fmaf(zs[ty][c], ws[c][tx], acc);
-    __syncthreads();
-  }
-  if (b < B && i < din) dX[static_cast<size_t>(b) * din + i] = acc;
-}
-
-// dW[o, i] = sum_b dZ[b, o] * X[b, i]; db[o] = sum_b dZ[b, o]
-__global__ void k_linear_bwd_weight(const float* __restrict__ dZ, const float* __restrict__ X, float* __restrict__ dW,
-                                    float* __restrict__ db, int B, int din, int dout) {
-  __shared__ float zs[32][17];
-  __shared__ float xs[32][17];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int o = blockIdx.y * 16 + ty, i = blockIdx.x * 16 + tx;
-  float acc = 0.f, accb = 0.f;
-  for (int b0 = 0; b0 < B; b0 += 32) {
-    for (int t = threadIdx.x; t < 32 * 16; t += 256) {
-      const int r = t / 16, c = t % 16;
-      const int gb = b0 + r;
-      const int go = blockIdx.y * 16 + c, gi = blockIdx.x * 16 + c;
-      zs[r][c] = (gb < B && go < dout) ? dZ[static_cast<size_t>(gb) * dout + go] : 0.f;
-      xs[r][c] = (gb < B && gi < din) ? X[static_cast<size_t>(gb) * din + gi] : 0.f;
-    }
-    __syncthreads();
-#pragma unroll 8
-    for (int r = 0; r < 32; ++r) {
-      acc = fmaf(zs[r][ty], xs[r][tx], acc);
-      accb += zs[r][ty];
-    }
-    __syncthreads();
-  }
-  if (o < dout && i < din) dW[static_cast<size_t>(o) * din + i] = acc;
-  if (db && blockIdx.x == 0 && tx == 0 && o < dout) db[o] = accb;
-}
-
-__global__ void k_gelu_bwd(float* __restrict__ dY, const float* __restrict__ PRE, long long n) {
-  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * blockDim.x)
-    dY[i] *= gelu_grad(PRE[i]);
+  for (int b = 0; b < B; ++b) acc += dZ[static_cast<size_t>(b) * dout + o];
+  db[o] = acc;
 }
 
 // Mean-squared error and its gradient d/dY of mean((Y-T)^2); per-CTA partial
@@ -245,6 +162,7 @@ struct heomgb_mlp {
   int cap = 0;                  // batch capacity of the activation buffers
   float *a1 = nullptr, *p1 = nullptr, *a2 = nullptr, *p2 = nullptr, *y = nullptr, *d = nullptr, *d2 = nullptr;
   float* part = nullptr;
+  int* err = nullptr;           // set by a tensor-core GEMM whose wait ran out
   cudaStream_t s = nullptr;
   void free_acts() {
     for (float* p : {a1, p1, a2, p2, y, d, d2, part}) cudaFree(p);
@@ -268,7 +186,7 @@ struct heomgb_mlp {
   ~heomgb_mlp() {
     free_acts();
     for (void* p : {static_cast<void*>(w), static_cast<void*>(wb), static_cast<void*>(g), static_cast<void*>(m),
-                    static_cast<void*>(v)})
+                    static_cast<void*>(v), static_cast<void*>(err)})
       cudaFree(p);
     if (s) cudaStreamDestroy(s);
   }
@@ -290,27 +208,68 @@ heomgb_status mguard(F&& f) {
   }
 }
 
-void linear_fwd(heomgb_mlp* M, const float* X, int layer, float* Y, float* PRE, int B, bool act) {
+GemmOperand op_f32(const float* p, long long sm, long long sk) { return GemmOperand{p, 0, sm, sk}; }
+GemmOperand op_bf16(const __nv_bfloat16* p, long long sm, long long sk) { return GemmOperand{p, 1, sm, sk}; }
+
+void gemm(heomgb_mlp* M, GemmOperand a, GemmOperand b, float* c, long long ldc, const float* bias, float* pre,
+          int m, int n, int k, int epi, cudaStream_t s) {
+  GemmArgs g{};
+  g.a = a;
+  g.b = b;
+  g.c = c;
+  g.ldc = ldc;
+  g.bias = bias;
+  g.pre = pre;
+  g.M = m;
+  g.N = n;
+  g.K = k;
+  g.epi = epi;
+  g.err = M->err;
+  ckm(launch_gemm_bf16(g, s), "tensor-core gemm");
+}
+
+// Y[b][o] = act(sum_i X[b][i] W[o][i] + bias[o]) for layer 0..2
+void linear_fwd(heomgb_mlp* M, const float* X, int layer, float* Y, float* PRE, int B, bool act, cudaStream_t s) {
   const int din = layer == 0 ? M->din : M->h, dout = layer == 2 ? M->dout : M->h;
-  const dim3 grid((dout + 15) / 16, (B + 15) / 16);
-  const __nv_bfloat16* W = M->wb + M->off[2 * layer];
-  const float* bias = M->w + M->off[2 * layer + 1];
-  if (act)
-    k_linear_fwd<true><<<grid, 256, 0, M->s>>>(X, W, bias, Y, PRE, B, din, dout);
-  else
-    k_linear_fwd<false><<<grid, 256, 0, M->s>>>(X, W, bias, Y, PRE, B, din, dout);
-  ++g_launches;
-  ckm(cudaGetLastError(), "linear fwd");
+  gemm(M, op_f32(X, din, 1), op_bf16(M->wb + M->off[2 * layer], din, 1), Y, dout, M->w + M->off[2 * layer + 1],
+       PRE, B, dout, din, act ? GEMM_GELU : GEMM_STORE, s);
+}
+
+void check_err(heomgb_mlp* M) {
+  int e = 0;
+  ckm(cudaMemcpyAsync(&e, M->err, sizeof(int), cudaMemcpyDeviceToHost, M->s), "mlp status");
+  ckm(cudaStreamSynchronize(M->s), "mlp sync");
+  if (e) {
+    ckm(cudaMemsetAsync(M->err, 0, sizeof(int), M->s), "mlp status reset");
+    throw std::runtime_error("tensor-core GEMM did not complete (a bounded wait ran out)");
+  }
 }
 
 void forward(heomgb_mlp* M, const float* X, float* out, int B) {
   M->ensure(B);
-  linear_fwd(M, X, 0, M->a1, M->p1, B, true);
-  linear_fwd(M, M->a1, 1, M->a2, M->p2, B, true);
-  linear_fwd(M, M->a2, 2, out, nullptr, B, false);
+  linear_fwd(M, X, 0, M->a1, M->p1, B, true, M->s);
+  linear_fwd(M, M->a1, 1, M->a2, M->p2, B, true, M->s);
+  linear_fwd(M, M->a2, 2, out, nullptr, B, false, M->s);
 }
 
-// Forward + backward: fills M->g with d(mean sq. error)/d(params); returns the loss.
+// Weight and bias gradients of layer `layer` from dZ (B x dout) and its input X (B x din):
+// dW[o][i] = sum_b dZ[b][o] X[b][i], db[o] = sum_b dZ[b][o]
+void weight_grad(heomgb_mlp* M, const float* dZ, const float* X, int layer, int B) {
+  const int din = layer == 0 ? M->din : M->h, dout = layer == 2 ? M->dout : M->h;
+  gemm(M, op_f32(dZ, 1, dout), op_f32(X, 1, din), M->g + M->off[2 * layer], din, nullptr, nullptr, dout, din, B,
+       GEMM_STORE, M->s);
+  k_bias_grad<<<(dout + 127) / 128, 128, 0, M->s>>>(dZ, M->g + M->off[2 * layer + 1], B, dout);
+  ++g_launches;
+}
+
+// dH[b][i] = (sum_o dZ[b][o] W[o][i]) gelu'(PRE[b][i]) for the hidden layer below `layer`
+void data_grad(heomgb_mlp* M, const float* dZ, int layer, const float* PRE, float* dH, int B) {
+  const int din = layer == 0 ? M->din : M->h, dout = layer == 2 ? M->dout : M->h;
+  gemm(M, op_f32(dZ, dout, 1), op_bf16(M->wb + M->off[2 * layer], 1, din), dH, din, nullptr,
+       const_cast<float*>(PRE), B, din, dout, GEMM_GELU_GRAD, M->s);
+}
+
+// Forward + backward: fills M->g with the gradient of the loss; returns the loss.
 float backward(heomgb_mlp* M, const float* X, const float* T, int B) {
   M->ensure(B);
   forward(M, X, M->y, B);
@@ -323,37 +282,16 @@ float backward(heomgb_mlp* M, const float* X, const float* T, int B) {
   else
     k_mse<<<gm, 256, 0, M->s>>>(M->y, T, dy, M->part, ny);
   ++g_launches;
-  // layer 3
-  {
-    const dim3 gw((M->h + 15) / 16, (M->dout + 15) / 16);
-    k_linear_bwd_weight<<<gw, 256, 0, M->s>>>(dy, M->a2, M->g + M->off[4], M->g + M->off[5], B, M->h, M->dout);
-    const dim3 gd((M->h + 15) / 16, (B + 15) / 16);
-    k_linear_bwd_data<<<gd, 256, 0, M->s>>>(dy, M->wb + M->off[4], M->d2, B, M->h, M->dout);
-    const long long nh = static_cast<long long>(B) * M->h;
-    k_gelu_bwd<<<grid_for(nh), 256, 0, M->s>>>(M->d2, M->p2, nh);
-    g_launches += 3;
-  }
-  // layer 2
   float* dh1 = M->d + ny;  // B*h scratch after dy
-  {
-    const dim3 gw((M->h + 15) / 16, (M->h + 15) / 16);
-    k_linear_bwd_weight<<<gw, 256, 0, M->s>>>(M->d2, M->a1, M->g + M->off[2], M->g + M->off[3], B, M->h, M->h);
-    const dim3 gd((M->h + 15) / 16, (B + 15) / 16);
-    k_linear_bwd_data<<<gd, 256, 0, M->s>>>(M->d2, M->wb + M->off[2], dh1, B, M->h, M->h);
-    const long long nh = static_cast<long long>(B) * M->h;
-    k_gelu_bwd<<<grid_for(nh), 256, 0, M->s>>>(dh1, M->p1, nh);
-    g_launches += 3;
-  }
-  // layer 1
-  {
-    const dim3 gw((M->din + 15) / 16, (M->h + 15) / 16);
-    k_linear_bwd_weight<<<gw, 256, 0, M->s>>>(dh1, X, M->g + M->off[0], M->g + M->off[1], B, M->din, M->h);
-    ++g_launches;
-  }
+  weight_grad(M, dy, M->a2, 2, B);
+  data_grad(M, dy, 2, M->p2, M->d2, B);      // d(layer-2 pre-activation)
+  weight_grad(M, M->d2, M->a1, 1, B);
+  data_grad(M, M->d2, 1, M->p1, dh1, B);     // d(layer-1 pre-activation)
+  weight_grad(M, dh1, X, 0, B);
   ckm(cudaGetLastError(), "mlp backward");
   std::vector<float> part(gl);
   ckm(cudaMemcpyAsync(part.data(), M->part, sizeof(float) * gl, cudaMemcpyDeviceToHost, M->s), "loss copy");
-  ckm(cudaStreamSynchronize(M->s), "mlp sync");
+  check_err(M);
   double loss = 0;
   for (float p : part) loss += p;
   return static_cast<float>(loss / static_cast<double>(M->loss_kind == 1 ? B : ny));
@@ -481,14 +419,24 @@ cudaError_t term_enqueue(heomgb_mlp* M, const TermBuffers& tb, const TermModel& 
   else
     k_term_pack<double2><<<tb.n_tier, 128, 0, s>>>(in, tm, tb.first, tb.n_tier, tb.X, tb.scale);
   const int din = M->din, h = M->h, dout = M->dout;
-  const dim3 g1((h + 15) / 16, (R + 15) / 16), g3((dout + 15) / 16, (R + 15) / 16);
-  k_linear_fwd<true><<<g1, 256, 0, s>>>(tb.X, M->wb + M->off[0], M->w + M->off[1], tb.A1, nullptr, R, din, h);
-  k_linear_fwd<true><<<g1, 256, 0, s>>>(tb.A1, M->wb + M->off[2], M->w + M->off[3], tb.A2, nullptr, R, h, h);
-  k_linear_fwd<false><<<g3, 256, 0, s>>>(tb.A2, M->wb + M->off[4], M->w + M->off[5], tb.Y, nullptr, R, h, dout);
+  gemm(M, op_f32(tb.X, din, 1), op_bf16(M->wb + M->off[0], din, 1), tb.A1, h, M->w + M->off[1], nullptr, R, h, din,
+       GEMM_GELU, s);
+  gemm(M, op_f32(tb.A1, h, 1), op_bf16(M->wb + M->off[2], h, 1), tb.A2, h, M->w + M->off[3], nullptr, R, h, h,
+       GEMM_GELU, s);
+  gemm(M, op_f32(tb.A2, h, 1), op_bf16(M->wb + M->off[4], h, 1), tb.Y, dout, M->w + M->off[5], nullptr, R, dout, h,
+       GEMM_STORE, s);
   const long long tot = static_cast<long long>(R) * tb.n2;
   k_term_scatter<<<grid_for(tot), 256, 0, s>>>(tb.Y, tb.X, tb.scale, tm, tb.n_tier, din, tb.P);
-  g_launches += 5;
+  g_launches += 2;  // the pack and scatter kernels; the GEMMs count their own
   return cudaGetLastError();
+}
+
+bool mlp_take_error(heomgb_mlp* M, cudaStream_t s) {
+  int e = 0;
+  ckm(cudaMemcpyAsync(&e, M->err, sizeof(int), cudaMemcpyDeviceToHost, s), "mlp status");
+  ckm(cudaStreamSynchronize(s), "mlp sync");
+  if (e) ckm(cudaMemsetAsync(M->err, 0, sizeof(int), s), "mlp status reset");
+  return e != 0;
 }
 
 void mlp_dims(const heomgb_mlp* M, int* din, int* h, int* dout) {
@@ -536,6 +484,8 @@ heomgb_status heomgb_mlp_create(int d_in, int d_hidden, int d_out, unsigned long
     ckm(cudaMalloc(&M->m, fb), "mlp alloc");
     ckm(cudaMalloc(&M->v, fb), "mlp alloc");
     ckm(cudaMalloc(&M->wb, sizeof(__nv_bfloat16) * o), "mlp alloc");
+    ckm(cudaMalloc(&M->err, sizeof(int)), "mlp alloc");
+    ckm(cudaMemsetAsync(M->err, 0, sizeof(int), M->s), "memset");
     ckm(cudaMemcpyAsync(M->w, w.data(), fb, cudaMemcpyHostToDevice, M->s), "mlp init");
     ckm(cudaMemsetAsync(M->g, 0, fb, M->s), "memset");
     ckm(cudaMemsetAsync(M->m, 0, fb, M->s), "memset");
@@ -597,7 +547,7 @@ heomgb_status heomgb_mlp_forward(heomgb_mlp* M, const float* x_dev, float* y_dev
   return mguard([&] {
     if (!M || !x_dev || !y_dev || batch < 1) throw std::invalid_argument("bad argument");
     forward(M, x_dev, y_dev, batch);
-    ckm(cudaStreamSynchronize(M->s), "sync");
+    check_err(M);
   });
 }
 

@@ -3,9 +3,12 @@
 THE ORACLE, NOT THE PRODUCT: tests use it to check the CUDA forward,
 backward and inference kernels of the terminator (libheom_gb300/csrc/mlp.cu).
 
-* MLP: x -> Linear(h) -> GELU -> Linear(h) -> GELU -> Linear(d_out); the
-  weight matrices are rounded to BF16 (round to nearest even) as the device
-  copies are, biases stay FP32, all arithmetic in float64 here.
+* MLP: x -> Linear(h) -> GELU -> Linear(h) -> GELU -> Linear(d_out).  Every
+  product is a BF16 GEMM on the device (both operands rounded to BF16, round to
+  nearest even, FP32 accumulation): here the weight matrices and each GEMM's
+  other operand (the layer input, or the back-propagated gradient) are
+  rounded to BF16 the same way, biases and bias gradients stay unrounded, and
+  the arithmetic is float64.
 * Terminator features of a tier-N ADO rho_n and mode k:
   [Re rho/s, Im rho/s, onehot(k), Re A/s, Im A/s], s = max |rho_n|,
   A = (n_k+1) (-i s_k (v_a - v_b) + a_k (v_a + v_b)) rho_ab / (ngamma_n + gamma_kk).
@@ -26,6 +29,11 @@ def bf16(x):
     rounding = ((u >> 16) & 1) + 0x7FFF
     u = ((u + rounding) >> 16) << 16
     return u.astype(np.uint32).view(np.float32)
+
+
+def q(x):
+    """A GEMM operand as the device stages it: float32, then BF16 (float64 out)."""
+    return bf16(np.asarray(x, dtype=np.float64).astype(np.float32)).astype(np.float64)
 
 
 def unpack(params, din, h, dout):
@@ -50,11 +58,11 @@ def gelu_grad(z):
 
 def forward(params, x, din, h, dout):
     W1, b1, W2, b2, W3, b3 = unpack(params, din, h, dout)
-    z1 = x @ W1.T + b1
+    z1 = q(x) @ W1.T + b1
     a1 = gelu(z1)
-    z2 = a1 @ W2.T + b2
+    z2 = q(a1) @ W2.T + b2
     a2 = gelu(z2)
-    return a2 @ W3.T + b3, (z1, a1, z2, a2)
+    return q(a2) @ W3.T + b3, (z1, a1, z2, a2)
 
 
 def softplus(z):
@@ -96,13 +104,13 @@ def gradients(params, x, t, din, h, dout, loss_kind=0):
     else:
         dy = 2.0 * (y - t) / y.size
         loss = float(np.mean((y - t) ** 2))
-    gW3 = dy.T @ a2
+    gW3 = q(dy).T @ q(a2)
     gb3 = dy.sum(0)
-    d2 = (dy @ W3) * gelu_grad(z2)
-    gW2 = d2.T @ a1
+    d2 = (q(dy) @ W3) * gelu_grad(z2)
+    gW2 = q(d2).T @ q(a1)
     gb2 = d2.sum(0)
-    d1 = (d2 @ W2) * gelu_grad(z1)
-    gW1 = d1.T @ x
+    d1 = (q(d2) @ W2) * gelu_grad(z1)
+    gW1 = q(d1).T @ q(x)
     gb1 = d1.sum(0)
     return np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gW3.ravel(), gb3]), loss
 

@@ -60,14 +60,16 @@ def _aggregate(n, eps, J, lam_cm, gamma_c_fs, temp_k, n_matsubara, depth, name, 
                       S=[S] * U, A=[A] * U, s_delta=[sd] * U, max_depth=depth, name=name, meta=meta)
 
 
-def exciton_7site(seed=1, depth=4) -> HeomParams:
+def exciton_7site(seed=1, depth=4, lam_cm=35.0, temp_k=300.0, gamma_c_fs=1.0 / 50.0) -> HeomParams:
+    """The 7-site aggregate; lam_cm, temp_k and gamma_c_fs vary the baths
+    (the defaults are the measured workload's)."""
     rng = np.random.default_rng(seed)
     n = 7
     eps = rng.normal(0.0, 100.0, n)
     J = rng.uniform(-100.0, 100.0, (n, n))
     J = np.triu(J, 1)
     J = J + J.T
-    return _aggregate(n, eps, J, 35.0, 1.0 / 50.0, 300.0, 1, depth, "exciton_7site",
+    return _aggregate(n, eps, J, lam_cm, gamma_c_fs, temp_k, 1, depth, "exciton_7site",
                       dict(solver="rkdp", dt=0.1, atol=1e-8, rtol=1e-8, t_final=1000.0))
 
 

@@ -162,6 +162,18 @@ def features(p: HeomParams, n_tab, rho_shallow, first):
     return X.reshape(T * K, 4 * n2 + K).astype(np.float32), s
 
 
+def sample_exciton7(rng, depth):
+    """7-site aggregates around the measured workload: a seeded Hamiltonian
+    (site energies ~N(0, 100 cm^-1), couplings ~U(-100, 100) cm^-1), the
+    reorganisation energy log-uniform in [15, 80] cm^-1 and the temperature
+    uniform in [200, 400] K (gamma_c = 1/50 fs)."""
+    from .configs import exciton_7site
+    seed = int(rng.integers(1, 1 << 30))
+    lam = math.exp(rng.uniform(math.log(15.0), math.log(80.0)))
+    temp = rng.uniform(200.0, 400.0)
+    return exciton_7site(seed=seed, depth=depth, lam_cm=lam, temp_k=temp), (seed, lam, temp)
+
+
 def sample_spin_boson(rng, depth):
     """Spin-boson parameters over the batched-sweep ranges."""
     from .configs import spin_boson
@@ -179,22 +191,35 @@ def admits(qme) -> bool:
     return qme.get_precision()["cancel_log10"] <= CANCEL_MAX
 
 
-def deep_trajectories(params, t_samples, dt=0.005, precision="fp64"):
+def deep_trajectories(params, t_samples, dt=0.005, precision="fp64", keep=None):
     """Plain-method states of a batch of (deep) instances at t_samples; returns
-    a list per instance of arrays (n_t, n_hrchy, n, n) and the mask of the
-    instances that stay bounded and that the closure applies to."""
+    a list per instance of arrays (n_t, n_keep, n, n) and the mask of the
+    instances that stay bounded and that the closure applies to.  keep: only
+    the first `keep` ADOs of every frame are kept (the tiers a shallower model
+    and its closure need), so deep batches need not be stored whole."""
     from .heom import batch_solver, from_params, rk4
     qmes = [from_params(p, precision=precision) for p in params]
     gate = [admits(q) for q in qmes]
     bs = batch_solver(qmes, rk4())
     rho = np.concatenate([p.rho0_ground().ravel() for p in params])
     off = bs.offsets()
-    frames = []
-    bs.solve(rho, [0.0] + list(t_samples), lambda t: frames.append(rho.copy()), {"dt": dt})
-    frames = np.array(frames[1:])
+    frames = [[] for _ in params]
+    seen = [0]
+
+    def grab(t):
+        seen[0] += 1
+        if seen[0] == 1:  # the initial state
+            return
+        for i, p in enumerate(params):
+            n2 = p.n_level ** 2
+            nk = p.n_hrchy() if keep is None else min(keep, p.n_hrchy())
+            frames[i].append(rho[off[i]:off[i] + nk * n2].copy())
+
+    bs.solve(rho, [0.0] + list(t_samples), grab, {"dt": dt})
     out, stable = [], []
     for i, p in enumerate(params):
-        a = frames[:, off[i]:off[i + 1]].reshape(len(t_samples), p.n_hrchy(), p.n_level, p.n_level)
+        nk = p.n_hrchy() if keep is None else min(keep, p.n_hrchy())
+        a = np.array(frames[i]).reshape(len(t_samples), nk, p.n_level, p.n_level)
         ok = bool(gate[i] and np.all(np.isfinite(a)) and np.abs(a[:, 0]).max() <= 2.0)
         out.append(a)
         stable.append(ok)
@@ -219,7 +244,9 @@ def make_dataset(params_deep, shallow_depth, t_samples, dt=0.005):
     K = p0.n_modes
     first = nh_sh - (comb(K + shallow_depth - 1, shallow_depth) if shallow_depth > 0 else 1)
     assert np.array_equal(n_deep[:nh_sh], n_sh)
-    traj, stable = deep_trajectories(params_deep, t_samples, dt)
+    # the tiers up to N + 1 (the targets' tier) of the deep frames
+    keep = comb(K + shallow_depth + 1, shallow_depth + 1)
+    traj, stable = deep_trajectories(params_deep, t_samples, dt, keep=keep)
     Xs, Ts = [], []
     n2 = p0.n_level ** 2
     for p, tr, ok in zip(params_deep, traj, stable):

@@ -1,5 +1,8 @@
-"""Learned terminator: the CUDA MLP kernels against the numpy oracle, and the
-terminator's inference feeding the right-hand side."""
+"""Learned terminator: the CUDA MLP kernels (BF16 tensor-core GEMMs) against
+the numpy oracle, and the terminator's inference feeding the right-hand side.
+The oracle rounds every GEMM operand to BF16 as the device does and sums in
+float64; the device sums in FP32, and an activation computed in FP32 can round
+to the neighbouring BF16 value, so outputs agree to 1e-3 of their scale."""
 import numpy as np
 import pytest
 
@@ -18,7 +21,8 @@ def _dev(a):
 
 
 @pytest.mark.parametrize("din,h,dout,B,kind", [(19, 256, 8, 300, 0), (210, 256, 98, 70, 0), (5, 48, 3, 1, 0),
-                                                (19, 256, 8, 300, 1), (210, 256, 98, 70, 1)])
+                                                (19, 256, 8, 300, 1), (210, 256, 98, 70, 1),
+                                                (210, 256, 98, 4100, 1), (300, 320, 40, 257, 0)])
 def test_forward_and_gradients_match_numpy(din, h, dout, B, kind):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(din)
@@ -36,11 +40,11 @@ def test_forward_and_gradients_match_numpy(din, h, dout, B, kind):
     mlp.forward(xd.data_ptr(), y.data_ptr(), B)
     params = mlp.get_params()
     yref, _ = mlp_oracle.forward(params, x.astype(np.float64), din, h, dout)
-    assert np.abs(y.cpu().numpy() - yref).max() <= 1e-4 * (1 + np.abs(yref).max())
+    assert np.abs(y.cpu().numpy() - yref).max() <= 1e-3 * (1 + np.abs(yref).max())
     g, loss = mlp.gradients(xd.data_ptr(), td.data_ptr(), B)
     gref, lref = mlp_oracle.gradients(params, x.astype(np.float64), t.astype(np.float64), din, h, dout, kind)
-    assert abs(loss - lref) <= 1e-4 * abs(lref)
-    assert np.abs(g - gref).max() <= 1e-3 * np.abs(gref).max()
+    assert abs(loss - lref) <= 1e-3 * abs(lref)
+    assert np.abs(g - gref).max() <= 3e-3 * np.abs(gref).max()
 
 
 def test_adam_training_reduces_loss():

@@ -1,6 +1,7 @@
 // Internal declarations shared by the kernels (kernels.cu) and the C ABI (api.cu).
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <atomic>
 
@@ -350,6 +351,24 @@ struct TermModel {
 };
 cudaError_t term_enqueue(heomgb_mlp* M, const TermBuffers& tb, const TermModel& tm, const TermInput& in,
                          bool y_float, cudaStream_t s);
+// The fused inference (tcgemm.cu): features, three tensor-core layers and the
+// gain head of the terminator in one launch.
+struct TermMlpArgs {
+  TermInput in;
+  TermModel tm;
+  int first, n_tier, apt;      // tier-N ADOs [first, first + n_tier); ADOs per CTA (apt K <= 128)
+  int din, h, dout;
+  const __nv_bfloat16* W1;
+  const __nv_bfloat16* W2;
+  const __nv_bfloat16* W3;
+  const float* b1;
+  const float* b2;
+  const float* b3;
+  float2* P;                   // n_tier K rows of n2 predictions
+  int* err;                    // set to 1 if a tensor-core wait ran out
+};
+bool term_fused_ok(int din, int h, int dout, int K);
+cudaError_t launch_term_fused(const TermMlpArgs& a, bool y_float, cudaStream_t s);
 void mlp_dims(const heomgb_mlp* M, int* din, int* h, int* dout);
 // true (and the flag cleared) if a tensor-core GEMM of M's inference gave up a wait
 bool mlp_take_error(heomgb_mlp* M, cudaStream_t s);

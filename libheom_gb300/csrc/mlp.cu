@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdint>
 #include <cstring>
 #include <memory>
@@ -413,6 +414,29 @@ namespace heomgb {
 cudaError_t term_enqueue(heomgb_mlp* M, const TermBuffers& tb, const TermModel& tm, const TermInput& in,
                          bool y_float, cudaStream_t s) {
   if (tb.n_tier <= 0) return cudaSuccess;
+  // one fused launch (features, three tensor-core layers, gain head) where the
+  // sizes allow it; HEOMGB_TERM_FUSED=0 keeps the five-launch form below
+  const char* fused_env = std::getenv("HEOMGB_TERM_FUSED");
+  if (term_fused_ok(M->din, M->h, M->dout, tb.K) && !(fused_env && std::string(fused_env) == "0")) {
+    TermMlpArgs a{};
+    a.in = in;
+    a.tm = tm;
+    a.first = tb.first;
+    a.n_tier = tb.n_tier;
+    a.apt = 128 / tb.K;
+    a.din = M->din;
+    a.h = M->h;
+    a.dout = M->dout;
+    a.W1 = M->wb + M->off[0];
+    a.W2 = M->wb + M->off[2];
+    a.W3 = M->wb + M->off[4];
+    a.b1 = M->w + M->off[1];
+    a.b2 = M->w + M->off[3];
+    a.b3 = M->w + M->off[5];
+    a.P = tb.P;
+    a.err = M->err;
+    return launch_term_fused(a, y_float, s);
+  }
   const int R = tb.n_tier * tb.K;
   if (y_float)
     k_term_pack<float2><<<tb.n_tier, 128, 0, s>>>(in, tm, tb.first, tb.n_tier, tb.X, tb.scale);

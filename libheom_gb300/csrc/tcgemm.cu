@@ -227,7 +227,269 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_bf16(const GemmArgs g) {
                  "r"(static_cast<uint32_t>(g.tmem_cols)));
 }
 
+// ------------------------------------------------------------------ fused terminator inference
+// One launch per stage evaluates the closure for every row (tier-N ADO j,
+// mode k): CTA t takes the rows of ADOs [t * apt, (t + 1) * apt) (apt = 128 / K
+// ADOs, at most 128 rows), builds their input features (the unfused pack's
+// formula) directly into shared memory as BF16 (the K-major core-matrix
+// layout), runs the three layers on the tensor cores with the activations in
+// shared memory and the accumulator in tensor memory (bias and GELU in the
+// epilogue that writes the next layer's operand), and applies the gain head:
+// P[(j K + k) n2 + e] = C_e rho_l[e] / sigma_k, C_e = y_e - i sg_e softplus(z_e).
+
+// One layer: D (tensor memory, 128 x n) = A (shared memory, 128 rows, K = kdim,
+// row-group stride sbo_a) x W^T (W: n rows of kdim BF16, row stride ldw), K in
+// chunks of 64 through the two B stages.  Returns false if a wait ran out (the
+// MMAs in flight are then drained, bounded).
+__device__ bool mma_layer(uint32_t a_base, uint32_t sbo_a, const __nv_bfloat16* W, int n, int kdim, int ldw, int npad,
+                          unsigned char* wb, uint64_t* mbar, uint32_t& parity, uint32_t tmem) {
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(npad >> 3) << 17) |
+                         (static_cast<uint32_t>(kBM >> 4) << 24);
+  const int nk = (kdim + kBK - 1) / kBK;
+  const size_t wbytes = static_cast<size_t>(256) * kBK * 2;
+  uint32_t issued = 0u;
+  bool ok = true;
+  GemmOperand wo{W, 1, ldw, 1};
+  for (int c = 0; c < nk && ok; ++c) {
+    const int b = c & 1;
+    unsigned char* sb = wb + b * wbytes;
+    if ((issued >> b) & 1u) {
+      uint32_t done = 0;
+      if (threadIdx.x == 0) done = g_wait(mbar + b, (parity >> b) & 1u);
+      if (!__syncthreads_or(done)) {
+        ok = false;
+        break;
+      }
+      parity ^= 1u << b;
+      issued &= ~(1u << b);
+    }
+    stage_operand(wo, 0, npad, n, c * kBK, kdim, sb);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (threadIdx.x == 0) {
+      const uint32_t b0 = s_addr(sb);
+#pragma unroll
+      for (int s = 0; s < kBK / 16; ++s)
+        g_mma(tmem, g_desc(a_base + c * (kBK / 8) * 128 + s * 256, 128, sbo_a),
+              g_desc(b0 + s * 256, 128, (kBK / 8) * 128), idesc, (c > 0 || s > 0) ? 1 : 0);
+      g_commit(mbar + b);
+    }
+    issued |= 1u << b;
+  }
+  for (int b = 0; b < 2; ++b) {
+    if (!((issued >> b) & 1u)) continue;
+    uint32_t done = 0;
+    if (threadIdx.x == 0) done = g_wait(mbar + b, (parity >> b) & 1u);
+    done = __syncthreads_or(done);
+    parity ^= 1u << b;
+    ok = ok && done;
+  }
+  fence_after();
+  return ok;
+}
+
+// Epilogue of a hidden layer: row r = 32 (w % 4) + lane, columns of half w / 4;
+// bias, GELU, BF16, written as the next layer's A operand (K = h, row-group
+// stride (h / 8) * 128).
+__device__ void hidden_epilogue(uint32_t tmem, const float* bias, int h, unsigned char* act) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, sp = warp & 3, half = warp >> 2;
+  const int r = sp * 32 + lane, cols = h / 2, c0 = half * cols;
+  const int sbo = (h / 8) * 128;
+  for (int q = 0; q < cols; q += 8) {
+    float v[8];
+    g_ld8(tmem + (static_cast<uint32_t>(sp * 32) << 16) + static_cast<uint32_t>(c0 + q), v);
+    uint32_t w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const __nv_bfloat162 hv = __floats2bfloat162_rn(gelu_f(v[2 * j] + bias[c0 + q + 2 * j]),
+                                                      gelu_f(v[2 * j + 1] + bias[c0 + q + 2 * j + 1]));
+      w[j] = *reinterpret_cast<const uint32_t*>(&hv);
+    }
+    const int kq = (c0 + q) >> 3;
+    *reinterpret_cast<uint4*>(act + (r >> 3) * sbo + kq * 128 + (r & 7) * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  fence_before();
+  __syncthreads();
+  fence_after();
+}
+
+template <typename TB>
+__global__ void __launch_bounds__(kThreads, 1) k_term_mlp(const TermMlpArgs A) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const TermModel& tm = A.tm;
+  const int n = tm.n, n2 = n * n, K = tm.K, din = A.din, h = A.h, dout = A.dout;
+  const int kpad1 = (din + kBK - 1) / kBK * kBK;
+  unsigned char* act = smem_raw;                         // 128 x 256 BF16
+  unsigned char* wb = smem_raw + 128 * 256 * 2;          // two 256 x 64 BF16 stages (later: the outputs)
+  float* ys = reinterpret_cast<float*>(wb);              // 128 x dout FP32 (after the last layer)
+  float* s_ado = reinterpret_cast<float*>(wb + 2 * 256 * kBK * 2);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(s_ado + 128);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
+  const int j0 = blockIdx.x * A.apt, na = min(A.apt, A.n_tier - j0), rows = na * K;
+  const int cur = A.in.ctl ? A.in.ctl->cur : 0;
+  const void* ysel = A.in.y_sel == 1 ? A.in.yb[cur] : (A.in.y_sel == 2 ? A.in.yb[1 - cur] : A.in.y_fixed);
+  const TB* y = static_cast<const TB*>(ysel);
+  if (threadIdx.x < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s_addr(tslot)),
+                 "r"(256u));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_addr(mbar)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(s_addr(mbar + 1)));
+    asm volatile("fence.mbarrier_init.release.cluster;\n");
+  }
+  // the scale s of every ADO of the tile: sqrt(max_e |rho_l[e]|^2) (a warp per ADO)
+  for (int j = threadIdx.x >> 5; j < na; j += kThreads / 32) {
+    const TB* yl = y + static_cast<size_t>(A.first + j0 + j) * n2;
+    float mx = 0.f;
+    for (int e = threadIdx.x & 31; e < n2; e += 32) {
+      const float re = static_cast<float>(yl[e].x), im = static_cast<float>(yl[e].y);
+      mx = fmaxf(mx, re * re + im * im);
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) s_ado[j] = sqrtf(mx) + 1e-30f;
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *tslot;
+  // input features, 8 per thread and unit (16 bytes of the core-matrix layout)
+  {
+    const int nq = kpad1 / 8, sbo = nq * 128, units = 128 * nq;
+    for (int u = threadIdx.x; u < units; u += kThreads) {
+      const int r8 = u & 7, q = (u >> 3) % nq, g = (u >> 3) / nq, r = g * 8 + r8;
+      float f8[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) f8[t] = 0.f;
+      if (r < rows) {
+        const int j = r / K, k = r - j * K, l = A.first + j0 + j;
+        const TB* yl = y + static_cast<size_t>(l) * n2;
+        const float inv = 1.0f / s_ado[j];
+        int ub = 0;
+        while (ub + 1 < tm.U && tm.bath_ptr[ub + 1] <= k) ++ub;
+        const double2 sk = tm.s[k], ak = tm.a[k], gk = tm.gdiag[k], gl = tm.ngd[l];
+        const double nk1 = static_cast<double>(tm.nidx[static_cast<size_t>(l) * K + k]) + 1.0;
+        const double dr = gl.x + gk.x, di = gl.y + gk.y, dd = dr * dr + di * di;
+        const double ir = dd > 0.0 ? dr / dd : 0.0, ii = dd > 0.0 ? -di / dd : 0.0;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          const int f = q * 8 + t;
+          float v = 0.f;
+          if (f < 2 * n2) {
+            const int e = f < n2 ? f : f - n2;
+            v = static_cast<float>(f < n2 ? yl[e].x : yl[e].y) * inv;
+          } else if (f < 2 * n2 + K) {
+            v = (f - 2 * n2 == k) ? 1.f : 0.f;
+          } else if (f < din) {
+            const int g2 = f - 2 * n2 - K;
+            const int e = g2 < n2 ? g2 : g2 - n2;
+            const int a = e / n, b = e - a * n;
+            const double2 va = tm.V[static_cast<size_t>(ub) * n2 + a * n + a];
+            const double2 vb = tm.V[static_cast<size_t>(ub) * n2 + b * n + b];
+            const double mr = va.x - vb.x, mi = va.y - vb.y, pr = va.x + vb.x, pi = va.y + vb.y;
+            const double t1r = sk.x * mr - sk.y * mi, t1i = sk.x * mi + sk.y * mr;
+            const double cr = t1i + (ak.x * pr - ak.y * pi), ci = -t1r + (ak.x * pi + ak.y * pr);
+            const double yr = static_cast<double>(yl[e].x), yi = static_cast<double>(yl[e].y);
+            const double zr = cr * yr - ci * yi, zi = cr * yi + ci * yr;
+            const double wr = zr * ir - zi * ii, wi = zr * ii + zi * ir;
+            v = static_cast<float>((g2 < n2 ? wr : wi) * nk1) * inv;
+          }
+          f8[t] = v;
+        }
+      }
+      uint32_t w[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const __nv_bfloat162 hv = __floats2bfloat162_rn(f8[2 * t], f8[2 * t + 1]);
+        w[t] = *reinterpret_cast<const uint32_t*>(&hv);
+      }
+      *reinterpret_cast<uint4*>(act + g * sbo + q * 128 + r8 * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+  }
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  fence_before();
+  __syncthreads();
+  fence_after();
+  uint32_t parity = 0u;
+  const int npad3 = (dout + 15) / 16 * 16;
+  bool ok = mma_layer(s_addr(act), (kpad1 / 8) * 128, A.W1, h, din, din, h, wb, mbar, parity, tmem);
+  if (ok) hidden_epilogue(tmem, A.b1, h, act);
+  ok = ok && mma_layer(s_addr(act), (h / 8) * 128, A.W2, h, h, h, h, wb, mbar, parity, tmem);
+  if (ok) hidden_epilogue(tmem, A.b2, h, act);
+  ok = ok && mma_layer(s_addr(act), (h / 8) * 128, A.W3, dout, h, h, npad3, wb, mbar, parity, tmem);
+  if (ok) {  // the outputs into shared memory (the B stages are free now)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, sp = warp & 3, half = warp >> 2;
+    const int r = sp * 32 + lane, cols = npad3 / 2;
+    for (int q = half * cols; q < (half + 1) * cols; q += 8) {
+      float v[8];
+      g_ld8(tmem + (static_cast<uint32_t>(sp * 32) << 16) + static_cast<uint32_t>(q), v);
+#pragma unroll
+      for (int t = 0; t < 8; ++t)
+        if (q + t < dout) ys[r * dout + q + t] = v[t] + A.b3[q + t];
+    }
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (threadIdx.x < 32)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(256u));
+  if (!ok) {
+    if (threadIdx.x == 0) atomicExch(A.err, 1);
+    return;
+  }
+  // gain head: the prediction of rho_{n+1_k} for every (row, element)
+  for (int i = threadIdx.x; i < rows * n2; i += kThreads) {
+    const int r = i / n2, e = i - r * n2;
+    const int j = r / K, k = r - j * K, l = A.first + j0 + j;
+    int ub = 0;
+    while (ub + 1 < tm.U && tm.bath_ptr[ub + 1] <= k) ++ub;
+    const int a = e / n, b = e - a * n;
+    const double dv = tm.V[static_cast<size_t>(ub) * n2 + a * n + a].x - tm.V[static_cast<size_t>(ub) * n2 + b * n + b].x;
+    float2 out = make_float2(0.f, 0.f);
+    if (dv != 0.0) {
+      const float sg = dv > 0.0 ? 1.f : -1.f;
+      const float* yr = ys + r * dout;
+      const float cr = yr[e], zz = yr[n2 + e];
+      const float ci = -sg * (fmaxf(zz, 0.f) + log1pf(expf(-fabsf(zz))));
+      const TB rho = y[static_cast<size_t>(l) * n2 + e];
+      const float rr = static_cast<float>(rho.x), ri = static_cast<float>(rho.y);
+      const float pr = cr * rr - ci * ri, pi = cr * ri + ci * rr;  // C rho
+      const double2 sk = tm.sigma[k];
+      const double sd = sk.x * sk.x + sk.y * sk.y;
+      const float ir = static_cast<float>(sk.x / sd), ii = static_cast<float>(-sk.y / sd);
+      out = make_float2(pr * ir - pi * ii, pr * ii + pi * ir);
+    }
+    A.P[(static_cast<size_t>(j0 + j) * K + k) * n2 + e] = out;
+  }
+}
+
 }  // namespace
+
+bool term_fused_ok(int din, int h, int dout, int K) {
+  return din <= 256 && h % kBK == 0 && h >= 64 && h <= 256 && dout <= 128 && K >= 1 && K <= 128;
+}
+
+size_t term_fused_smem() { return 128 * 256 * 2 + 2 * 256 * kBK * 2 + 128 * sizeof(float) + 32; }
+
+cudaError_t launch_term_fused(const TermMlpArgs& a, bool y_float, cudaStream_t s) {
+  if (a.n_tier <= 0) return cudaSuccess;
+  const size_t smem = term_fused_smem();
+  const int grid = (a.n_tier + a.apt - 1) / a.apt;
+  const void* kern = y_float ? reinterpret_cast<const void*>(k_term_mlp<float2>)
+                             : reinterpret_cast<const void*>(k_term_mlp<double2>);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  if (y_float)
+    k_term_mlp<float2><<<grid, kThreads, smem, s>>>(a);
+  else
+    k_term_mlp<double2><<<grid, kThreads, smem, s>>>(a);
+  ++g_launches;
+  return cudaGetLastError();
+}
 
 size_t gemm_smem(int bn) {
   return 2 * (static_cast<size_t>(kBM) * kBK * 2 + static_cast<size_t>(bn) * kBK * 2) + 32;

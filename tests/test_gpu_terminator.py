@@ -57,13 +57,21 @@ def test_adam_training_reduces_loss():
     assert losses[-1] < 0.05 * losses[0]
 
 
-def test_terminator_feeds_rhs_like_numpy():
-    p = configs.spin_boson(eps=0.3, lam=0.4, beta=1.5, depth=3)
+@pytest.mark.parametrize("fused", ["1", "0"])
+@pytest.mark.parametrize("which", ["spin_boson", "exciton7"])
+def test_terminator_feeds_rhs_like_numpy(fused, which, monkeypatch):
+    """The closure's predictions enter the +1 terms of the truncated tier, by
+    the fused inference launch (features, three tensor-core layers and the
+    gain head in one kernel) and by the five-launch form."""
+    monkeypatch.setenv("HEOMGB_TERM_FUSED", fused)
+    p = (configs.spin_boson(eps=0.3, lam=0.4, beta=1.5, depth=3) if which == "spin_boson"
+         else configs.exciton_7site(depth=2))
     din, dout = T.dims(p)
     mlp = T.MLP(din, 256, dout, seed=7)
     q = lh.from_params(p)
     rng = np.random.default_rng(2)
-    rho = (rng.standard_normal((p.n_hrchy(), 2, 2)) + 1j * rng.standard_normal((p.n_hrchy(), 2, 2))) * 0.3
+    shape = (p.n_hrchy(), p.n_level, p.n_level)
+    rho = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) * 0.3
     plain = q.calc_diff(rho)
     T.attach(q, mlp)
     got = q.calc_diff(rho)
@@ -73,16 +81,18 @@ def test_terminator_feeds_rhs_like_numpy():
     first = int(np.argmax(n_tab.sum(1) == p.max_depth))
     X, s = mlp_oracle.term_features(p, n_tab, rho, first)
     Y, _ = mlp_oracle.forward(mlp.get_params(), X, din, 256, dout)
-    v = np.diag(p.V[0])
-    cphi = 1j * (v[:, None] - v[None, :])
-    sg = np.sign((v[:, None] - v[None, :]).real).ravel()
+    bath_of, _, _, _, sig = T._mode_constants(p)
+    n = p.n_level
     expect = plain.copy()
     K = p.n_modes
     for j, l in enumerate(range(first, nh)):
         for k in range(K):
+            v = np.diag(p.V[bath_of[k]])
+            cphi = 1j * (v[:, None] - v[None, :])
+            sg = np.sign((v[:, None] - v[None, :]).real).ravel()
             C = mlp_oracle.gain_head(Y[j * K + k], sg) * np.abs(sg)
-            pred = (C * rho[l].ravel()).reshape(2, 2) / p.sigma[0][k]
-            expect[l] -= cphi * p.sigma[0][k] * pred
+            pred = (C * rho[l].ravel()).reshape(n, n) / sig[k]
+            expect[l] -= cphi * sig[k] * pred
     scale = np.abs(plain).max()
     assert np.abs(got - expect).max() <= 1e-5 * scale
     assert np.abs(got - plain).max() > 1e-8 * scale  # the terminator does contribute

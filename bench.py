@@ -374,6 +374,77 @@ def secondary_aggregate24(stream, fma_peaks, steps=3):
     return out
 
 
+def north_star_exciton7(stream, plain_ms, chosen_ms, steps=3):
+    """The 7-site workload to t_final = 1 ps (Dormand-Prince, atol = rtol = 1e-8)
+    in four forms: plain FP64 depth 4 (the drop-in), mixed depth 4 (the chosen
+    form), and depth 3 with plain truncation and with the learned closure
+    (mixed; the closure trained here by the library's kernels on 8 seeded
+    depth-6 trajectories, about 20 s).  Each form's error is max over t = 0,
+    100, ..., 1000 fs of max |delta rho_0| against the depth-6 FP64 solve of
+    the same aggregate (3060 vs 38760 ADOs), its time the median of `steps`
+    device solves."""
+    import torch
+
+    import libheom_gb300 as lh
+    from libheom_gb300 import configs
+    from libheom_gb300 import terminator as T
+    kw = dict(dt=0.1, atol=1e-8, rtol=1e-8)
+    t_out = [100.0 * i for i in range(11)]
+
+    def rho0_traj(p, precision, mlp=None):
+        q = lh.from_params(p, precision=precision)
+        if mlp is not None:
+            T.attach(q, mlp)
+        qs = lh.qme_solver(q, lh.rkdp())
+        rho = p.rho0_ground()
+        out = []
+        qs.solve(rho, t_out, lambda t: out.append(rho[0].copy()), dict(kw))
+        return np.array(out), qs, q
+
+    def timed(qs, p):
+        r0 = torch.from_numpy(p.rho0_ground().ravel()).cuda()
+        r = torch.empty_like(r0)
+        ms = []
+        for i in range(steps + 1):
+            with torch.cuda.stream(stream):
+                r.copy_(r0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            qs.solve_device(r.data_ptr(), [0.0, 1000.0], None, dict(kw))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i > 0:
+                ms.append(e0.elapsed_time(e1))
+        return statistics.median(ms)
+
+    t0 = time.perf_counter()
+    rng = np.random.default_rng(31)
+    deep = [T.sample_exciton7(rng, 6)[0] for _ in range(8)]
+    X, Tt, _ = T.make_dataset(deep, 3, list(np.arange(20.0, 200.01, 20.0)), dt=1.0)
+    din, dout = T.dims(deep[0])
+    mlp = T.MLP(din, 256, dout, seed=3)
+    mlp.set_loss(1, dout // 2)
+    T.train(mlp, X, Tt, epochs=8, batch=4096, lr=1e-3, cosine=True)
+    train_s = time.perf_counter() - t0
+    ref, _, _ = rho0_traj(configs.exciton_7site(depth=6), "fp64")
+    out = {"workload": "exciton7, rkdp atol=rtol=1e-8 to 1 ps", "reference": "depth-6 FP64 solve (38760 ADOs)",
+           "error": "max over t = 0..1000 fs (every 100 fs) of max |delta rho_0| vs the reference",
+           "closure_training_s": train_s, "closure_training": "8 depth-6 trajectories, 8 epochs"}
+    forms = {}
+    for name, depth, prec, use in (("plain_fp64_depth4", 4, "fp64", False), ("mixed_depth4", 4, "mixed", False),
+                                   ("mixed_depth3_truncated", 3, "mixed", False),
+                                   ("mixed_depth3_closure", 3, "mixed", True)):
+        p = configs.exciton_7site(depth=depth)
+        traj, qs, _ = rho0_traj(p, prec, mlp if use else None)
+        ms = plain_ms if name == "plain_fp64_depth4" else (chosen_ms if name == "mixed_depth4" else timed(qs, p))
+        forms[name] = {"ms_to_t_final": ms, "err_vs_depth6": float(np.abs(traj - ref).max()),
+                       "n_hrchy": p.n_hrchy()}
+    for f in forms.values():
+        f["speedup_vs_plain_fp64"] = plain_ms / f["ms_to_t_final"]
+    out["forms"] = forms
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -555,6 +626,9 @@ def run_ours(args):
             "gpu_launches": launches, "e2e": e2e, "roofline": roof, "clocks": clocks}
     if rank == 0 and world == 1 and args.workload == "exciton7" and not args.no_secondary:
         line["secondary"] = {"aggregate24": secondary_aggregate24(stream, fma_peaks)}
+        if plain is not None:
+            line["secondary"]["north_star_exciton7"] = north_star_exciton7(stream, plain["ms_per_step"],
+                                                                           total_ms / args.steps)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(w, keep_states=True)
         sample = cb.pop("_final")

@@ -330,6 +330,8 @@ struct heomgb_qme {
   DiagInst dinst{};          // diagonal-coupling instance (PATH_DIAG), device pointers into arena
   DiagPlan diff_plan;        // tiles for calc_diff
   heomgb_mlp* term = nullptr;  // learned terminator (not owned); null = plain truncation
+  const float2* term_cke = nullptr;  // its set-up tables (TermModel::cke, sgn), in term_arena
+  const float* term_sgn = nullptr;
   TermBuffers diff_tb;       // terminator buffers for calc_diff
   DeviceArena term_arena;
   DeviceArena arena;
@@ -1017,6 +1019,8 @@ TermModel term_model(const heomgb_qme* q) {
   tm.sigma = q->dm.sigma;
   tm.V = q->dm.V;
   tm.bath_ptr = q->dm.bath_ptr;
+  tm.cke = q->term_cke;
+  tm.sgn = q->term_sgn;
   return tm;
 }
 
@@ -2178,10 +2182,46 @@ heomgb_status heomgb_qme_set_terminator(heomgb_qme* q, heomgb_mlp* mlp) {
     q->diff_tb = TermBuffers{};
     q->term = mlp;
     DiagInst di = q->dinst;
+    q->term_cke = nullptr;
+    q->term_sgn = nullptr;
     if (mlp) {
       alloc_term(q->term_arena, q, q->diff_tb);
       di.term_p = q->diff_tb.P;
       di.term_first = q->diff_tb.first;
+      // per mode k and element e: -i s_k (v_a - v_b) + a_k (v_a + v_b), sign(Re(v_a - v_b))
+      const int n = q->n, n2 = n * n, K = q->K;
+      std::vector<cd> sv, av;
+      std::vector<int> bath_of;
+      for (int u = 0; u < q->U; ++u) {
+        const Bath& B = q->baths[u];
+        for (int k = 0; k < B.len; ++k) {
+          cd sk(0.0, 0.0), ak(0.0, 0.0);  // s = S phi_0, a = A phi_0 as the model forms them
+          for (int j = 0; j < B.len; ++j) {
+            const cd Sv = B.S[static_cast<size_t>(k) * B.len + j], Av = B.A[static_cast<size_t>(k) * B.len + j];
+            if (Sv != cd(0.0, 0.0)) sk += Sv * B.phi0[j];
+            if (Av != cd(0.0, 0.0)) ak += Av * B.phi0[j];
+          }
+          sv.push_back(sk);
+          av.push_back(ak);
+          bath_of.push_back(u);
+        }
+      }
+      std::vector<cd> cke(static_cast<size_t>(K) * n2);
+      std::vector<float> sgn(static_cast<size_t>(K) * n2);
+      const cd I(0.0, 1.0);
+      for (int k = 0; k < K; ++k) {
+        const Bath& B = q->baths[bath_of[k]];
+        for (int a = 0; a < n; ++a)
+          for (int b = 0; b < n; ++b) {
+            const cd va = B.V[static_cast<size_t>(a) * n + a], vb = B.V[static_cast<size_t>(b) * n + b];
+            cke[static_cast<size_t>(k) * n2 + a * n + b] = -I * sv[k] * (va - vb) + av[k] * (va + vb);
+            const double dv = (va - vb).real();
+            sgn[static_cast<size_t>(k) * n2 + a * n + b] = dv > 0.0 ? 1.f : (dv < 0.0 ? -1.f : 0.f);
+          }
+      }
+      q->term_cke = q->term_arena.upload(to_f2(cke), q->stream());
+      q->term_sgn = q->term_arena.upload(sgn, q->stream());
+      ck(cudaStreamSynchronize(q->stream()), "terminator tables");
     }
     build_plan(q->diff_plan, {di}, q->diff_plan.block, q->diff_plan.ept, q->diff_plan.min_blocks,
                q->precision_eff == HEOMGB_MIXED, q->n_sm,

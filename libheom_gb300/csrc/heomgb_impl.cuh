@@ -348,6 +348,11 @@ struct TermModel {
   const double2* sigma = nullptr; // K
   const double2* V = nullptr;     // U*n2
   const int* bath_ptr = nullptr;  // U+1
+  // set-up tables of the fused inference (k, e = a n + b): the adiabatic
+  // estimate's coefficient -i s_k (v_a - v_b) + a_k (v_a + v_b) and the gain
+  // head's sign(Re(v_a - v_b)), for V of mode k's bath
+  const float2* cke = nullptr;    // K * n2
+  const float* sgn = nullptr;     // K * n2
 };
 cudaError_t term_enqueue(heomgb_mlp* M, const TermBuffers& tb, const TermModel& tm, const TermInput& in,
                          bool y_float, cudaStream_t s);

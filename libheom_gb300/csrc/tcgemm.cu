@@ -326,7 +326,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_term_mlp(const TermMlpArgs A) {
   unsigned char* wb = smem_raw + 128 * 256 * 2;          // two 256 x 64 BF16 stages (later: the outputs)
   float* ys = reinterpret_cast<float*>(wb);              // 128 x dout FP32 (after the last layer)
   float* s_ado = reinterpret_cast<float*>(wb + 2 * 256 * kBK * 2);
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(s_ado + 128);
+  float2* rowf = reinterpret_cast<float2*>(s_ado + 128);  // per row: (n_k + 1) / (ngamma_l + gamma_kk)
+  float2* isig = rowf + 128;                              // per mode: 1 / sigma_k (K <= 128)
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(isig + 128);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
   const int j0 = blockIdx.x * A.apt, na = min(A.apt, A.n_tier - j0), rows = na * K;
   const int cur = A.in.ctl ? A.in.ctl->cur : 0;
@@ -353,6 +355,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_term_mlp(const TermMlpArgs A) {
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) s_ado[j] = sqrtf(mx) + 1e-30f;
   }
+  for (int k = threadIdx.x; k < K; k += kThreads) {
+    const double2 sk = tm.sigma[k];
+    const double sd = sk.x * sk.x + sk.y * sk.y;
+    isig[k] = make_float2(static_cast<float>(sk.x / sd), static_cast<float>(-sk.y / sd));
+  }
+  // the row factors, in FP64 once per row (the per-feature work below is FP32)
+  for (int r = threadIdx.x; r < rows; r += kThreads) {
+    const int j = r / K, k = r - j * K, l = A.first + j0 + j;
+    const double2 gk = tm.gdiag[k], gl = tm.ngd[l];
+    const double nk1 = static_cast<double>(tm.nidx[static_cast<size_t>(l) * K + k]) + 1.0;
+    const double dr = gl.x + gk.x, di = gl.y + gk.y, dd = dr * dr + di * di;
+    rowf[r] = dd > 0.0 ? make_float2(static_cast<float>(nk1 * dr / dd), static_cast<float>(-nk1 * di / dd))
+                       : make_float2(0.f, 0.f);
+  }
   fence_before();
   __syncthreads();
   fence_after();
@@ -369,12 +385,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_term_mlp(const TermMlpArgs A) {
         const int j = r / K, k = r - j * K, l = A.first + j0 + j;
         const TB* yl = y + static_cast<size_t>(l) * n2;
         const float inv = 1.0f / s_ado[j];
-        int ub = 0;
-        while (ub + 1 < tm.U && tm.bath_ptr[ub + 1] <= k) ++ub;
-        const double2 sk = tm.s[k], ak = tm.a[k], gk = tm.gdiag[k], gl = tm.ngd[l];
-        const double nk1 = static_cast<double>(tm.nidx[static_cast<size_t>(l) * K + k]) + 1.0;
-        const double dr = gl.x + gk.x, di = gl.y + gk.y, dd = dr * dr + di * di;
-        const double ir = dd > 0.0 ? dr / dd : 0.0, ii = dd > 0.0 ? -di / dd : 0.0;
+        const float2 fr = rowf[r];
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
           const int f = q * 8 + t;
@@ -384,19 +395,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_term_mlp(const TermMlpArgs A) {
             v = static_cast<float>(f < n2 ? yl[e].x : yl[e].y) * inv;
           } else if (f < 2 * n2 + K) {
             v = (f - 2 * n2 == k) ? 1.f : 0.f;
-          } else if (f < din) {
+          } else if (f < din) {  // the adiabatic estimate (n_k + 1) c_ke rho_e / (ngamma_l + gamma_kk), in FP32
             const int g2 = f - 2 * n2 - K;
             const int e = g2 < n2 ? g2 : g2 - n2;
-            const int a = e / n, b = e - a * n;
-            const double2 va = tm.V[static_cast<size_t>(ub) * n2 + a * n + a];
-            const double2 vb = tm.V[static_cast<size_t>(ub) * n2 + b * n + b];
-            const double mr = va.x - vb.x, mi = va.y - vb.y, pr = va.x + vb.x, pi = va.y + vb.y;
-            const double t1r = sk.x * mr - sk.y * mi, t1i = sk.x * mi + sk.y * mr;
-            const double cr = t1i + (ak.x * pr - ak.y * pi), ci = -t1r + (ak.x * pi + ak.y * pr);
-            const double yr = static_cast<double>(yl[e].x), yi = static_cast<double>(yl[e].y);
-            const double zr = cr * yr - ci * yi, zi = cr * yi + ci * yr;
-            const double wr = zr * ir - zi * ii, wi = zr * ii + zi * ir;
-            v = static_cast<float>((g2 < n2 ? wr : wi) * nk1) * inv;
+            const float2 c = __ldg(tm.cke + static_cast<size_t>(k) * n2 + e);
+            const float2 cf = make_float2(c.x * fr.x - c.y * fr.y, c.x * fr.y + c.y * fr.x);
+            const float yr = static_cast<float>(yl[e].x), yi = static_cast<float>(yl[e].y);
+            v = (g2 < n2 ? cf.x * yr - cf.y * yi : cf.x * yi + cf.y * yr) * inv;
           }
           f8[t] = v;
         }
@@ -445,23 +450,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_term_mlp(const TermMlpArgs A) {
   for (int i = threadIdx.x; i < rows * n2; i += kThreads) {
     const int r = i / n2, e = i - r * n2;
     const int j = r / K, k = r - j * K, l = A.first + j0 + j;
-    int ub = 0;
-    while (ub + 1 < tm.U && tm.bath_ptr[ub + 1] <= k) ++ub;
-    const int a = e / n, b = e - a * n;
-    const double dv = tm.V[static_cast<size_t>(ub) * n2 + a * n + a].x - tm.V[static_cast<size_t>(ub) * n2 + b * n + b].x;
+    const float sg = __ldg(tm.sgn + static_cast<size_t>(k) * n2 + e);  // sign(Re(v_a - v_b))
     float2 out = make_float2(0.f, 0.f);
-    if (dv != 0.0) {
-      const float sg = dv > 0.0 ? 1.f : -1.f;
+    if (sg != 0.f) {
       const float* yr = ys + r * dout;
       const float cr = yr[e], zz = yr[n2 + e];
       const float ci = -sg * (fmaxf(zz, 0.f) + log1pf(expf(-fabsf(zz))));
       const TB rho = y[static_cast<size_t>(l) * n2 + e];
       const float rr = static_cast<float>(rho.x), ri = static_cast<float>(rho.y);
       const float pr = cr * rr - ci * ri, pi = cr * ri + ci * rr;  // C rho
-      const double2 sk = tm.sigma[k];
-      const double sd = sk.x * sk.x + sk.y * sk.y;
-      const float ir = static_cast<float>(sk.x / sd), ii = static_cast<float>(-sk.y / sd);
-      out = make_float2(pr * ir - pi * ii, pr * ii + pi * ir);
+      const float2 is = isig[k];  // 1 / sigma_k
+      out = make_float2(pr * is.x - pi * is.y, pr * is.y + pi * is.x);
     }
     A.P[(static_cast<size_t>(j0 + j) * K + k) * n2 + e] = out;
   }
@@ -473,7 +472,9 @@ bool term_fused_ok(int din, int h, int dout, int K) {
   return din <= 256 && h % kBK == 0 && h >= 64 && h <= 256 && dout <= 128 && K >= 1 && K <= 128;
 }
 
-size_t term_fused_smem() { return 128 * 256 * 2 + 2 * 256 * kBK * 2 + 128 * sizeof(float) + 32; }
+size_t term_fused_smem() {
+  return 128 * 256 * 2 + 2 * 256 * kBK * 2 + 128 * sizeof(float) + 2 * 128 * sizeof(float2) + 32;
+}
 
 cudaError_t launch_term_fused(const TermMlpArgs& a, bool y_float, cudaStream_t s) {
   if (a.n_tier <= 0) return cudaSuccess;

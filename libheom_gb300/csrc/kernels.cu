@@ -1280,10 +1280,15 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_ls_resident(const Resi
     for (int s = 0; s < 4 && ok; ++s) {
       const float2* Xg = R.Yb[s & 1];
       float2 D[EPT];
-      res_own<HREAL, EPT>(Hs, Yf, n, n2, E, el, D);  // all reads of Yf end before the wait's sync
+      // every thread's reads of Yf (its elements' rows and columns, written by
+      // other threads in the epilogue below) end before that epilogue: the grid
+      // wait syncs the CTA, and the first stage, which has no wait, syncs here
+      res_own<HREAL, EPT>(Hs, Yf, n, n2, E, el, D);
       if (step > 0 || s > 0) {
         ok = grid_wait(R.bar, gen, R.spin_limit);
         if (!ok) break;
+      } else {
+        __syncthreads();
       }
       res_bath<EPT>(Xg, Toff, Tcf, E, D);
 #pragma unroll

@@ -182,3 +182,30 @@ def test_resident_fixed_step_bit_identical(maker, ept, solver, form, monkeypatch
     assert tune["resident"]
     assert st_r["rhs"] == st_s["rhs"]
     assert np.array_equal(res, stg)
+
+
+@pytest.mark.parametrize("solver", ["lsrk4", "rk4"])
+@pytest.mark.parametrize("ept,per_sm", [("1", "1"), ("1", "3"), ("1", "6"), ("2", "2"), ("2", "4")])
+def test_resident_fixed_step_bit_identical_every_shape(solver, ept, per_sm, monkeypatch):
+    """The resident fixed-step intervals give the stage kernels' bits at every
+    grid shape (a shape changes which CTA owns which ADOs and how the threads
+    of a CTA interleave; the LSRK4 kernel once lost a CTA barrier on its first
+    stage and differed only at some shapes)."""
+    p = configs.exciton_7site(depth=3)
+    dt = 0.5
+    t = [0.0, 37 * dt + 0.3 * dt, 60 * dt]
+
+    def go(resident):
+        monkeypatch.setenv("HEOMGB_RESIDENT", "1" if resident else "0")
+        monkeypatch.setenv("HEOMGB_RESIDENT_EPT", ept)
+        monkeypatch.setenv("HEOMGB_RESIDENT_PER_SM", per_sm)
+        monkeypatch.setenv("HEOMGB_LOCAL", "0")
+        qs = lh.qme_solver(lh.from_params(p, precision="mixed"), lh.SOLVERS[solver]())
+        rho = p.rho0_ground()
+        qs.solve(rho, t, None, {"dt": dt})
+        return rho, qs.tuning()
+
+    res, tune = go(True)
+    stg, _ = go(False)
+    assert tune["resident"]
+    assert np.array_equal(res, stg)

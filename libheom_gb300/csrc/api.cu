@@ -247,6 +247,9 @@ void build_plan(DiagPlan& P, const std::vector<DiagInst>& insts, int block, int 
       throw unsupported_error("site-local-bath kernel: one eligible instance and a compiled variant");
     if (sites_smem(insts[0].n, insts[0].K, sites_tile, insts[0].site_w) > cap)
       throw unsupported_error("site-local-bath tile exceeds shared memory");
+    // a thread owns at most one register block of a tile
+    if (static_cast<long long>(sites_tile) * (insts[0].n / sites_rt) * (insts[0].n / 4) > block)
+      throw unsupported_error("site-local-bath tile: more register blocks than threads");
   }
   for (size_t i = 0; i < P.inst.size(); ++i) {
     DiagInst& I = P.inst[i];
@@ -1311,9 +1314,9 @@ void autotune(heomgb_qme_solver* qs) {
         const int per_ado = (insts[0].n / v.rt) * (insts[0].n / 4);
         for (int t = 1; t <= 16; ++t) {
           if (pin_sb && t != pin_st) continue;
-          const int nq = t * per_ado, waves = (nq + b - 1) / b;
-          // every thread busy in at least 85% of the passes over a tile
-          if (!pin_sb && (nq < b / 2 || nq > 4 * b || nq < 0.85 * waves * b)) continue;
+          const int nq = t * per_ado;
+          // one register block per thread, and at least 85 % of the threads busy
+          if (nq > b || (!pin_sb && nq < 0.85 * b)) continue;
           if (sites_smem(insts[0].n, insts[0].K, t, insts[0].site_w) * v.minb > 220 * 1024) continue;
           try {
             build_plan(qs->plan, insts, b, 1, v.minb, qs->mixed, q->n_sm, qs->stream, false, t, v.rt);

@@ -850,7 +850,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
     for (int le = threadIdx.x; le < E; le += blockDim.x) {
       const double2 v = R.S[cur][A.gidx(le, n2)];
       Sv[static_cast<size_t>(cur) * E + le] = v;
-      const float2 f = make_float2(d2f(v.x), d2f(v.y));
+      const float2 f = to_f(v);
       Yf[static_cast<size_t>(cur) * E + le] = f;
       yt[le] = f;
     }
@@ -924,9 +924,10 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
           ff_add_prod(hi.x, lo.x, c_dpBh[5], c_dpBl[5], k.x);
           ff_add_prod(hi.y, lo.y, c_dpBh[5], c_dpBl[5], k.y);
           const double2 sc = Sc[le];
-          const double2 y = make_double2((sc.x + f2d(hi.x)) + f2d(lo.x), (sc.y + f2d(hi.y)) + f2d(lo.y));
+          const double2 hd = to_d(hi), ld = to_d(lo);
+          const double2 y = make_double2((sc.x + hd.x) + ld.x, (sc.y + hd.y) + ld.y);
           Sn[le] = y;
-          const float2 yb = make_float2(d2f(y.x), d2f(y.y));
+          const float2 yb = to_f(y);
           Yn[le] = yb;
           Xn[le] = yb;
           R.Yb[1 - cur][g] = yb;
@@ -1000,7 +1001,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
   for (int le = threadIdx.x; le < E; le += blockDim.x) {
     const double2 v = R.S[0][A.gidx(le, n2)];
     Sv[le] = v;
-    const float2 f = make_float2(d2f(v.x), d2f(v.y));
+    const float2 f = to_f(v);
     Yf[le] = f;
     yt[le] = f;
   }
@@ -1036,15 +1037,16 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
           Xn[le] = y;
           R.Ytmp[s & 1][g] = y;
           double2 a = s == 0 ? Sv[le] : Av[le];
-          a.x += f2d(__fmul_rn(w, k.x));
-          a.y += f2d(__fmul_rn(w, k.y));
+          const double2 kw = to_d(make_float2(__fmul_rn(w, k.x), __fmul_rn(w, k.y)));
+          a.x += kw.x;
+          a.y += kw.y;
           Av[le] = a;
         } else {  // rho = acc + k4/6
           const double2 a = Av[le];
-          const double2 v = make_double2(a.x + f2d(__fmul_rn(1.0f / 6.0f, k.x)),
-                                         a.y + f2d(__fmul_rn(1.0f / 6.0f, k.y)));
+          const double2 k6 = to_d(make_float2(__fmul_rn(1.0f / 6.0f, k.x), __fmul_rn(1.0f / 6.0f, k.y)));
+          const double2 v = make_double2(a.x + k6.x, a.y + k6.y);
           Sv[le] = v;
-          const float2 f = make_float2(d2f(v.x), d2f(v.y));
+          const float2 f = to_f(v);
           Yf[le] = f;
           Xn[le] = f;  // the next step's stage-1 input (yt[0])
           R.Yb[0][g] = f;
@@ -1267,7 +1269,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_ls_resident(const Resi
   for (int le = threadIdx.x; le < E; le += blockDim.x) {
     const double2 v = R.S[0][A.gidx(le, n2)];
     Sv[le] = v;
-    Yf[le] = make_float2(d2f(v.x), d2f(v.y));
+    Yf[le] = to_f(v);
   }
   __syncthreads();
   ResElems<EPT> el;
@@ -1304,9 +1306,10 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_ls_resident(const Resi
         }
         Bv[le] = b;
         const double2 sp = Sv[le];
-        const double2 v = make_double2(fma(B[s], f2d(b.x), sp.x), fma(B[s], f2d(b.y), sp.y));
+        const double2 bd = to_d(b);
+        const double2 v = make_double2(fma(B[s], bd.x, sp.x), fma(B[s], bd.y, sp.y));
         Sv[le] = v;
-        const float2 f = make_float2(d2f(v.x), d2f(v.y));
+        const float2 f = to_f(v);
         Yf[le] = f;
         R.Yb[1 - (s & 1)][el.gi[r]] = f;
       }
@@ -1561,9 +1564,10 @@ __global__ void __launch_bounds__(512, 2) k_fixed_local(const LocalArgs A) {
             const float2 b = s == 0 ? make_float2(__fmul_rn(-fdt, D.x), __fmul_rn(-fdt, D.y))
                                     : make_float2(fmaf(-fdt, D.x, -pf.x), fmaf(-fdt, D.y, -pf.y));
             buf[g] = b;
-            const double2 v = make_double2(fma(Bs, f2d(b.x), pb.x), fma(Bs, f2d(b.y), pb.y));
+            const double2 bd = to_d(b);
+            const double2 v = make_double2(fma(Bs, bd.x, pb.x), fma(Bs, bd.y, pb.y));
             A.S[g] = v;
-            const float2 f = make_float2(d2f(v.x), d2f(v.y));
+            const float2 f = to_f(v);
             A.Yf[g] = f;
             Xn[le] = f;
           } else {
@@ -1590,14 +1594,15 @@ __global__ void __launch_bounds__(512, 2) k_fixed_local(const LocalArgs A) {
             const float w = static_cast<float>(s == 0 ? (1.0 / 6.0) : (2.0 / 6.0));
             Xn[le] = make_float2(fmaf(c, k.x, pf.x), fmaf(c, k.y, pf.y));
             double2 acc = pa;
-            acc.x += f2d(__fmul_rn(w, k.x));
-            acc.y += f2d(__fmul_rn(w, k.y));
+            const double2 kw = to_d(make_float2(__fmul_rn(w, k.x), __fmul_rn(w, k.y)));
+            acc.x += kw.x;
+            acc.y += kw.y;
             A.acc[g] = acc;
           } else {  // rho = acc + k4/6
-            const double2 v = make_double2(pa.x + f2d(__fmul_rn(1.0f / 6.0f, k.x)),
-                                           pa.y + f2d(__fmul_rn(1.0f / 6.0f, k.y)));
+            const double2 k6 = to_d(make_float2(__fmul_rn(1.0f / 6.0f, k.x), __fmul_rn(1.0f / 6.0f, k.y)));
+            const double2 v = make_double2(pa.x + k6.x, pa.y + k6.y);
             A.S[g] = v;
-            const float2 f = make_float2(d2f(v.x), d2f(v.y));
+            const float2 f = to_f(v);
             A.Yf[g] = f;
             Xn[le] = f;
           }
@@ -2186,7 +2191,7 @@ __global__ void k_to_bulk(const double2* src, float2* dst, long long n) {
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * blockDim.x) {
     const double2 v = src[i];
-    dst[i] = make_float2(d2f(v.x), d2f(v.y));
+    dst[i] = to_f(v);
   }
 }
 

@@ -57,6 +57,18 @@ template <> __device__ __forceinline__ double occ<double>(int v) {
 }
 __device__ __forceinline__ double2 to_d(double2 v) { return v; }
 __device__ __forceinline__ double2 to_d(float2 v) { return make_double2(f2d(v.x), f2d(v.y)); }
+// FP64 -> FP32 of a complex value (round to nearest even).  The integer-
+// assembled d2f keeps the FP64 pipe free; a translation unit whose kernels
+// have that pipe to spare and are issue-bound defines
+// HEOMGB_HW_D2F_EPILOGUE to take the hardware conversion instead (the same
+// bits: both are the IEEE conversion).
+__device__ __forceinline__ float2 to_f(double2 v) {
+#if defined(HEOMGB_HW_D2F_EPILOGUE)
+  return make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
+#else
+  return make_float2(d2f(v.x), d2f(v.y));
+#endif
+}
 
 template <typename TC> __device__ __forceinline__ const cx_t<TC>* pick(const double2* d, const float2* f);
 template <> __device__ __forceinline__ const double2* pick<double>(const double2* d, const float2*) { return d; }
@@ -67,7 +79,7 @@ template <typename TC> __device__ __forceinline__ void st_bulk(void* base, size_
   if constexpr (std::is_same<TC, double>::value) {
     static_cast<double2*>(base)[g] = v;
   } else {
-    static_cast<float2*>(base)[g] = make_float2(d2f(v.x), d2f(v.y));
+    static_cast<float2*>(base)[g] = to_f(v);
   }
 }
 template <typename TC> __device__ __forceinline__ double2 ld_bulk(const void* base, size_t g) {
@@ -84,7 +96,7 @@ template <typename TC> __device__ __forceinline__ void st_bulk_cs(void* base, si
   if constexpr (std::is_same<TC, double>::value) {
     __stcs(static_cast<double2*>(base) + g, v);
   } else {
-    __stcs(static_cast<float2*>(base) + g, make_float2(d2f(v.x), d2f(v.y)));
+    __stcs(static_cast<float2*>(base) + g, to_f(v));
   }
 }
 template <typename TC> __device__ __forceinline__ double2 ld_bulk_cs(const void* base, size_t g) {
@@ -99,7 +111,7 @@ template <typename TC> __device__ __forceinline__ double2 as_bulk(double2 v) {
   if constexpr (std::is_same<TC, double>::value) {
     return v;
   } else {
-    return make_double2(f2d(d2f(v.x)), f2d(d2f(v.y)));
+    return to_d(to_f(v));
   }
 }
 
@@ -321,7 +333,9 @@ template <typename TC, int KIND = -1>
 __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> Dc, double dt, int cur,
                                            const EpiPre& p) {
   constexpr bool MIX = std::is_same<TC, float>::value;
-  const double2 D = to_d(Dc);
+  // the mixed form's stage epilogues take the FP32 value; only calc_diff
+  // (EPI_DIFF) and the FP64 form need it in FP64
+  const double2 D = (MIX && (KIND >= 0 ? KIND : st.kind) != EPI_DIFF) ? make_double2(0.0, 0.0) : to_d(Dc);
   switch (KIND >= 0 ? KIND : st.kind) {
     case EPI_DIFF: {
       const double2 ad = cmul(st.alpha, D);
@@ -341,8 +355,9 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
         const float2 k = make_float2(__fmul_rn(-fdt, Dc.x), __fmul_rn(-fdt, Dc.y));
         static_cast<float2*>(st.Ynext)[g] = make_float2(fmaf(static_cast<float>(c), k.x, p.f.x),
                                                         fmaf(static_cast<float>(c), k.y, p.f.y));
-        a.x += f2d(__fmul_rn(static_cast<float>(w), k.x));
-        a.y += f2d(__fmul_rn(static_cast<float>(w), k.y));
+        const double2 kw = to_d(make_float2(__fmul_rn(static_cast<float>(w), k.x), __fmul_rn(static_cast<float>(w), k.y)));
+        a.x += kw.x;
+        a.y += kw.y;
       } else {
         // explicit FMAs, shared with k_fixed_local
         const double2 k = make_double2(-dt * D.x, -dt * D.y);
@@ -357,8 +372,9 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
       double2 v;
       if constexpr (MIX) {
         const float fdt = static_cast<float>(dt);
-        v = make_double2(p.a.x + f2d(__fmul_rn(1.0f / 6.0f, __fmul_rn(-fdt, Dc.x))),
-                         p.a.y + f2d(__fmul_rn(1.0f / 6.0f, __fmul_rn(-fdt, Dc.y))));
+        const double2 k6 = to_d(make_float2(__fmul_rn(1.0f / 6.0f, __fmul_rn(-fdt, Dc.x)),
+                                            __fmul_rn(1.0f / 6.0f, __fmul_rn(-fdt, Dc.y))));
+        v = make_double2(p.a.x + k6.x, p.a.y + k6.y);
       } else {
         const double2 k = make_double2(-dt * D.x, -dt * D.y);
         v = make_double2(fma(1.0 / 6.0, k.x, p.a.x), fma(1.0 / 6.0, k.y, p.a.y));
@@ -374,7 +390,8 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
         const float2 b = st.ls_first ? make_float2(__fmul_rn(-fdt, Dc.x), __fmul_rn(-fdt, Dc.y))
                                      : make_float2(fmaf(-fdt, Dc.x, -p.f.x), fmaf(-fdt, Dc.y, -p.f.y));
         __stcs(reinterpret_cast<float2*>(st.acc) + g, b);
-        const double2 v = make_double2(fma(st.coef, f2d(b.x), p.b.x), fma(st.coef, f2d(b.y), p.b.y));
+        const double2 bd = to_d(b);
+        const double2 v = make_double2(fma(st.coef, bd.x, p.b.x), fma(st.coef, bd.y, p.b.y));
         __stcs(st.S[1 - st.ls_in] + g, v);
         if (st.bulk_separate) st_bulk<TC>(st.Yb[1 - st.ls_in], g, v);
       } else {
@@ -400,9 +417,10 @@ __device__ __forceinline__ double epi_post(const Stage& st, size_t g, cx_t<TC> D
           float2 hi = p.f, lo = p.g;
           ff_add_prod(hi.x, lo.x, c_dpBh[5], c_dpBl[5], k.x);
           ff_add_prod(hi.y, lo.y, c_dpBh[5], c_dpBl[5], k.y);
-          const double2 y = make_double2((p.a.x + f2d(hi.x)) + f2d(lo.x), (p.a.y + f2d(hi.y)) + f2d(lo.y));
+          const double2 hd = to_d(hi), ld = to_d(lo);
+          const double2 y = make_double2((p.a.x + hd.x) + ld.x, (p.a.y + hd.y) + ld.y);
           __stcs(st.S[1 - cur] + g, y);
-          static_cast<float2*>(st.Yb[1 - cur])[g] = make_float2(d2f(y.x), d2f(y.y));
+          static_cast<float2*>(st.Yb[1 - cur])[g] = to_f(y);
         }
       } else {
         const double2 k = make_double2(-dt * D.x, -dt * D.y);

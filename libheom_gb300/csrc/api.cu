@@ -1306,8 +1306,8 @@ void autotune(heomgb_qme_solver* qs) {
       int rt, minb;
       std::vector<int> blocks;
     };
-    std::vector<SV> variants = {{4, 2, {128, 192, 256}}, {2, 3, {128, 192, 256}}, {2, 4, {128, 192, 256}},
-                                {2, 2, {288, 320, 384}}};
+    std::vector<SV> variants = {{4, 2, {128, 192, 224, 256}}, {2, 3, {128, 192, 224, 256}},
+                                {2, 4, {128, 192, 224, 256}}, {2, 2, {288, 320, 352, 384}}};
     if (pin_sb) variants = {{pin_sr, pin_sm, {pin_sb}}};
     for (const SV& v : variants)
       for (int b : v.blocks) {

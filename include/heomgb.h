@@ -204,16 +204,19 @@ heomgb_status heomgb_qme_solver_tuning(const heomgb_qme_solver* qs, int* block, 
  * counterpart: the reference evaluates every term on CUDA cores. */
 heomgb_status heomgb_qme_solver_tensor_cores(const heomgb_qme_solver* qs, int* on);
 /* 1 when the autotuner picked the stage kernel for site-local baths (every V_u
- * diagonal with a single nonzero entry, as in exciton aggregates; n_level a
- * multiple of 4, at least 8; mixed form): per-ADO lists of occupied modes for
- * the -1 terms, the commutator in registers, a compile-time stage epilogue and
- * cp.async-staged tiles; ados_per_tile (may be NULL) receives its tile.
- * HEOMGB_SITES=0 keeps it out of the search, HEOMGB_TILE=sites:<block>x<tile>x<2|3>
- * pins it.  No reference counterpart: heom_hilb::calc_diff_impl
- * (heom_hilb.h:70-215) visits every mode of every ADO. */
+ * diagonal with a single nonzero entry, as in exciton aggregates; real H;
+ * n_level a multiple of 4, at least 8; mixed form): per tile of consecutive
+ * ADOs, the commutator in register blocks, then the bath terms one warp per
+ * ADO over its occupied modes, then a coalesced compile-time stage epilogue;
+ * cp.async-staged tiles.  Same values as the general kernel (bit-identical
+ * states).  ados_per_tile (may be NULL) receives its tile.  HEOMGB_SITES=0
+ * keeps it out of the search, HEOMGB_TILE=sites:<block>x<tile>x<CTAs per
+ * SM>[x<rows 4|2>] pins it.  No reference counterpart:
+ * heom_hilb::calc_diff_impl (heom_hilb.h:70-215) visits every mode of every
+ * ADO. */
 heomgb_status heomgb_qme_solver_site_kernel(const heomgb_qme_solver* qs, int* on, int* ados_per_tile);
 /* 1 when the solver runs each output interval (rkdp, rk4, lsrk4 in the mixed
- * form; rk4 in the FP64 form) as one resident
+ * form; rk4, and rkdp for site-local baths, in the FP64 form) as one resident
  * cooperative launch (one model on the diagonal-coupling path,
  * state held in the CTAs' shared memory between stages), else 0; grid and
  * ados_per_cta (may be NULL) receive its CTAs and the ADOs each owns.

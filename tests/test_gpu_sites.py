@@ -50,6 +50,8 @@ CASES = {
     "agg12_sqrt": lambda: dataclasses.replace(configs.aggregate_24site(n_sites=12, depth=3), normalization="sqrt"),
     "agg8_filtered": lambda: dataclasses.replace(configs.aggregate_24site(n_sites=8, depth=4),
                                                  hrchy_filter=lambda idx, d: idx[0] <= 1 and d <= 3 + (idx[1] == 0)),
+    # n > 32: the bath-term pass's lanes cover a row or column in two rounds
+    "agg36_depth2": lambda: configs.aggregate_24site(n_sites=36, depth=2),
 }
 SOLVES = {
     "rk4": ([0.0, 2.0, 4.0], dict(dt=0.5)),

@@ -1425,7 +1425,7 @@ void plan_resident(heomgb_qme_solver* qs) {
       const int E = apc * I.n2;  // ept elements per thread
       const int block = std::max(64, ((E + ept - 1) / ept + 31) / 32 * 32);
       if (block > kResidentMaxBlock) continue;
-      const int nb = resident_blocks_per_sm(variant, hreal, ept, block, smem);
+      const int nb = resident_blocks_per_sm(variant, hreal, ept, I.n, block, smem);
       if (nb < 1 || static_cast<long long>(nb) * q->n_sm < grid) continue;
       shapes.push_back(Shape{grid, apc, block, ept, smem});
       last_grid = grid;

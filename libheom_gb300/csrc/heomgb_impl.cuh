@@ -225,7 +225,7 @@ size_t resident_dp64_smem(const DiagInst& I, int ados_per_cta);
 const void* resident_dp64_kernel(bool hreal, int ept);
 // smem of a CTA owning ados_per_cta ADOs in the given scheme's kernel
 size_t resident_smem(int n2, int ados_per_cta, int scheme);
-int resident_blocks_per_sm(int scheme, bool hreal, int ept, int block, size_t smem);
+int resident_blocks_per_sm(int scheme, bool hreal, int ept, int n, int block, size_t smem);
 cudaError_t launch_resident(const ResidentArgs& args, int scheme, bool hreal, int ept, int grid, int block,
                             size_t smem, cudaStream_t s);
 

@@ -762,9 +762,13 @@ __device__ __forceinline__ void res_build(const DiagInst& I, const ResAdos& A, i
 
 // Own part of a stage (commutator and damping) for the thread's elements: it
 // reads only this CTA's copy Xs of the stage input (k_rhs_diag's order).
-template <bool HREAL, int EPT>
-__device__ __forceinline__ void res_own(const float2* Hs, const float2* Xs, int n, int n2, int E,
+// NT > 0: the state dimension as a compile-time constant (n = NT; the loop over
+// c unrolled, every index a constant offset), the same arithmetic in the same
+// order as the runtime-n form.
+template <bool HREAL, int EPT, int NT = 0>
+__device__ __forceinline__ void res_own(const float2* Hs, const float2* Xs, int n_rt, int n2_rt, int E,
                                         const ResElems<EPT>& el, float2 (&Dp)[EPT]) {
+  const int n = NT > 0 ? NT : n_rt, n2 = NT > 0 ? NT * NT : n2_rt;
 #pragma unroll
   for (int r = 0; r < EPT; ++r) {
     const int le = threadIdx.x + r * blockDim.x;
@@ -773,7 +777,17 @@ __device__ __forceinline__ void res_own(const float2* Hs, const float2* Xs, int 
     const int lt = el.lt[r], e = el.e[r], a = el.a[r], b = el.b[r];
     const float2* yl = Xs + static_cast<size_t>(lt) * n2;
     float2 acc = make_float2(0.f, 0.f);  // [H, rho]
-    if (HREAL) {
+    if (HREAL && NT > 0) {
+#pragma unroll
+      for (int cc = 0; cc < (NT > 0 ? NT : 1); ++cc) {
+        const float hac = Hs[a * n + cc].x, hcb = Hs[cc * n + b].x;
+        const float2 ycb = yl[cc * n + b], yac = yl[a * n + cc];
+        acc.x = fmaf(hac, ycb.x, acc.x);
+        acc.x = fmaf(-hcb, yac.x, acc.x);
+        acc.y = fmaf(hac, ycb.y, acc.y);
+        acc.y = fmaf(-hcb, yac.y, acc.y);
+      }
+    } else if (HREAL) {
 #pragma unroll 4
       for (int cc = 0; cc < n; ++cc) {
         const float hac = Hs[a * n + cc].x, hcb = Hs[cc * n + b].x;
@@ -824,7 +838,7 @@ __device__ __forceinline__ void res_bath(const float2* Xg, const int* Toff, cons
   }
 }
 
-template <bool HREAL, int EPT>
+template <bool HREAL, int EPT, int NT = 0>
 __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const ResidentArgs R) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ DpCtl c;
@@ -885,7 +899,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
       const float2* Xs = yt + static_cast<size_t>(s & 1) * E;
       float2* Xn = yt + static_cast<size_t>((s + 1) & 1) * E;
       float2 D[EPT];
-      res_own<HREAL, EPT>(Hs, Xs, n, n2, E, el, D);
+      res_own<HREAL, EPT, NT>(Hs, Xs, n, n2, E, el, D);
       // the other CTAs' stage input: wait for their stage s - 1 (stage 1 reads
       // the state copy, complete before the attempt)
       if (s > 0) {
@@ -981,7 +995,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_dp_resident(const Resi
 // inputs Y2, Y3, Y4 and the new state's FP32 copy go through global memory
 // for the neighbour gathers.  Per element the arithmetic is k_rhs_diag's with
 // the mixed form's RK4 epilogues (EPI_RK4_1..4), in the same order.
-template <bool HREAL, int EPT>
+template <bool HREAL, int EPT, int NT = 0>
 __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const ResidentArgs R) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const DiagInst& I = R.inst;
@@ -1017,7 +1031,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident(const Res
       const float2* Xs = yt + static_cast<size_t>(s & 1) * E;
       float2* Xn = yt + static_cast<size_t>((s + 1) & 1) * E;
       float2 D[EPT];
-      res_own<HREAL, EPT>(Hs, Xs, n, n2, E, el, D);
+      res_own<HREAL, EPT, NT>(Hs, Xs, n, n2, E, el, D);
       if (step > 0 || s > 0) {  // the other CTAs' stage input (or new state) of the last stage
         ok = grid_wait(R.bar, gen, R.spin_limit);
         if (!ok) break;
@@ -1251,7 +1265,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_rk4_resident64(const R
 // memory; the new state's FP32 copy goes through global memory (alternating
 // two buffers) for the neighbour gathers.  Same per-element arithmetic as
 // k_rhs_diag with the mixed form's EPI_LS epilogue.
-template <bool HREAL, int EPT>
+template <bool HREAL, int EPT, int NT = 0>
 __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_ls_resident(const ResidentArgs R) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const DiagInst& I = R.inst;
@@ -1285,7 +1299,7 @@ __global__ void __launch_bounds__(kResidentMaxBlock, 2) k_ls_resident(const Resi
       // every thread's reads of Yf (its elements' rows and columns, written by
       // other threads in the epilogue below) end before that epilogue: the grid
       // wait syncs the CTA, and the first stage, which has no wait, syncs here
-      res_own<HREAL, EPT>(Hs, Yf, n, n2, E, el, D);
+      res_own<HREAL, EPT, NT>(Hs, Yf, n, n2, E, el, D);
       if (step > 0 || s > 0) {
         ok = grid_wait(R.bar, gen, R.spin_limit);
         if (!ok) break;
@@ -1333,8 +1347,19 @@ size_t resident_smem(int n2, int ados_per_cta, int scheme) {
 }
 
 // the kernel instance for the scheme, H real or complex and EPT elements per thread
-static const void* resident_kernel(int scheme, bool hreal, int ept) {
+static const void* resident_kernel(int scheme, bool hreal, int ept, int n) {
   if (scheme == kResidentDpF64) return resident_dp64_kernel(hreal, ept);
+  if (hreal && n == 7) {  // compile-time n for the mixed intervals of 7-level systems
+    switch (scheme * 8 + ept) {
+      case 1: return reinterpret_cast<const void*>(k_dp_resident<true, 1, 7>);
+      case 2: return reinterpret_cast<const void*>(k_dp_resident<true, 2, 7>);
+      case 9: return reinterpret_cast<const void*>(k_rk4_resident<true, 1, 7>);
+      case 10: return reinterpret_cast<const void*>(k_rk4_resident<true, 2, 7>);
+      case 17: return reinterpret_cast<const void*>(k_ls_resident<true, 1, 7>);
+      case 18: return reinterpret_cast<const void*>(k_ls_resident<true, 2, 7>);
+      default: break;
+    }
+  }
   switch (scheme * 8 + ept * 2 + (hreal ? 1 : 0)) {
     case 2: return reinterpret_cast<const void*>(k_dp_resident<false, 1>);
     case 3: return reinterpret_cast<const void*>(k_dp_resident<true, 1>);
@@ -1356,8 +1381,8 @@ static const void* resident_kernel(int scheme, bool hreal, int ept) {
   }
 }
 
-int resident_blocks_per_sm(int scheme, bool hreal, int ept, int block, size_t smem) {
-  const void* kern = resident_kernel(scheme, hreal, ept);
+int resident_blocks_per_sm(int scheme, bool hreal, int ept, int n, int block, size_t smem) {
+  const void* kern = resident_kernel(scheme, hreal, ept, n);
   if (!kern) return 0;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
     return 0;
@@ -1368,7 +1393,7 @@ int resident_blocks_per_sm(int scheme, bool hreal, int ept, int block, size_t sm
 
 cudaError_t launch_resident(const ResidentArgs& args, int scheme, bool hreal, int ept, int grid, int block,
                             size_t smem, cudaStream_t s) {
-  const void* kern = resident_kernel(scheme, hreal, ept);
+  const void* kern = resident_kernel(scheme, hreal, ept, args.inst.n);
   if (!kern) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return e;

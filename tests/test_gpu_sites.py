@@ -52,6 +52,9 @@ CASES = {
                                                  hrchy_filter=lambda idx, d: idx[0] <= 1 and d <= 3 + (idx[1] == 0)),
     # n > 32: the bath-term pass's lanes cover a row or column in two rounds
     "agg36_depth2": lambda: configs.aggregate_24site(n_sites=36, depth=2),
+    # the smallest hierarchies: one ADO (no bath terms), and one tier below it
+    "agg8_depth0": lambda: configs.aggregate_24site(n_sites=8, depth=0),
+    "agg8_depth1": lambda: configs.aggregate_24site(n_sites=8, depth=1),
 }
 SOLVES = {
     "rk4": ([0.0, 2.0, 4.0], dict(dt=0.5)),

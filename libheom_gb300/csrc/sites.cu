@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_rhs_sites(const DiagSet ds, cons
       for (int i = 0; i < RT; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = make_float2(0.f, 0.f);
-#pragma unroll 2
+#pragma unroll 4
       for (int c = 0; c < n; ++c) {
         float ha[RT];  // H[a0+i][c]
         if (RT == 4) {

@@ -16,8 +16,21 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "heomgb.h"
 #include "heomgb_impl.cuh"
+
+// NVTX ranges around the host-side phases (model set-up, planning and tile
+// search, solves, output intervals, graph replays): named regions on a
+// profiler's timeline, no-ops without one (the role of the reference's
+// CALL_TRACE stack, utility.h:21-25).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 using cd = std::complex<double>;
 using namespace heomgb;
@@ -1173,6 +1186,7 @@ void alloc_solver(heomgb_qme_solver* qs) {
 // thread (which sets ADOs per tile), timed on right-hand-side launches over
 // the solver's own buffers; the fastest shape is kept for the captured graphs.
 void autotune(heomgb_qme_solver* qs) {
+  const NvtxRange range("heomgb plan: tile search");
   heomgb_qme* q = qs->q;
   std::vector<DiagInst> insts;
   long long off = 0;
@@ -1389,6 +1403,7 @@ void autotune(heomgb_qme_solver* qs) {
 // kept.  HEOMGB_RESIDENT=0 keeps the stage kernels; HEOMGB_RESIDENT_PER_SM
 // and HEOMGB_RESIDENT_EPT pin the shape.
 void plan_resident(heomgb_qme_solver* qs) {
+  const NvtxRange range("heomgb plan: resident interval");
   heomgb_qme* q = qs->q;
   qs->resident = false;
   const int scheme = resident_scheme(qs);
@@ -1502,6 +1517,7 @@ void plan_resident(heomgb_qme_solver* qs) {
 // HEOMGB_LOCAL=0 keeps the other paths, HEOMGB_LOCAL=1 takes the fastest
 // shape without the comparison.
 void plan_local(heomgb_qme_solver* qs) {
+  const NvtxRange range("heomgb plan: instance-resident bins");
   heomgb_qme* q = qs->q;
   qs->local = false;
   if ((qs->kind != HEOMGB_RK4 && qs->kind != HEOMGB_LSRK4) || q->path != PATH_DIAG || qs->term || qs->plan.tcore)
@@ -1747,6 +1763,7 @@ void ensure_graphs(heomgb_qme_solver* qs) {
 }
 
 void replay(heomgb_qme_solver* qs, bool big) {
+  const NvtxRange range(big ? "heomgb replay: 50 steps / 32 attempts" : "heomgb replay: 1 step / 4 attempts");
   ck(cudaGraphLaunch(big ? qs->g_big : qs->g_small, qs->stream), "graph launch");
   const int nodes = big ? qs->nodes_big : qs->nodes_small;
   g_launches += nodes;
@@ -1781,6 +1798,7 @@ double need_kw(const heomgb_kwargs* kw, int has, double v, const char* key) {
 // replays the reference's time loop to get the step sequence (m steps of dt,
 // then the clamped last step), and the device runs it as graph replays.
 void solve_fixed(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwargs* kw) {
+  const NvtxRange range("heomgb interval: fixed steps");
   const double dt = need_kw(kw, kw ? kw->has_dt : 0, kw ? kw->dt : 0, "dt");
   long long m = 0;
   double t = t0, d = dt, last = dt;
@@ -1868,6 +1886,7 @@ void solve_fixed(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwarg
 int solve_adaptive(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwargs* kw, int cur);
 
 int solve_resident(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwargs* kw, int cur) {
+  const NvtxRange range("heomgb interval: resident Dormand-Prince");
   if (qs->dt_save == -1.0) qs->dt_save = need_kw(kw, kw ? kw->has_dt : 0, kw ? kw->dt : 0, "dt");
   const double atol = need_kw(kw, kw ? kw->has_atol : 0, kw ? kw->atol : 0, "atol");
   const double rtol = need_kw(kw, kw ? kw->has_rtol : 0, kw ? kw->rtol : 0, "rtol");
@@ -1910,6 +1929,7 @@ int solve_resident(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwa
 // (adaptive_step_size_solver.h:32-56, rkdp.h:81-179) with the controller on
 // the device; the host only polls the `done` flag between graph replays.
 int solve_adaptive(heomgb_qme_solver* qs, double t0, double t1, const heomgb_kwargs* kw, int cur) {
+  const NvtxRange range("heomgb interval: Dormand-Prince graphs");
   if (qs->dt_save == -1.0) qs->dt_save = need_kw(kw, kw ? kw->has_dt : 0, kw ? kw->dt : 0, "dt");
   const double atol = need_kw(kw, kw ? kw->has_atol : 0, kw ? kw->atol : 0, "atol");
   const double rtol = need_kw(kw, kw ? kw->has_rtol : 0, kw ? kw->rtol : 0, "rtol");
@@ -1952,6 +1972,7 @@ void transpose_instances(heomgb_qme_solver* qs, const double2* in, double2* out)
 
 void solve_impl(heomgb_qme_solver* qs, void* rho, bool host, const double* t_list, int n_t, heomgb_callback cb,
                 void* user, const heomgb_kwargs* kw) {
+  const NvtxRange range("heomgb solve");
   if (!qs) throw arg_error("null qme_solver");
   for (heomgb_qme* m : qs->qmes) need_ready(m);
   if (!rho) throw arg_error("null rho");
@@ -2004,6 +2025,7 @@ void solve_impl(heomgb_qme_solver* qs, void* rho, bool host, const double* t_lis
 }  // namespace
 
 namespace heomgb {
+
 void set_error_message(const std::string& msg) { g_err = msg; }
 }  // namespace heomgb
 
@@ -2161,6 +2183,7 @@ heomgb_status heomgb_qme_set_stream(heomgb_qme* q, void* cuda_stream) {
 
 heomgb_status heomgb_qme_set_param(heomgb_qme* q) {
   return guard([&] {
+    const NvtxRange range("heomgb set_param");
     require(q != nullptr, "null qme");
     build_model(q);
   });
